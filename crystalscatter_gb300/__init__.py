@@ -1,0 +1,316 @@
+"""Python host binding of the GB300 CrystalScatter pixel calculation.
+
+The native library (``_lib/libcrystalscatter.so``, C ABI in
+``include/crystalscatter.h``) does all preparation and computing. This module
+loads it with ctypes and mirrors the public methods of the reference class
+``SasCalc_GENERIC_calculation`` (Source/sc_calc_generic_gpu.h:77-598) with the
+same names and argument meaning, plus the console's key/value entry
+(``--mcpval``). There is no CPU fallback: without the native library or
+without a GPU every calculation raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = [
+    "CsParams", "SasCalc_GENERIC_calculation", "CrystalScatterError", "load_library", "library_path",
+    "CS_MODE_FP64", "CS_MODE_MIXED",
+]
+
+CS_OK = 0
+CS_ERR_PARAM = 1
+CS_ERR_CUDA = 2
+CS_ERR_TIMEOUT = 3
+CS_ERR_UNSUPPORTED = 4
+CS_ERR_ALLOC = 5
+CS_ERR_STATE = 6
+CS_ERR_SIZE = 7
+CS_MODE_FP64 = 0
+CS_MODE_MIXED = 1
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def library_path():
+    return os.path.join(_HERE, "_lib", "libcrystalscatter.so")
+
+
+class CrystalScatterError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+        self.msg = msg
+
+
+_D3 = ctypes.c_double * 3
+
+
+class CsParams(ctypes.Structure):
+    """Mirror of ``cs_params`` (include/crystalscatter.h)."""
+    _fields_ = [
+        ("ltype", ctypes.c_int),
+        ("uca", ctypes.c_double), ("ucb", ctypes.c_double), ("ucc", ctypes.c_double),
+        ("ucalpha", ctypes.c_double), ("ucbeta", ctypes.c_double), ("ucgamma", ctypes.c_double),
+        ("ceff", ctypes.c_double),
+        ("twinned", ctypes.c_int),
+        ("ceffcyl", ctypes.c_double), ("reff", ctypes.c_double), ("acpl", ctypes.c_double),
+        ("bcpl", ctypes.c_double), ("ifluc", ctypes.c_double), ("rfluc", ctypes.c_double),
+        ("particle", ctypes.c_int), ("ordis", ctypes.c_int), ("interior", ctypes.c_int),
+        ("radius", ctypes.c_double), ("radiusi", ctypes.c_double), ("sigma", ctypes.c_double),
+        ("dbeta", ctypes.c_double), ("length", ctypes.c_double), ("sigmal", ctypes.c_double),
+        ("alphash", ctypes.c_double), ("rho", ctypes.c_double), ("alpha", ctypes.c_double),
+        ("peak", ctypes.c_int),
+        ("peakpar", ctypes.c_double), ("debyewaller", ctypes.c_double), ("azi", ctypes.c_double),
+        ("domainsize", ctypes.c_double),
+        ("debyescherrer", ctypes.c_int), ("para", ctypes.c_int),
+        ("ax1", _D3), ("ax2", _D3), ("ax3", _D3), ("sigxyz", _D3),
+        ("ucpsi", ctypes.c_double), ("ucn1", ctypes.c_double), ("ucn2", ctypes.c_double),
+        ("ucn3", ctypes.c_double), ("theta", ctypes.c_double), ("phi", ctypes.c_double),
+        ("rottheta", ctypes.c_double), ("rotphi", ctypes.c_double),
+        ("gridpoints", ctypes.c_int), ("hklmax", ctypes.c_int),
+        ("qmax", ctypes.c_double), ("qmin", ctypes.c_double),
+        ("radq1", ctypes.c_int), ("radq2", ctypes.c_int), ("radq4", ctypes.c_int),
+        ("expand", ctypes.c_int), ("use1d", ctypes.c_int),
+        ("pixnox", ctypes.c_double), ("pixnoy", ctypes.c_double), ("pixx_mm", ctypes.c_double),
+        ("pixy_mm", ctypes.c_double), ("det", ctypes.c_double), ("wavelength", ctypes.c_double),
+        ("beamx", ctypes.c_double), ("beamy", ctypes.c_double),
+        ("usebeamstop", ctypes.c_int),
+        ("bfactor", ctypes.c_double),
+        ("waxs", ctypes.c_int),
+        ("p1", ctypes.c_double),
+        ("iso", ctypes.c_double), ("izero", ctypes.c_double), ("base", ctypes.c_double),
+    ]
+
+
+_lib = None
+
+
+def _sig(lib):
+    H = ctypes.c_void_p
+    P = ctypes.POINTER
+    lib.cs_version.restype = ctypes.c_char_p
+    lib.cs_gpu_available.restype = ctypes.c_int
+    lib.cs_create.restype = H
+    lib.cs_destroy.argtypes = [H]
+    lib.cs_default_params.argtypes = [P(CsParams)]
+    lib.cs_set_params.argtypes = [H, P(CsParams)]
+    lib.cs_get_params.argtypes = [H, P(CsParams)]
+    lib.cs_set_param.argtypes = [H, ctypes.c_char_p, ctypes.c_double]
+    lib.cs_set_param_text.argtypes = [H, ctypes.c_char_p, ctypes.c_char_p]
+    lib.cs_set_kv.argtypes = [H, ctypes.c_char_p]
+    lib.cs_calc_image.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.cs_image_dims.argtypes = [H] + [P(ctypes.c_int)] * 4
+    lib.cs_data.restype = P(ctypes.c_double)
+    lib.cs_data.argtypes = [H]
+    lib.cs_copy_image.argtypes = [H, ctypes.c_void_p, ctypes.c_size_t]
+    lib.cs_timer_ms.restype = ctypes.c_double
+    lib.cs_timer_ms.argtypes = [H, ctypes.c_int]
+    lib.cs_new_switch_used.argtypes = [H]
+    lib.cs_calc_image_device.argtypes = [H, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int]
+    lib.cs_launch_prepared.argtypes = [H, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int]
+    lib.cs_prepared_pixels.argtypes = [H, P(ctypes.c_long)]
+    lib.cs_set_fit_data.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    lib.cs_set_nofit_rect.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.cs_fit_chi2.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P(ctypes.c_double),
+                                P(ctypes.c_long), P(ctypes.c_long)]
+    lib.cs_last_error.restype = ctypes.c_char_p
+    lib.cs_last_error.argtypes = [H]
+    lib.cs_prepared_size.restype = ctypes.c_size_t
+    lib.cs_prepare_params.argtypes = [P(CsParams), ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
+                                      ctypes.c_char_p, ctypes.c_size_t]
+    return lib
+
+
+def load_library(path=None):
+    """Load the native library (built by ``crystalscatter_gb300.build``); raises if absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or library_path()
+    if not os.path.exists(p):
+        raise CrystalScatterError(CS_ERR_CUDA, f"native library not built: {p} (run __graft_entry__.build())")
+    lib = _sig(ctypes.CDLL(p))
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def default_params():
+    p = CsParams()
+    load_library().cs_default_params(ctypes.byref(p))
+    return p
+
+
+def prepare_params(params, ign_new_switch=0, ign_cbs=0):
+    """Host preparation only: returns (status, raw prepared block bytes, message)."""
+    lib = load_library()
+    n = lib.cs_prepared_size()
+    buf = ctypes.create_string_buffer(n)
+    err = ctypes.create_string_buffer(512)
+    rc = lib.cs_prepare_params(ctypes.byref(params), ign_new_switch, ign_cbs, buf, n, err, 512)
+    return rc, buf, err.value.decode()
+
+
+class SasCalc_GENERIC_calculation:
+    """Drop-in for the reference class: setters by group, doCalculation,
+    doFitCalculation, setFitData, setNoFitRect, data()/minX()... ."""
+
+    def __init__(self):
+        self._lib = load_library()
+        self._h = self._lib.cs_create()
+        if not self._h:
+            raise CrystalScatterError(CS_ERR_ALLOC, "cs_create failed")
+        self.higResTimerElapsedPrep = 0.0
+        self.higResTimerElapsedCalc = 0.0
+
+    def __del__(self):
+        self.cleanup()
+
+    def cleanup(self):
+        if getattr(self, "_h", None):
+            self._lib.cs_destroy(self._h)
+            self._h = None
+
+    def _check(self, rc):
+        if rc != CS_OK:
+            raise CrystalScatterError(rc, self._lib.cs_last_error(self._h).decode())
+        return rc
+
+    # ---------------------------------------------------------------- params
+    def params(self):
+        p = CsParams()
+        self._lib.cs_get_params(self._h, ctypes.byref(p))
+        return p
+
+    def set_params(self, p):
+        self._check(self._lib.cs_set_params(self._h, ctypes.byref(p)))
+
+    def setParam(self, key, value):
+        """Reference key (e.g. 'EditRadius', 'ComboBoxParticle') -> number or combobox text."""
+        if isinstance(value, str):
+            return self._check(self._lib.cs_set_param_text(self._h, key.encode(), value.encode()))
+        return self._check(self._lib.cs_set_param(self._h, key.encode(), float(value)))
+
+    def setParams(self, mapping):
+        for k, v in mapping.items():
+            self.setParam(k, v)
+
+    def setKeyValues(self, kv):
+        """The console's ``--mcpval`` string ``"radius=10;cbparticle=sphere;..."``."""
+        self._check(self._lib.cs_set_kv(self._h, kv.encode()))
+
+    # the reference's individual setters (sc_calc_generic_gpu.h:108-353)
+    def setLType(self, v): self.setParam("LType", v)
+    def setUCA(self, v): self.setParam("uca", v)
+    def setUCB(self, v): self.setParam("ucb", v)
+    def setUCC(self, v): self.setParam("ucc", v)
+    def setComboBoxParticle(self, v): self.setParam("ComboBoxParticle", v)
+    def setOrdis(self, v): self.setParam("Ordis", v)
+    def setComboBoxInterior(self, v): self.setParam("ComboBoxInterior", v)
+    def setRadiusF(self, v): self.setParam("EditRadius", v)
+    def setRadiusI(self, v): self.setParam("EditRadiusi", v)
+    def setSigmaF(self, v): self.setParam("EditSigma", v)
+    def setDBetaF(self, v): self.setParam("EditDbeta", v)
+    def setLength(self, v): self.setParam("Length", v)
+    def setSigmaL(self, v): self.setParam("SigmaL", v)
+    def setComboBoxPeak(self, v): self.setParam("ComboBoxPeak", v)
+    def setDisplacement(self, v): self.setParam("EditDebyeWaller", v)
+    def setAzi(self, v): self.setParam("EditAzi", v)
+    def setDomainsize(self, v): self.setParam("EditDomainSize", v)
+    def setRadioButtonDebyeScherrer(self, f): self.setParam("RadButDebyeScherrer", 1 if f else 0)
+    def setPolTheta(self, v): self.setParam("theta", v)
+    def setPolPhi(self, v): self.setParam("phi", v)
+    def setHKLmax(self, v): self.setParam("HKLmax", v)
+    def setGridPoints(self, v, d1=False): self.setParam("GridPoints", v)
+    def setpixnox(self, v): self.setParam("EditPixelNoX", v)
+    def setpixnoy(self, v): self.setParam("EditPixelNoY", v)
+    def setpixx(self, v): self.setParam("EditPixelX", v)
+    def setpixy(self, v): self.setParam("EditPixelY", v)
+    def setdet(self, v): self.setParam("EditDet", v)
+    def setwave(self, v): self.setParam("EditWavelength", v)
+    def setBeamStop(self, x, y):
+        self.setParam("BeamPosX", x)
+        self.setParam("BeamPosY", y)
+    def setUseBeamStop(self, f): self.setParam("CenterBeam", 1 if f else 0)
+    def setIso(self, v): self.setParam("iso", v)
+    def setIZero(self, v): self.setParam("I0", v)
+    def setBase(self, v): self.setParam("Base", v)
+
+    # ------------------------------------------------------------ calculation
+    def doCalculation(self, numThreads=0, bIgnoreNewSwitch=False, bIgnoreCbs=False, mode=CS_MODE_FP64):
+        self._check(self._lib.cs_calc_image(self._h, int(numThreads), int(bool(bIgnoreNewSwitch)),
+                                            int(bool(bIgnoreCbs)), int(mode)))
+        self.higResTimerElapsedPrep = self._lib.cs_timer_ms(self._h, 0)
+        self.higResTimerElapsedCalc = self._lib.cs_timer_ms(self._h, 1)
+
+    def _dims(self):
+        d = [ctypes.c_int() for _ in range(4)]
+        self._lib.cs_image_dims(self._h, *[ctypes.byref(x) for x in d])
+        return [x.value for x in d]
+
+    def minX(self): return self._dims()[0]
+    def maxX(self): return self._dims()[1]
+    def minY(self): return self._dims()[2]
+    def maxY(self): return self._dims()[3]
+
+    def data(self):
+        """The image as a (maxY-minY, maxX-minX) float64 array (copy)."""
+        x0, x1, y0, y1 = self._dims()
+        n = (x1 - x0) * (y1 - y0)
+        out = np.empty(max(n, 0), dtype=np.float64)
+        if n > 0:
+            self._check(self._lib.cs_copy_image(self._h, out.ctypes.data, n))
+        return out.reshape((y1 - y0, x1 - x0)) if n > 0 else out
+
+    def xyIntensity(self, x, y):
+        x0, x1, y0, y1 = self._dims()
+        return float(self.data()[y - y0, x - x0])
+
+    def newSwitchUsed(self):
+        return bool(self._lib.cs_new_switch_used(self._h))
+
+    def getLastErrorMessage(self):
+        return self._lib.cs_last_error(self._h).decode()
+
+    @staticmethod
+    def gpuAvailable():
+        return bool(load_library().cs_gpu_available())
+
+    # -------------------------------------------------------------------- fit
+    def setFitData(self, sx, sy, data):
+        a = np.ascontiguousarray(data, dtype=np.float64).reshape(-1)
+        if a.size != sx * sy:
+            raise CrystalScatterError(CS_ERR_SIZE, "fit data size mismatch")
+        self._check(self._lib.cs_set_fit_data(self._h, int(sx), int(sy), a.ctypes.data))
+        return True
+
+    def setNoFitRect(self, i, x0, y0, x1, y1):
+        self._lib.cs_set_nofit_rect(self._h, i, x0, y0, x1, y1)
+
+    def doFitCalculation(self, numThreads=0, bstop=0, border=0, mode=CS_MODE_FP64):
+        """Returns (chi2, cnt, nancnt); chi2 is 1e20 on failure like the reference."""
+        chi2 = ctypes.c_double()
+        cnt = ctypes.c_long()
+        nan = ctypes.c_long()
+        rc = self._lib.cs_fit_chi2(self._h, int(numThreads), int(bstop), int(border), int(mode),
+                                   ctypes.byref(chi2), ctypes.byref(cnt), ctypes.byref(nan))
+        self._check(rc)
+        return chi2.value, cnt.value, nan.value
+
+    # --------------------------------------------------------- device-resident
+    def calc_device(self, d_out_ptr, n_doubles, stream_ptr=0, bIgnoreNewSwitch=False, bIgnoreCbs=False,
+                    mode=CS_MODE_FP64):
+        self._check(self._lib.cs_calc_image_device(self._h, ctypes.c_void_p(d_out_ptr), n_doubles,
+                                                   ctypes.c_void_p(stream_ptr), int(bool(bIgnoreNewSwitch)),
+                                                   int(bool(bIgnoreCbs)), int(mode)))
+
+    def launch_prepared(self, d_out_ptr, n_doubles, stream_ptr=0, mode=CS_MODE_FP64):
+        self._check(self._lib.cs_launch_prepared(self._h, ctypes.c_void_p(d_out_ptr), n_doubles,
+                                                 ctypes.c_void_p(stream_ptr), int(mode)))
+
+    def prepared_pixels(self):
+        n = ctypes.c_long()
+        self._check(self._lib.cs_prepared_pixels(self._h, ctypes.byref(n)))
+        return n.value

@@ -1,0 +1,540 @@
+// cs_fp64.cuh — FP64 per-pixel functions (the plain GPU drop-in).
+//
+// Device restatement of the reference's pixel path with the reference's
+// operation order, so that results agree with its FP64 CPU path to ~1e-12:
+//   convert_idx2q              Source/sc_calc_generic_gpu.cu:249-287
+//   formpq_partSphere          Source/sc_lib_formpq_partSphere.h:11-196 (cs 0, 1)
+//   formfq_partSphere          Source/sc_lib_formfq_partSphere.h:8-52 (cs 0)
+//   formpq_partCylinder        Source/sc_lib_formpq_partCylinder.h:8-391 (ordis 0, 6; cs 0)
+//   formfq_partCylinder        Source/sc_lib_formfq_partCylinder.h:8-216 (ordis 0, 6; cs 0)
+//   qrombdeltac/trapzddeltac   Source/sc_calc_generic_gpu.cu:1370-1488, 956-1272 (i0 = 4)
+//   qrombchid/trapzdchid       Source/sc_calc_generic_gpu.cu:1495-1583, 1590-2965 (i1 = 1..4)
+//   polint                     Source/sc_calc_generic_gpu.cu:1280-1335
+//   calc_partSphere_lattNone_ordisIsotropic      Source/sc_gpu_pSph_lNon_oIso.h:15-51
+//   calc_partSphere_peakGauss_lattFCC_ordisGauss Source/sc_gpu_pSph_pGau_lFCC_oGau.h:15-171
+//   calc_partCylinder_lattNone_ordisGauss        Source/sc_gpu_pCyl_lNon_oGau.h:15-100
+//   calc_partCylinder_lattNone_ordisZDir         Source/sc_gpu_pCyl_lNon_oZDi.h:17-88
+//   calc_partCylinder_peakGauss_lattBCT_ordisZDir Source/sc_gpu_pCyl_pGau_lBCT_oZDi.h:16-245
+// Quirks of the reference (0-based orcase compared with 1-based integers,
+// the inverted acos clamp, latpar3 read with the isotropic peak index, the
+// misplaced parenthesis in the sphere asymptote) are reproduced on purpose.
+#ifndef CS_FP64_CUH
+#define CS_FP64_CUH
+
+#include "cs_prepared.h"
+#include "cs_tables.h"
+
+namespace cs64 {
+
+#define CS_EPS9 0.000000001
+#define CS_EPS3 0.001
+
+__device__ __forceinline__ double sqr(double x) { return x * x; }
+
+// myacos of the reference (Source/sc_calc_generic_gpu.cu:30): the clamp maps
+// x < -1 to 0 and x > 1 to pi.
+__device__ __forceinline__ double myacos(double x) { return (x < -1) ? 0.0 : ((x > +1) ? M_PI : acos(x)); }
+
+struct Ctx {
+    const cs_prepared *__restrict__ P;
+    const cs_chi_node *__restrict__ chi;     // chi node table (global, levels 1..CS_NODE_LEVELS)
+    const cs_delta_node *__restrict__ dnode; // delta node table of this parameter set (may be null)
+};
+
+__device__ __forceinline__ void convert_idx2q(const cs_prepared &P, int ihex, int i, double &qx, double &qy,
+                                              double &qz) {
+    if (P.use1d) {
+        qx = (P.qmax - P.qmin) / (double)(P.zmax) * (double)ihex;
+        qy = 1e-20;
+        qz = 1e-20;
+    } else if (P.usebeamstop) {
+        double mdet = (ihex)*P.pixnoy / (2.0 * P.zmax);
+        double ndet = (i)*P.pixnox / (2.0 * P.zmax);
+        double xdet = P.pixx_m * (ndet - P.beamx0);
+        double ydet = P.pixy_m * (mdet - P.beamy0);
+        double rdet = sqrt(xdet * xdet + ydet * ydet);
+        double phidet = atan2(ydet, xdet);
+        double thetadet = atan2(rdet, P.det);
+        qx = 2 * M_PI * cos(phidet) * sin(thetadet) / P.wave;
+        qy = 2 * M_PI * sin(phidet) * sin(thetadet) / P.wave;
+        qz = 2 * M_PI * (1 - cos(thetadet)) / P.wave;
+    } else {
+        qx = P.qmax * i / (double)(P.zmax);
+        qy = P.qmax * ihex / (double)(P.zmax);
+        qz = 1e-20;
+    }
+}
+
+// power series 1 + sum_n c[n] (q^2)^n with the reference's qq = qq*q*q
+// and its stop at relative increment < 1e-4 (the loops of the formpq/formfq
+// libraries)
+__device__ __forceinline__ double series_q(const double *__restrict__ c, double q, int nmax) {
+    double pqsum = 1.0;
+    double oldpqsum = 0.0;
+    double qq = 1.0;
+    for (int nser = 1; nser <= nmax; nser++) {
+        qq = qq * q * q;
+        pqsum = pqsum + c[nser] * qq;
+        double delser = fabs((pqsum - oldpqsum) / pqsum);
+        if (delser < 0.0001) break;
+        oldpqsum = pqsum;
+    }
+    return pqsum;
+}
+
+// ------------------------------------------------------------------ spheres
+__device__ double formpq_sphere(const cs_prepared &P, double q) {
+    double zr = (1 - sqr(P.sigma)) / (sqr(P.sigma));
+    const double radiusm = P.radius / P.p1;
+    const double zz = zr;
+    if (P.cs == 0) {
+        if (q < 0.4 * P.limq[4]) {
+            return series_q(P.carrp[3], q, 100);
+        }
+        const double argq = q * P.radius / (zr + 1);
+        if (zr * (zr - 1) * (zr - 2) * (zr - 3) * (zr - 4) * (zr - 5) == 0) zr += CS_EPS3;
+        double pqr = (1 / (2.0 * zr * (zr - 1) * (zr - 2) * (zr - 3))) * pow(argq, -4);
+        const double pq1 = pqr * (1 + cos((zr - 3) * atan(2.0 * argq)) / pow(1.0 + 4 * argq * argq, (zr - 3) / 2.0));
+        const double pq2 = (pqr / ((zr - 4) * argq)) * sin((zr - 4) * atan(2.0 * argq)) / pow(1.0 + 4 * argq * argq, (zr - 4) / 2.0);
+        const double pq3 = (pqr / ((zr - 4) * (zr - 5) * argq * argq)) *
+                           (1 - cos((zr - 5) * atan(2.0 * argq)) / pow(1.0 + 4 * argq * argq, zr - 5) / 2.0);
+        return 9.0 * (pq1 - 2.0 * pq2 + pq3);
+    }
+    if (P.cs == 1) {
+        const double cc1 = sqr(P.rho);
+        const double cc2 = 2 * P.p1 * P.rho * (1 - P.rho);
+        const double cc3 = sqr(1 - P.rho) * sqr(P.p1);
+        const double cc4 = -2 * sqr(P.rho);
+        const double cc5 = -2 * P.p1 * P.rho * (1 - P.rho);
+        const double cc6 = sqr(P.rho);
+        const double cc7 = -2 * P.rho * (1 - P.rho);
+        const double cc8 = -sqr(1 - P.rho) * 2 * P.p1;
+        const double cc9 = 2 * P.rho * (1 - P.rho);
+        const double cc10 = sqr(1 - P.rho);
+        const double ccc1 = sqr(1 - P.rho) * pow(P.p1, 6);
+        const double ccc2 = 2 * P.rho * (1 - P.rho) * pow(P.p1, 3);
+        const double ccc3 = P.rho * P.rho;
+        const double vv3 = sqr((1 - P.rho) * pow(P.p1, 3) + P.rho);
+        const double argq = q * radiusm / (zz + 1);
+        const double argpq = q * P.radius / (zz + 1);
+        const double pqr = (1 / (2.0 * zr * (zr - 1) * (zr - 2) * (zr - 3))) * pow(argq, -4);
+        double F121, F122, F123;
+        if (q < (0.5 * P.limq[4])) {
+            F121 = ccc1 * series_q(P.carrp[3], q, 120) / vv3;
+        } else {
+            const double ac3 = pqr * (1 + cos((zr - 3) * atan(2.0 * argpq)) / pow(1.0 + 4 * argpq * argpq, (zr - 3) / 2.0));
+            const double ac8 = (pqr / ((zr - 4) * argq)) * sin((zr - 4) * atan(2.0 * argpq)) / pow(1.0 + 4 * argpq * argpq, (zr - 4) / 2.0);
+            const double ac10 = (pqr / ((zr - 4) * (zr - 5) * argq * argq)) *
+                                (1 - cos((zr - 5) * atan(2.0 * argpq)) / pow(1.0 + 4 * argpq * argpq, (zr - 5) / 2.0));
+            F121 = 9 * (cc3 * ac3 + cc8 * ac8 + cc10 * ac10) / vv3;
+        }
+        if (q < (0.5 * P.limq[5])) {
+            F122 = ccc2 * series_q(P.carrp[4], q, 120) / vv3;
+        } else {
+            const double argbm = (zr - 3) * atan(argpq - argq);
+            const double nenbm = pow(1.0 + sqr(argpq - argq), (zr - 3) / 2.0);
+            const double argbp = (zr - 3) * atan(argpq + argq);
+            const double nenbp = pow(1.0 + sqr(argpq + argq), (zr - 3) / 2.0);
+            const double ac2 = pqr * (cos(argbm) / nenbm + cos(argbp) / nenbp);
+            const double argep = (zr - 4) * atan(argpq + argq);
+            const double nenep = pow(1.0 + sqr(argpq + argq), (zr - 4) / 2.0);
+            const double argem = (zr - 4) * atan(argpq - argq);
+            const double nenem = pow(1.0 + sqr(argpq - argq), (zr - 4) / 2.0);
+            const double ac5 = (pqr / ((zr - 4) * argq)) * (sin(argep) / nenep - sin(argem) / nenem);
+            const double arggp = (zr - 4) * atan(argpq + argq);
+            const double nengp = pow(1.0 + sqr(argpq + argq), (zr - 4) / 2.0);
+            const double arggm = (zr - 4) * atan(argq - argpq);
+            const double nengm = pow(1.0 + sqr(argq - argpq), (zr - 4) / 2.0);
+            const double ac7 = (pqr / ((zr - 4) * argq)) * (sin(arggp) / nengp - sin(arggm) / nengm);
+            const double ac9 = (pqr / ((zr - 4) * (zr - 5) * argq * argq)) * (cos(argbm) / nenbm - cos(argbp) / nenbp);
+            F122 = 9 * (cc2 * ac2 + cc5 * ac5 + cc7 * ac7 + cc9 * ac9) / vv3;
+        }
+        if (q < (0.5 * P.limq[6])) {
+            F123 = ccc3 * series_q(P.carrp[5], q, 120) / vv3;
+        } else {
+            const double ac1 = pqr * (1 + cos((zr - 3) * atan(2.0 * argq)) / pow(1.0 + 4 * argq * argq, (zr - 3) / 2.0));
+            const double ac4 = (pqr / ((zr - 4) * argq)) * sin((zr - 4) * atan(2.0 * argq)) / pow(1.0 + 4 * argq * argq, (zr - 4) / 2.0);
+            const double ac6 = (pqr / ((zr - 4) * (zr - 5) * argq * argq)) *
+                               (1 - cos((zr - 5) * atan(2.0 * argq)) / pow(1.0 + 4 * argq * argq, (zr - 5) / 2.0));
+            F123 = 9 * (cc1 * ac1 + cc4 * ac4 + cc6 * ac6) / vv3;
+        }
+        return F121 + F122 + F123;
+    }
+    return 0.0;
+}
+
+__device__ double formfq_sphere(const cs_prepared &P, double q) {
+    const double zr = (1 - sqr(P.sigma)) / sqr(P.sigma);
+    if (P.cs == 0) {
+        if (q < (0.4 * P.limqf[4])) {
+            return series_q(P.carrf[3], q, 100);
+        }
+        const double argq = q * P.radius / (zr + 1);
+        const double pqr = (1 / (zr * (zr - 1)) * pow(argq, -2));
+        const double pq1 = pqr * cos((zr - 1) * atan(argq)) / pow(1.0 + argq * argq, (zr - 1) / 2.0);
+        const double pq2 = (pqr / ((zr - 2) * argq)) * sin((zr - 2) * atan(argq)) / pow(1.0 + argq * argq, (zr - 2) / 2.0);
+        const double pq3 = 3 * (pq2 - pq1);
+        return pq3 * pq3;
+    }
+    return 0.0;
+}
+
+// ------------------------------------------------- Romberg orientation average
+// Neville extrapolation to 0 over the last five trapezoid estimates; the
+// abscissae are 1, 1/4, ..., 1/256 times a power of two for every window, which
+// leaves each rounding equal to the reference's.
+__device__ __forceinline__ void polint5(const double ya[5], double &y, double &dy) {
+    const double xa[5] = {1.0, 0.25, 0.0625, 0.015625, 0.00390625};
+    double c[5], d[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) {
+        c[i] = ya[i];
+        d[i] = ya[i];
+    }
+    int ns = 4;  // smallest |xa| is the last one (0-based)
+    y = ya[4];
+    ns = ns - 1;
+#pragma unroll
+    for (int m = 1; m <= 4; m++) {
+#pragma unroll
+        for (int i = 0; i < 5 - m; i++) {
+            double ho = xa[i];
+            double hp = xa[i + m];
+            double w = c[i + 1] - d[i];
+            double den = ho - hp;
+            if (den != 0) den = w / den;
+            d[i] = hp * den;
+            c[i] = ho * den;
+        }
+        // reference (1-based ns1 = ns+1): if 2*ns1 < 5-m then dy=c[ns1+1] else dy=d[ns1], ns1--
+        if (2 * (ns + 1) < 5 - m)
+            dy = c[ns + 1];
+        else {
+            dy = d[ns];
+            ns = ns - 1;
+        }
+        y = y + dy;
+    }
+}
+
+// chi integrand of trapzdchid for the cylinder cases i1 = 1..4; any other i1
+// leaves the integrand 0 (the reference has no branch for orcGeneral = 0).
+struct ChiArgs {
+    double qx, qy, l, z, zp1, a1, zm1, zm1h;
+    double p11, p12, p13, p21, p22, p23;
+    int i1;
+};
+
+__device__ __forceinline__ double chi_integrand(const ChiArgs &A, double cx, double sx, double cd, double sd) {
+    const double eps = 0.0000000001;
+    double argx;
+    switch (A.i1) {
+    case 1: {
+        const double mlx1 = A.p11 * cx * sd + A.p12 * sx * sd + A.p13 * cd;
+        const double mlx2 = A.p21 * sx * sd + A.p22 * cx * sd + A.p23 * cd;
+        argx = (A.qx * mlx1 + A.qy * mlx2 + eps) * A.l / A.zp1;
+        break;
+    }
+    case 2: argx = (A.qx * cd - A.qy * sx * sd + eps) * A.l / A.zp1; break;
+    case 3: argx = (A.qx * sx * sd + A.qy * cd + eps) * A.l / A.zp1; break;
+    case 4: argx = (A.qx * sx * sd - A.qy * cx * sd + eps) * A.l / A.zp1; break;
+    default: return 0.0;
+    }
+    return (A.a1 / (argx * argx)) * (1 - cos(A.zm1 * atan(2.0 * argx)) / pow(1.0 + 4 * argx * argx, A.zm1h));
+}
+
+// qrombchid over chi in [0, chi_b] for one delta node (cd = cos(delta), sd = sin(delta)).
+__device__ double qromb_chi(const Ctx &C, const ChiArgs &A, double cd, double sd) {
+    const double a = 0.0, b = C.P->romb_chi_b;
+    double win[5];
+    double cur;
+    int cnt;
+    double pq = 0.0, dss = 0.0;
+    {
+        const cs_chi_node n0 = C.chi[0], n1 = C.chi[1];
+        double pa = chi_integrand(A, n0.c, n0.s, cd, sd);
+        double pb = chi_integrand(A, n1.c, n1.s, cd, sd);
+        cur = 0.5 * (b - a) * (pa + pb);
+        cnt = 1;
+    }
+    win[4] = cur;
+    for (int j = 2; j <= 20; j++) {
+        const double tnm = cnt;
+        const double del = (b - a) / tnm;
+        double sump = 0.0;
+        if (j <= CS_NODE_LEVELS) {
+            const cs_chi_node *nd = C.chi + CS_NODE_OFFSET(j);
+            for (int k = 0; k < cnt; k++) {
+                const cs_chi_node n = nd[k];
+                sump += chi_integrand(A, n.c, n.s, cd, sd);
+            }
+        } else {
+            double x = a + 0.5 * del;
+            for (int k = 0; k < cnt; k++) {
+                double s, c;
+                sincos(x, &s, &c);
+                sump += chi_integrand(A, c, s, cd, sd);
+                x += del;
+            }
+        }
+        cur = 0.5 * (cur + (b - a) * sump / tnm);
+        cnt = 2 * cnt;
+        win[0] = win[1];
+        win[1] = win[2];
+        win[2] = win[3];
+        win[3] = win[4];
+        win[4] = cur;
+        if (j >= 5) {
+            polint5(win, pq, dss);
+            if (fabs(dss) < (1.0e-4 * fabs(pq))) break;
+            if (fabs(pq) < 1.0e-300) break;
+        }
+    }
+    return pq;
+}
+
+// qrombdeltac(i0 = 4): Gaussian-weighted delta integral of qrombchid.
+__device__ double qromb_delta_cyl(const Ctx &C, const ChiArgs &A) {
+    const cs_prepared &P = *C.P;
+    const double a = 0.0, b = P.romb_delta_b;
+    const double dbeta = P.romb_dbeta;
+    double win[5];
+    double cur;
+    int cnt;
+    double pq = 0.0, dss = 0.0;
+    {
+        const cs_delta_node n0 = C.dnode[0], n1 = C.dnode[1];
+        double pa = qromb_chi(C, A, n0.c, n0.s);
+        double pb = qromb_chi(C, A, n1.c, n1.s);
+        pa = n0.w * pa / (2.0 * M_PI);
+        pb = n1.w * pb / (2.0 * M_PI);
+        cur = 0.5 * (b - a) * (pa + pb);
+        cnt = 1;
+    }
+    win[4] = cur;
+    for (int j = 2; j <= 20; j++) {
+        const double tnm = cnt;
+        const double del = (b - a) / tnm;
+        double sump = 0.0;
+        if (j <= CS_NODE_LEVELS) {
+            const cs_delta_node *nd = C.dnode + CS_NODE_OFFSET(j);
+            for (int k = 0; k < cnt; k++) {
+                const cs_delta_node n = nd[k];
+                double px = qromb_chi(C, A, n.c, n.s);
+                px = n.w * px / (2.0 * M_PI);
+                sump = sump + px;
+            }
+        } else {
+            double x = a + 0.5 * del;
+            for (int k = 0; k < cnt; k++) {
+                double s, c;
+                sincos(x, &s, &c);
+                double px = qromb_chi(C, A, c, s);
+                px = s * exp(-x * x / (dbeta * dbeta)) * px / (2.0 * M_PI);
+                sump = sump + px;
+                x = x + del;
+            }
+        }
+        cur = 0.5 * (cur + (b - a) * sump / tnm);
+        cnt = 2 * cnt;
+        win[0] = win[1];
+        win[1] = win[2];
+        win[2] = win[3];
+        win[3] = win[4];
+        win[4] = cur;
+        if (j >= 5) {
+            polint5(win, pq, dss);
+            if (fabs(dss) < (1.0e-4 * fabs(pq))) break;
+            if (fabs(pq) < 1.0e-100) break;
+        }
+    }
+    return pq;
+}
+
+__device__ __forceinline__ ChiArgs chi_args(const cs_prepared &P, double qxs, double qys, double sigma, int i1) {
+    ChiArgs A;
+    A.qx = qxs;
+    A.qy = qys;
+    A.l = P.length;
+    A.z = (1 - sigma * sigma) / (sigma * sigma);
+    A.zp1 = A.z + 1;
+    A.a1 = 1 / (2.0 * A.z * (A.z - 1));
+    A.zm1 = A.z - 1;
+    A.zm1h = (A.z - 1) / 2.0;
+    A.p11 = P.romb_p[0];
+    A.p12 = P.romb_p[1];
+    A.p13 = P.romb_p[2];
+    A.p21 = P.romb_p[3];
+    A.p22 = P.romb_p[4];
+    A.p23 = P.romb_p[5];
+    A.i1 = i1;
+    return A;
+}
+
+// ---------------------------------------------------------------- cylinders
+// double series of the general orientation (ordis 0, q < 0.4 limq1); the
+// power tables qxn/qyn live in local memory as in the reference.
+__device__ double cyl_double_series(const cs_prepared &P, double qxs, double qys, const double *__restrict__ carr1,
+                                    int variant) {
+    double pql = 1.0;
+    double oldpqsum = 0.0;
+    double qxn[121], qyn[121];
+    qxn[0] = 1.0;
+    qyn[0] = 1.0;
+    for (int nser = 1; nser <= 120; nser++) {
+        qxn[nser] = qxn[nser - 1] * qxs * qxs;
+        qyn[nser] = qyn[nser - 1] * qys * qys;
+        double binsum = 0.0;
+        if (variant == 0) {
+            for (int mser = 0; mser <= nser; mser++) binsum += P.carr11pm[nser - mser][mser] * qxn[mser] * qyn[nser - mser];
+        } else if (variant == 1) {
+            for (int mser = 0; mser <= nser; mser++) binsum += P.carr11pm[nser - mser][mser] * qyn[mser] * qxn[nser - mser];
+        } else if (variant == 2) {
+            for (int mser = 0; mser <= nser; mser++) binsum += P.carr11pm[mser][nser - mser] * qyn[mser] * qxn[nser - mser];
+        } else {
+            for (int mser = 0; mser <= nser; mser++) binsum += P.carr11pm[mser][nser - mser] * qxn[mser] * qyn[nser - mser];
+        }
+        pql += carr1[nser] * binsum;
+        double delser = fabs((pql - oldpqsum) / pql);
+        if (delser < 0.0001) break;
+        oldpqsum = pql;
+    }
+    return pql;
+}
+
+__device__ double formpq_cylinder(const Ctx &C, double qxs, double qys, double q) {
+    const cs_prepared &P = *C.P;
+    double pqr = 0, pql = 0;
+    const double zl = P.sigmal == 1.0 ? CS_EPS9 : (1 - sqr(P.sigmal)) / sqr(P.sigmal);
+    const double zr = P.sigma == 1.0 ? CS_EPS9 : (1 - sqr(P.sigma)) / (sqr(P.sigma));
+    if (P.ordis == 6) {
+        if (P.orcase == 4)
+            pql = 1.0;
+        else {
+            if (q < (0.6 * P.limq[1])) {
+                pql = 1.0;
+                double oldpqsum = 0.0;
+                double qqnn = 1.0;
+                for (int nser = 1; nser <= 120; nser++) {
+                    qqnn = qqnn * (qxs + qys) * (qxs + qys);
+                    pql += P.carrp[0][nser] * qqnn;
+                    const double delser = fabs((pql - oldpqsum) / pql);
+                    if (delser < 0.0001) break;
+                    oldpqsum = pql;
+                }
+            } else {
+                const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
+                pql = (1 / (2.0 * zl * (zl - 1))) * (1 / (arglq * arglq)) *
+                      (1 - cos((zl - 1) * atan(2.0 * arglq)) / pow(1.0 + 4 * arglq * arglq, (zl - 1) / 2.0));
+            }
+        }
+    }
+    if (P.ordis == 0) {
+        if (P.orcase == 4)
+            pql = 1.0;
+        else {
+            if (q < (0.4 * P.limq[1])) {
+                pql = 1.0;
+                // orcase 1 and 2 share one formula, orcase 3 swaps x and y, orcase 0 adds nothing
+                if (P.orcase == 1 || P.orcase == 2)
+                    pql = cyl_double_series(P, qxs, qys, P.carrp[0], 0);
+                else if (P.orcase == 3)
+                    pql = cyl_double_series(P, qxs, qys, P.carrp[0], 1);
+            } else {
+                const ChiArgs A = chi_args(P, qxs, qys, P.sigmal, P.orcase);
+                pql = qromb_delta_cyl(C, A);
+                pql = pql / P.norm;
+            }
+        }
+    }
+    if (P.cs == 0) {
+        if ((P.length / P.radius) < 2)
+            pqr = 1;
+        else {
+            if (q < (0.65 * P.limq[4])) {
+                pqr = series_q(P.carrp[3], q, 120);
+            } else {
+                const double argpq = q * P.radius / (zr + 1);
+                const double pqr1 = (1 / (zr * (zr - 1) * (zr - 2))) * pow(argpq, -3);
+                const double pqr2 = (1 / (zr * (zr - 1) * (zr - 2))) * pow(argpq, -3) * sin((zr - 2) * atan(2.0 * argpq)) /
+                                    pow(1.0 + 4 * argpq * argpq, (zr - 2) / 2.0);
+                const double pqr3 = (1 / (zr * (zr - 1) * (zr - 2) * (zr - 3))) * pow(argpq, -4) *
+                                    cos((zr - 3) * atan(2.0 * argpq)) / pow(1.0 + 4 * argpq * argpq, (zr - 3) / 2.0);
+                pqr = (4. / M_PI) * (pqr1 - pqr2 - (9. / 8.0) * pqr3);
+            }
+        }
+        return pql * pqr;
+    }
+    return 0.0;
+}
+
+__device__ double formfq_cylinder(const Ctx &C, double limql, double qxs, double qys, double q) {
+    const cs_prepared &P = *C.P;
+    const double zl = (1 - sqr(P.sigmal)) / sqr(P.sigmal);
+    const double zr = (1 - sqr(P.sigma)) / sqr(P.sigma);
+    double pql = 0, pqr = 0;
+    if (P.ordis == 6) {
+        if (P.orcase == 4)
+            pql = 1.0;
+        else {
+            if (limql < (0.6 * P.limqf[1])) {
+                double pqsum = 1.0;
+                double oldpqsum = 0.0;
+                double qqnn = 1.0;
+                for (int nser = 1; nser <= 120; nser++) {
+                    qqnn = qqnn * (qxs + qys) * (qxs + qys);
+                    pqsum = pqsum + P.carrf[0][nser] * qqnn;
+                    const double delser = fabs((pqsum - oldpqsum) / pqsum);
+                    if (delser < 0.0001) break;
+                    oldpqsum = pqsum;
+                }
+                pql = pqsum;
+            } else {
+                const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
+                pql = (1 / (2.0 * zl * (zl - 1))) * (1 / (arglq * arglq)) *
+                      (1 - cos((zl - 1) * atan(2.0 * arglq)) / pow(1.0 + 4 * arglq * arglq, (zl - 1) / 2.0));
+            }
+        }
+    }
+    if (P.ordis == 0) {
+        if (P.orcase == 4)
+            pql = 1.0;
+        else {
+            if (limql < (0.2 * P.limqf[1])) {
+                double pqsum = 1.0;
+                if (P.orcase == 1)
+                    pqsum = cyl_double_series(P, qxs, qys, P.carrf[0], 2);
+                if (P.orcase == 2)
+                    pqsum = cyl_double_series(P, qxs, qys, P.carrf[0], 0);
+                if (P.orcase == 3)
+                    pqsum = cyl_double_series(P, qxs, qys, P.carrf[0], 3);
+                pql = pqsum;
+            } else {
+                const ChiArgs A = chi_args(P, qxs, qys, P.sigmal, P.orcase);
+                pql = qromb_delta_cyl(C, A);
+                pql = pql / P.norm;
+            }
+        }
+    }
+    if (P.cs == 0) {
+        if (q < (1.0 * P.limqf[4])) {
+            pqr = series_q(P.carrf[3], q, 120);
+        } else {
+            const double argpq = q * P.radius / (zr + 1);
+            const double pqr1 = P.gamma_ratio[0] * pow(argpq, -3 / 2.0) *
+                                (sin((zr - 1 / 2.0) * atan(argpq)) - cos((zr - 1 / 2.0) * atan(argpq))) /
+                                pow(1.0 + argpq * argpq, (zr - 1 / 2.0) / 2.0);
+            const double pqr2 = P.gamma_ratio[1] * pow(argpq, -5 / 2.0) *
+                                (sin((zr - 3 / 2.0) * atan(argpq)) + cos((zr - 3 / 2.0) * atan(argpq))) /
+                                pow(1.0 + argpq * argpq, (zr - 3 / 2.0) / 2.0);
+            const double pqr3 = (2 / sqrt(M_PI)) * (pqr1 + (9 / 16.0) * pqr2);
+            pqr = pqr3 * pqr3;
+        }
+        return pql * pqr;
+    }
+    return 0.0;
+}
+
+}  // namespace cs64
+
+#endif

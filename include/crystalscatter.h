@@ -1,0 +1,160 @@
+/*
+ * crystalscatter.h — C ABI of the GB300 implementation of CrystalScatter's
+ * per-pixel 2D small-angle scattering pattern calculation.
+ *
+ * The ABI replaces the public surface of the reference class
+ * SasCalc_GENERIC_calculation (Source/sc_calc_generic_gpu.h:77-598) and the
+ * console key/value entry (Source/sc_mainCons.cpp:858-913). Every function
+ * takes plain pointers and sizes; no C++ or CUDA types cross the boundary.
+ * A handle holds one parameter set, its prepared constants, its device
+ * buffers and one CUDA stream. A handle is not thread safe; use one handle per
+ * host thread (the reference itself allows one calculation per process).
+ *
+ * Status codes: every int-returning call returns CS_OK or an error code and
+ * leaves a message in cs_last_error(). Parameter rejections carry exactly the
+ * reference's message text (SasCalc_GENERIC_calculation::checkAllParameters,
+ * Source/sc_calc_generic_cpu.cpp:198-308).
+ */
+#ifndef CRYSTALSCATTER_H
+#define CRYSTALSCATTER_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CS_OK 0
+#define CS_ERR_PARAM 1       /* parameters rejected (reference checkAllParameters / isCbsValid) */
+#define CS_ERR_CUDA 2        /* CUDA runtime error, no usable GPU or extension not loaded */
+#define CS_ERR_TIMEOUT 3     /* a bounded device-side wait gave up */
+#define CS_ERR_UNSUPPORTED 4 /* the reference computes no coefficients for this combination */
+#define CS_ERR_ALLOC 5       /* host or device allocation failed */
+#define CS_ERR_STATE 6       /* call order error (e.g. fit without fit data) */
+#define CS_ERR_SIZE 7        /* caller buffer too small / size limit exceeded */
+
+/* Precision of a calculation. */
+#define CS_MODE_FP64 0  /* plain FP64 GPU drop-in: same operation order as the reference */
+#define CS_MODE_MIXED 1 /* FP32 bulk with FP64 guard bands; <= 1e-5 relative to FP64 */
+
+/* Quadrant selection (reference _radQX, Source/sc_math.h:26-31). */
+#define CS_RAD_Q1 0
+#define CS_RAD_Q2 1
+#define CS_RAD_Q4 2
+
+/*
+ * All parameters of one calculation. Field meaning, units and defaults follow
+ * the reference setters (Source/sc_calc_generic_gpu.h:108-353) and the
+ * console defaults (SC_CalcCons, Source/sc_calcCons.cpp:24-100, 649-668):
+ *   lengths in nm, pixel sizes in mm, distance in m, angles in degrees.
+ * Combobox fields hold the reference's 0-based combobox index
+ * (ComboBoxPeak: 0 = Lorentzian ... 7 = Anisotropic Gaussian; the engine
+ * adds 1 exactly like setComboBoxPeak).
+ */
+typedef struct cs_params {
+    /* Lattice group: setLatticeParams, sc_calc_generic_gpu.h:123-144 */
+    int ltype;
+    double uca, ucb, ucc, ucalpha, ucbeta, ucgamma;
+    double ceff;
+    int twinned;
+    double ceffcyl, reff, acpl, bcpl, ifluc, rfluc;
+    /* Particle group: setParticleParams, sc_calc_generic_gpu.h:192-209 */
+    int particle, ordis, interior;
+    double radius, radiusi, sigma, dbeta, length, sigmal, alphash, rho, alpha;
+    /* Peak shape group: setPeakShapeParams, sc_calc_generic_gpu.h:235-263 */
+    int peak;
+    double peakpar, debyewaller, azi, domainsize;
+    int debyescherrer, para;
+    double ax1[3], ax2[3], ax3[3], sigxyz[3];
+    /* Orientation group: setOrientationParams, sc_calc_generic_gpu.h:274-285 */
+    double ucpsi, ucn1, ucn2, ucn3, theta, phi, rottheta, rotphi;
+    /* Calculation group: setCalculationParams, sc_calc_generic_gpu.h:296-307 */
+    int gridpoints, hklmax;
+    double qmax, qmin;
+    int radq1, radq2, radq4, expand, use1d;
+    /* Experiment group: setExperimentParams, sc_calc_generic_gpu.h:318-330 */
+    double pixnox, pixnoy, pixx_mm, pixy_mm, det, wavelength, beamx, beamy;
+    int usebeamstop; /* "CenterBeam": 1 = beam-centre geometry, 0 = midpoint/qmax */
+    /* Controls group: setControlParams, sc_calc_generic_gpu.h:337-342 */
+    double bfactor;
+    int waxs;
+    double p1;
+    /* Pixel manipulation group: setPixelManipulationParams, sc_calc_generic_gpu.h:348-353 */
+    double iso, izero, base;
+} cs_params;
+
+typedef struct cs_handle cs_handle;
+
+/* Library / device */
+const char *cs_version(void);
+int cs_gpu_available(void); /* 1 when a CUDA device is usable (reference gpuAvailable, sc_calc_generic_gpu.h:441) */
+
+/* Handle lifetime: constructor / cleanup() (sc_calc_generic_cpu.cpp:102, 994) */
+cs_handle *cs_create(void);
+void cs_destroy(cs_handle *h);
+
+/* Parameters */
+void cs_default_params(cs_params *p);                   /* SC_CalcCons defaults */
+int cs_set_params(cs_handle *h, const cs_params *p);    /* grouped set*Params */
+int cs_get_params(cs_handle *h, cs_params *p);
+/* One parameter by the reference's own key (SC_Calc_GENERIC::prepareData keys,
+   Source/sc_calc_generic.cpp:142-238, plus RadioButtonQ1/Q2/Q4, ExpandImage,
+   CenterBeam, EditAxis1x..3z and Editdom1..3 as in SC_CalcCons). Combobox
+   keys take the numeric index. Mirrors SC_CalcCons::updateParamValue
+   (Source/sc_calcCons.cpp:573). */
+int cs_set_param(cs_handle *h, const char *key, double value);
+/* Combobox by text, e.g. ("ComboBoxParticle", "cylinder"); mirrors
+   SC_CalcCons::updateParamValue(QString,QString) (sc_calcCons.cpp:610). */
+int cs_set_param_text(cs_handle *h, const char *key, const char *text);
+/* The console --mcpval string "key=value;key=value" with the lower-case JSON
+   keys of generateJsonKeyList (Source/sc_mainCons.cpp:76-119) and the value
+   rules of calculateFromChatbotKeyValList (sc_mainCons.cpp:858-900). */
+int cs_set_kv(cs_handle *h, const char *kv);
+
+/* Calculation: doCalculation(numThreads, bIgnoreNewSwitch, bIgnoreCbs)
+   (Source/sc_calc_generic_cpu.cpp:1151). num_threads must be 0 (GPU); any
+   other value is rejected: this library has no CPU fallback. The image is
+   kept in the handle's host buffer (data()) and device buffer. */
+int cs_calc_image(cs_handle *h, int num_threads, int ign_new_switch, int ign_cbs, int mode);
+/* Image extents (minX/maxX/minY/maxY, sc_calc_generic_gpu.h:579-582). The
+   image holds (xmax-xmin)*(ymax-ymin) doubles, row-major in y. */
+int cs_image_dims(cs_handle *h, int *xmin, int *xmax, int *ymin, int *ymax);
+const double *cs_data(cs_handle *h); /* data(), valid until the next calculation */
+int cs_copy_image(cs_handle *h, double *out, size_t n_doubles);
+double cs_timer_ms(cs_handle *h, int which); /* 0 = prep (higResTimerElapsedPrep), 1 = calc */
+int cs_new_switch_used(cs_handle *h);        /* newSwitchUsed() */
+
+/* Device-resident variant: prepares on the host, then writes the image into
+   the caller's device buffer d_out (n_doubles capacity) on the caller's CUDA
+   stream (cudaStream_t passed as void*, NULL = the handle's stream). No
+   host<->device copy of the image. Returns after enqueueing (asynchronous). */
+int cs_calc_image_device(cs_handle *h, double *d_out, size_t n_doubles, void *stream, int ign_new_switch,
+                         int ign_cbs, int mode);
+/* Re-launch the last prepared calculation into d_out without host work. */
+int cs_launch_prepared(cs_handle *h, double *d_out, size_t n_doubles, void *stream, int mode);
+int cs_prepared_pixels(cs_handle *h, long *npix);
+
+/* 2D fit support: setFitData (sc_calc_generic_cpu.cpp:8220), setNoFitRect
+   (sc_calc_generic_gpu.h:365), doFitCalculation (sc_calc_generic_cpu.cpp:1334).
+   chi2 = sum of FQSVERGL over unmasked pixels, reduced on the device. */
+int cs_set_fit_data(cs_handle *h, int width, int height, const double *data);
+int cs_set_nofit_rect(cs_handle *h, int id, int x0, int y0, int x1, int y1);
+int cs_fit_chi2(cs_handle *h, int num_threads, int bstop, int border, int mode, double *chi2, long *cnt,
+                long *nancnt);
+
+const char *cs_last_error(cs_handle *h);
+
+/* Host preparation alone, without any CUDA call (the reference's private
+   prepareCalculation, Source/sc_calc_generic_cpu.cpp:319-988): fills the
+   prepared constant block (layout: crystalscatter_gb300/csrc/cs_prepared.h,
+   cs_prepared_size() bytes) for a parameter set, with the quadrant flags of
+   the parameter set applied to the default quadrant state. Used by the test
+   oracle and by tests of the preparation. */
+size_t cs_prepared_size(void);
+int cs_prepare_params(const cs_params *p, int ign_new_switch, int ign_cbs, void *out, size_t out_size, char *err,
+                      size_t errlen);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CRYSTALSCATTER_H */

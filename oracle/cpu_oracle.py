@@ -1,0 +1,101 @@
+"""Python access to the CPU test oracle (oracle/_build/liboracle_cs.so).
+
+TEST INFRASTRUCTURE: the checker for the GPU path and the timed CPU baseline.
+The parameter set is prepared by the library's host preparation
+(cs_prepare_params, no CUDA involved) and then evaluated pixel by pixel by
+the oracle's own restatement of the reference's per-pixel functions.
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+LIB = os.path.join(HERE, "_build", "liboracle_cs.so")
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            from oracle import build_oracle
+            build_oracle.build()
+        lib = ctypes.CDLL(LIB)
+        lib.oracle_image_rows.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        lib.oracle_image_rows.restype = ctypes.c_long
+        lib.oracle_pixel.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        lib.oracle_pixel.restype = ctypes.c_double
+        lib.oracle_supported.argtypes = [ctypes.c_void_p]
+        lib.oracle_fit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_long),
+                                   ctypes.POINTER(ctypes.c_long)]
+        lib.oracle_fit.restype = ctypes.c_double
+        _lib = lib
+    return _lib
+
+
+def prepare(params, ign_cbs=0):
+    """Prepared block (CsPrepared) for a dict of reference keys."""
+    import crystalscatter_gb300 as cs
+    from crystalscatter_gb300 import prepared
+    lib = cs.load_library()
+    h = lib.cs_create()
+    try:
+        for k, v in params.items():
+            if lib.cs_set_param(h, k.encode(), float(v)) != 0:
+                raise KeyError(k)
+        p = cs.CsParams()
+        lib.cs_get_params(h, ctypes.byref(p))
+    finally:
+        lib.cs_destroy(h)
+    rc, P, msg = prepared.prepare(p, 0, ign_cbs)
+    if rc != 0:
+        raise RuntimeError(f"prepare failed ({rc}): {msg}")
+    return P
+
+
+def image(params, ign_cbs=0, nthreads=None, rows=None):
+    """The oracle image for a parameter dict (all rows, or ihex rows [r0,r1))."""
+    P = prepare(params, ign_cbs)
+    lib = load()
+    if not lib.oracle_supported(ctypes.byref(P)):
+        raise RuntimeError("oracle: combination not covered")
+    ny = P.ymax - P.ymin
+    nx = P.xmax - P.xmin
+    out = np.zeros((ny, nx), dtype=np.float64)
+    nt = nthreads or os.cpu_count() or 1
+    r0, r1 = rows if rows else (0, 0)
+    lib.oracle_image_rows(ctypes.byref(P), out.ctypes.data, int(r0), int(r1), int(nt))
+    return out
+
+
+def image_prepared(P, nthreads=None, rows=None):
+    lib = load()
+    out = np.zeros((P.ymax - P.ymin, P.xmax - P.xmin), dtype=np.float64)
+    r0, r1 = rows if rows else (0, 0)
+    n = lib.oracle_image_rows(ctypes.byref(P), out.ctypes.data, int(r0), int(r1), int(nthreads or os.cpu_count() or 1))
+    return out, n
+
+
+def fit(params, target, bstop=0, border=0, nofit=()):
+    """doFitCalculation on the CPU: (chi2, cnt, nancnt, fqs)."""
+    P = prepare(params)
+    target = np.ascontiguousarray(target, dtype=np.float64)
+    h, w = target.shape
+    P.fit_width = w
+    P.fit_height = h
+    P.fit_bstop = bstop
+    P.fit_border = border
+    for i in range(4):
+        r = nofit[i] if i < len(nofit) else (-1, -1, -1, -1)
+        P.nofit_x0[i], P.nofit_y0[i], P.nofit_x1[i], P.nofit_y1[i] = r
+    fqs = np.zeros((h, w), dtype=np.float64)
+    cnt = ctypes.c_long()
+    nan = ctypes.c_long()
+    chi2 = load().oracle_fit(ctypes.byref(P), target.ctypes.data, fqs.ctypes.data, ctypes.byref(cnt), ctypes.byref(nan))
+    return chi2, cnt.value, nan.value, fqs

@@ -1,0 +1,127 @@
+"""ctypes binding of oracle/_ref/libscref.so — the reference's own FP64 CPU
+path compiled from its sources by oracle/build_ref.sh.
+
+TEST INFRASTRUCTURE ONLY: used by tests/ and tests/golden/make_golden.py to
+pin the oracle and to generate golden fixtures. Nothing in the product imports
+it. The library exists only where the reference sources were available at
+build time.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_ref", "libscref.so")
+
+_lib = None
+
+
+def available():
+    return os.path.exists(LIB)
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    lib = ctypes.CDLL(LIB)
+    V = ctypes.c_void_p
+    lib.ref_create.restype = V
+    lib.ref_destroy.argtypes = [V]
+    lib.ref_set.argtypes = [V, ctypes.c_char_p, ctypes.c_double]
+    lib.ref_clear.argtypes = [V]
+    lib.ref_run.argtypes = [V, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.ref_error.restype = ctypes.c_char_p
+    lib.ref_error.argtypes = [V]
+    lib.ref_dims.argtypes = [V] + [ctypes.POINTER(ctypes.c_int)] * 4
+    lib.ref_image.argtypes = [V, ctypes.c_void_p, ctypes.c_long]
+    lib.ref_image.restype = ctypes.c_long
+    lib.ref_timer.argtypes = [V, ctypes.c_int]
+    lib.ref_timer.restype = ctypes.c_double
+    lib.ref_get_array.argtypes = [V, ctypes.c_char_p, ctypes.c_void_p]
+    lib.ref_get_scalar.argtypes = [V, ctypes.c_char_p]
+    lib.ref_get_scalar.restype = ctypes.c_double
+    lib.ref_get_latpar.argtypes = [V, ctypes.c_int, ctypes.c_void_p]
+    lib.ref_set_fit_data.argtypes = [V, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    lib.ref_set_nofit_rect.argtypes = [V] + [ctypes.c_int] * 5
+    lib.ref_fit.argtypes = [V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_long),
+                            ctypes.POINTER(ctypes.c_long)]
+    lib.ref_fit.restype = ctypes.c_double
+    lib.ref_fit_fqs.argtypes = [V, ctypes.c_void_p, ctypes.c_long]
+    lib.ref_fit_fqs.restype = ctypes.c_long
+    _lib = lib
+    return lib
+
+
+class RefCalc:
+    """One reference calculation: parameters by reference key, then run()."""
+
+    def __init__(self, params=None):
+        self.lib = load()
+        self.h = self.lib.ref_create()
+        if params:
+            self.set(params)
+
+    def close(self):
+        if self.h:
+            self.lib.ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def set(self, params):
+        for k, v in params.items():
+            self.lib.ref_set(self.h, k.encode(), float(v))
+
+    def run(self, nthreads=1, ign_new_switch=False, ign_cbs=False):
+        rc = self.lib.ref_run(self.h, int(nthreads), int(ign_new_switch), int(ign_cbs))
+        return rc, self.lib.ref_error(self.h).decode()
+
+    def dims(self):
+        d = [ctypes.c_int() for _ in range(4)]
+        self.lib.ref_dims(self.h, *[ctypes.byref(x) for x in d])
+        return [x.value for x in d]
+
+    def image(self):
+        x0, x1, y0, y1 = self.dims()
+        n = (x1 - x0) * (y1 - y0)
+        out = np.zeros(max(n, 1), dtype=np.float64)
+        if n > 0:
+            self.lib.ref_image(self.h, out.ctypes.data, n)
+        return out[:n].reshape(y1 - y0, x1 - x0) if n > 0 else out[:0]
+
+    def array(self, name):
+        n = 131 * 131 if name.startswith("carr11") or name.startswith("carr22") else 151
+        out = np.zeros(n, dtype=np.float64)
+        self.lib.ref_get_array(self.h, name.encode(), out.ctypes.data)
+        return out
+
+    def scalar(self, name):
+        return self.lib.ref_get_scalar(self.h, name.encode())
+
+    def latpar(self, which):
+        if which == 3:
+            out = np.zeros(2500 * 17, dtype=np.float32)
+        else:
+            out = np.zeros(2500 * 6, dtype=np.int32)
+        self.lib.ref_get_latpar(self.h, which, out.ctypes.data)
+        return out.reshape(2500, -1)
+
+    def timer(self, which):
+        return self.lib.ref_timer(self.h, which)
+
+    def fit(self, data, nthreads=1, bstop=0, border=0, nofit=()):
+        data = np.ascontiguousarray(data, dtype=np.float64)
+        h, w = data.shape
+        self.lib.ref_set_fit_data(self.h, w, h, data.ctypes.data)
+        for i in range(4):
+            r = nofit[i] if i < len(nofit) else (-1, -1, -1, -1)
+            self.lib.ref_set_nofit_rect(self.h, i, *r)
+        cnt = ctypes.c_long()
+        nan = ctypes.c_long()
+        chi2 = self.lib.ref_fit(self.h, int(nthreads), int(bstop), int(border), ctypes.byref(cnt), ctypes.byref(nan))
+        fqs = np.zeros(w * h, dtype=np.float64)
+        self.lib.ref_fit_fqs(self.h, fqs.ctypes.data, w * h)
+        return chi2, cnt.value, nan.value, fqs.reshape(h, w)

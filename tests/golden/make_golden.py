@@ -1,0 +1,151 @@
+"""Generates the golden fixtures in this directory from the reference itself.
+
+Runs the reference's own FP64 CPU path (oracle/_ref/libscref.so, built from
+the reference sources by oracle/build_ref.sh) on small synthetic cases and
+stores, per case: the parameters, the image, the prepared coefficient arrays
+and switch points (known answers for the host preparation), and for fit cases
+the chi^2 sums. Usage (needs the reference sources and the built oracle/_ref):
+
+    python tests/golden/make_golden.py
+
+The cases are the benchmark workloads on coarser grids with the same q-range
+(crystalscatter_gb300.configs.scaled) plus variants that reach other branches
+(quadrant mirroring, midpoint geometry, beam offset, core/shell spheres,
+cylinder orientations, BCT parameter sets) and rejected parameter sets.
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from crystalscatter_gb300 import configs as C  # noqa: E402
+from oracle import refbind  # noqa: E402
+
+ARRAYS = ["carr1p", "carr2p", "carr3p", "carr4p", "carr5p", "carr6p", "carr1f", "carr4f", "carr5f", "carr6f",
+          "carr11pm"]
+SCALARS = ["limq1", "limq2", "limq3", "limq4", "limq5", "limq6", "limq1f", "limq4f", "norm", "order", "orcase",
+           "peakmax1", "peakmax2", "latpar1", "latpar2", "latpar3", "newswitch"]
+
+
+def image_cases():
+    cases = {
+        "sphere_g64": C.scaled(C.SPHERE, 64),
+        "cyl_gauss_g32": C.scaled(C.CYL_GAUSS, 32),
+        "cyl_gauss_x_g24": C.scaled(C.CYL_GAUSS_X, 24),
+        "sphere_fcc_g32": C.scaled(C.SPHERE_FCC, 32),
+        "sphere_fcc_hkl3_g24": dict(C.scaled(C.SPHERE_FCC, 24), HKLmax=3),
+        # quadrant mirroring and geometry variants
+        "sphere_q1_expand_g32": dict(C.scaled(C.SPHERE, 32), RadioButtonQ1=1, RadioButtonQ4=0, ExpandImage=1),
+        "sphere_q2_expand_g32": dict(C.scaled(C.SPHERE, 32), RadioButtonQ2=1, RadioButtonQ4=0, ExpandImage=1),
+        "sphere_q1_noexpand_g32": dict(C.scaled(C.SPHERE, 32), RadioButtonQ1=1, RadioButtonQ4=0, ExpandImage=0),
+        "sphere_midpoint_g32": dict(C.scaled(C.SPHERE, 32), CenterBeam=0, EditQmax=2.0),
+        "sphere_beamoffset_g32": dict(C.scaled(C.SPHERE, 32), BeamPosX=5.5, BeamPosY=-3.0),
+        "sphere_bgiso_g32": dict(C.scaled(C.SPHERE, 32), Base=1e-3, iso=0.25, ifluc=0.1, rfluc=2.0, I0=7.5),
+        "sphere_coreshell_g32": dict(C.scaled(C.SPHERE, 32), ComboBoxInterior=1, EditRadiusi=14.0, EditRho=0.3),
+        "sphere_wide_sigma_g32": dict(C.scaled(C.SPHERE, 32), EditSigma=0.3),
+        # cylinder orientations, no lattice
+        "cyl_gauss_y_g24": dict(C.scaled(C.CYL_GAUSS, 24), phi=90.0),
+        "cyl_gauss_z_g24": dict(C.scaled(C.CYL_GAUSS, 24), theta=0.0, phi=0.0),
+        "cyl_zdir_x_g32": dict(C.scaled(C.CYL_GAUSS, 32), Ordis=6, phi=0.0),
+        "cyl_zdir_y_g32": dict(C.scaled(C.CYL_GAUSS, 32), Ordis=6, phi=90.0),
+        "cyl_zdir_z_g32": dict(C.scaled(C.CYL_GAUSS, 32), Ordis=6, theta=0.0, phi=0.0),
+        "cyl_zdir_gen_g32": dict(C.scaled(C.CYL_GAUSS, 32), Ordis=6, theta=60.0, phi=30.0),
+    }
+    for k in range(4):
+        b = C.bct_set(k)
+        cases[f"cyl_bct_set{k}_g24"] = C.scaled(b, 24)
+    cases["cyl_bct_zaxis_g24"] = dict(C.scaled(C.bct_set(0), 24), theta=0.0, phi=0.0)
+    return cases
+
+
+def ign_cbs_for(p):
+    # cylinder on BCT is rejected by the console's combination check; the
+    # benchmark runs it with bIgnoreCbs (doCalculation(..., bIgnoreCbs=true))
+    return 1 if (p.get("ComboBoxParticle") == 1 and p.get("LType") == 8) else 0
+
+
+def rejected_cases():
+    base = C.scaled(C.SPHERE, 8)
+    return {
+        "uca_small": dict(base, uca=0.005),
+        "ucc_small": dict(base, ucc=0.0),
+        "particle_default": {k: v for k, v in base.items() if k != "ComboBoxParticle"},
+        "cyl_on_bct_checked": dict(C.scaled(C.bct_set(0), 8)),
+        "ltype_invalid": dict(base, LType=25),
+        "peak_invalid": dict(C.scaled(C.SPHERE_FCC, 8), ComboBoxPeak=9),
+    }
+
+
+def main():
+    if not refbind.available():
+        sys.exit("oracle/_ref/libscref.so not built (oracle/build_ref.sh)")
+    out = {}
+    for name, p in image_cases().items():
+        r = refbind.RefCalc(p)
+        ign = ign_cbs_for(p)
+        rc, err = r.run(nthreads=8, ign_cbs=ign)
+        assert rc == 0, (name, err)
+        img = r.image()
+        rec = {"image": img, "dims": np.array(r.dims())}
+        for a in ARRAYS:
+            rec[a] = r.array(a)
+        for s in SCALARS:
+            rec["s_" + s] = np.array(r.scalar(s))
+        if p.get("LType", 12) != 12:
+            pm2 = int(r.scalar("peakmax2"))
+            rec["latpar1"] = r.latpar(1)[: pm2 + 1]
+            rec["latpar2"] = r.latpar(2)[: pm2 + 1]
+            rec["latpar3"] = r.latpar(3)[: pm2 + 1]
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
+        out[name] = {"params": p, "ign_cbs": ign, "shape": list(img.shape),
+                     "nonfinite": int((~np.isfinite(img)).sum()), "zeros": int((img == 0).sum())}
+        print(name, img.shape, "nonfinite", out[name]["nonfinite"], "zeros", out[name]["zeros"])
+        r.close()
+
+    # fit cases: target = reference image * deterministic multiplicative noise
+    fits = {}
+    rng = np.random.default_rng(20261203)
+    p = C.scaled(C.SPHERE, 32)
+    r = refbind.RefCalc(p)
+    r.run(nthreads=8)
+    img = r.image()
+    target = img * (1.0 + 0.05 * rng.standard_normal(img.shape))
+    target[0, 0] = 0.0
+    target[3, 5] = -1.0
+    variants = {
+        "plain": dict(bstop=0, border=0, nofit=()),
+        "border_bstop": dict(bstop=4, border=3, nofit=()),
+        "nofit_rects": dict(bstop=0, border=0, nofit=((2, 2, 10, 12), (30, 40, 50, 60))),
+        "corner_threshold": dict(bstop=-1, border=0, nofit=()),
+    }
+    fit_params = dict(p, EditRadius=10.4)
+    for vname, v in variants.items():
+        rf = refbind.RefCalc(fit_params)
+        chi2, cnt, nan, fqs = rf.fit(target, nthreads=8, bstop=v["bstop"], border=v["border"], nofit=v["nofit"])
+        fits[vname] = {"chi2": chi2, "cnt": cnt, "nancnt": nan, "bstop": v["bstop"], "border": v["border"],
+                       "nofit": [list(x) for x in v["nofit"]]}
+        np.save(os.path.join(HERE, f"fit_{vname}_fqs.npy"), fqs)
+        print("fit", vname, chi2, cnt, nan)
+        rf.close()
+    np.save(os.path.join(HERE, "fit_target.npy"), target)
+
+    rej = {}
+    for name, p in rejected_cases().items():
+        r = refbind.RefCalc(p)
+        rc, err = r.run(nthreads=1)
+        rej[name] = {"params": p, "rc": rc, "error": err, "dims": r.dims()}
+        print("rejected", name, repr(err))
+        r.close()
+
+    with open(os.path.join(HERE, "cases.json"), "w") as f:
+        json.dump({"images": out, "fit": {"params": fit_params, "variants": fits}, "rejected": rej}, f, indent=1,
+                  sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,72 @@
+"""Shared test helpers: golden fixture access and the per-pixel error metric."""
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def golden_cases():
+    with open(os.path.join(GOLDEN, "cases.json")) as f:
+        return json.load(f)
+
+
+def golden(name):
+    return dict(np.load(os.path.join(GOLDEN, f"{name}.npz")))
+
+
+def rel_error(got, ref):
+    """Per-pixel relative error |g-r| / max(|r|, tau), tau = 1e-30 * max|r|.
+
+    Non-finite reference pixels must be matched by the same class (NaN by NaN,
+    +inf by +inf, -inf by -inf); such pixels get error 0 when matched and inf
+    otherwise. Returns (rel array, number of non-finite class mismatches)."""
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    fin = np.isfinite(ref)
+    mism = 0
+    rel = np.zeros(ref.shape)
+    nf = ~fin
+    if nf.any():
+        same = (np.isnan(ref) & np.isnan(got)) | ((ref == got) & np.isinf(ref))
+        mism = int((nf & ~same).sum())
+        rel[nf & ~same] = np.inf
+    gf = fin
+    tau = 1e-30 * (np.max(np.abs(ref[gf])) if gf.any() else 1.0)
+    with np.errstate(invalid="ignore", over="ignore"):
+        d = np.abs(got[gf] - ref[gf]) / np.maximum(np.abs(ref[gf]), tau)
+    d[~np.isfinite(d)] = np.inf
+    rel[gf] = d
+    return rel, mism
+
+
+def params_struct(cs, params):
+    """A cs_params filled like the console: defaults, then reference keys."""
+    import ctypes
+    lib = cs.load_library()
+    h = lib.cs_create()
+    try:
+        for k, v in params.items():
+            rc = lib.cs_set_param(h, k.encode(), float(v))
+            assert rc == 0, (k, lib.cs_last_error(h))
+        p = cs.CsParams()
+        lib.cs_get_params(h, ctypes.byref(p))
+        return p
+    finally:
+        lib.cs_destroy(h)
+
+
+def written_mask(params, shape):
+    """Pixels that the reference actually writes. With quadrant expansion the
+    mirroring never writes column x = -zmax (Q1, Q2) nor row y = -zmax at
+    x < 0 (Q2); the reference leaves whatever the reused image buffer held
+    there (Source/sc_calc_generic_cpu.cpp:1246-1269, checkArrays :8201), so
+    those pixels are excluded from comparisons."""
+    m = np.ones(shape, dtype=bool)
+    if params.get("ExpandImage", 0) and not params.get("RadioButtonQ4", 1):
+        zmax = int(params["GridPoints"])
+        m[:, 0] = False  # x = -zmax
+        if params.get("RadioButtonQ2", 0) and not params.get("RadioButtonQ1", 0):
+            m[0, :zmax] = False  # y = -zmax, x < 0
+    return m
