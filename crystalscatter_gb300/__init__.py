@@ -115,6 +115,7 @@ def _sig(lib):
     lib.cs_set_nofit_rect.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.cs_fit_chi2.argtypes = [H, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P(ctypes.c_double),
                                 P(ctypes.c_long), P(ctypes.c_long)]
+    lib.cs_mixed_redo_pixels.argtypes = [H, P(ctypes.c_long)]
     lib.cs_last_error.restype = ctypes.c_char_p
     lib.cs_last_error.argtypes = [H]
     lib.cs_prepared_size.restype = ctypes.c_size_t
@@ -309,6 +310,11 @@ class SasCalc_GENERIC_calculation:
     def launch_prepared(self, d_out_ptr, n_doubles, stream_ptr=0, mode=CS_MODE_FP64):
         self._check(self._lib.cs_launch_prepared(self._h, ctypes.c_void_p(d_out_ptr), n_doubles,
                                                  ctypes.c_void_p(stream_ptr), int(mode)))
+
+    def mixed_redo_pixels(self):
+        n = ctypes.c_long()
+        self._check(self._lib.cs_mixed_redo_pixels(self._h, ctypes.byref(n)))
+        return n.value
 
     def prepared_pixels(self):
         n = ctypes.c_long()

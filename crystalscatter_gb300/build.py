@@ -18,7 +18,10 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libcrystalscatter.so")
 
 HOST_SOURCES = ["cs_prep.cpp", "cs_params.cpp", "cs_capi.cpp"]
-CUDA_SOURCES = ["cs_kernels.cu"]
+CUDA_SOURCES = ["cs_kernels.cu", "cs_mixed.cu"]
+# the FP64 drop-in keeps the reference's separate multiply and add roundings;
+# the mixed kernels use fused multiply-add
+FMAD = {"cs_kernels.cu": "false", "cs_mixed.cu": "true"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -65,7 +68,7 @@ def build(verbose=False, force=False):
         obj = os.path.join(OUT, f + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([_nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false",
+            jobs.append([_nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=" + FMAD[f],
                          "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills", "-c", src, "-o", obj])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         outs = list(ex.map(_run, jobs))

@@ -1,0 +1,70 @@
+"""Console entry: compute one image on the GPU.
+
+    python -m crystalscatter_gb300.cli --workload cyl_gauss_x --grid 64 --repeat 3
+    python -m crystalscatter_gb300.cli --mcpval "cbparticle=sphere;radius=10;gridpoints=128" --out img.dat
+
+The parameter set is a named workload (crystalscatter_gb300.configs), optionally
+rescaled to another grid with the same q-range, then modified by a console
+``--mcpval`` key/value string (the rules of the console front end,
+Source/sc_mainCons.cpp:858-900). ``--out`` writes the raw image format of the
+reference (Source/widimage.cpp:1480-1500): a 19-byte text header
+"minX maxX minY maxY" (each %4d) followed by the doubles row by row.
+"""
+import argparse
+import json
+import sys
+import time
+
+import numpy as np
+
+from . import CS_MODE_FP64, CS_MODE_MIXED, SasCalc_GENERIC_calculation
+from . import configs as C
+
+
+def write_dat(path, img, x0, x1, y0, y1):
+    header = f"{x0:4d} {x1:4d} {y0:4d} {y1:4d}".encode()
+    with open(path, "wb") as f:
+        f.write(header)
+        f.write(np.ascontiguousarray(img, dtype="<f8").tobytes())
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="sphere", choices=sorted(C.WORKLOADS) + ["bct0"])
+    ap.add_argument("--grid", type=int, default=0, help="GridPoints (half the image edge); 0 = workload size")
+    ap.add_argument("--mcpval", default="", help="console key/value string applied after the workload")
+    ap.add_argument("--mode", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--ign-cbs", action="store_true")
+    ap.add_argument("--out", default="")
+    a = ap.parse_args(argv)
+    params = C.bct_set(0) if a.workload == "bct0" else C.WORKLOADS[a.workload]
+    if a.grid:
+        params = C.scaled(params, a.grid)
+    ign = a.ign_cbs or (params.get("ComboBoxParticle") == 1 and params.get("LType") == 8)
+    calc = SasCalc_GENERIC_calculation()
+    calc.setParams(params)
+    if a.mcpval:
+        calc.setKeyValues(a.mcpval)
+    mode = CS_MODE_MIXED if a.mode == "mixed" else CS_MODE_FP64
+    times = []
+    for _ in range(max(1, a.repeat)):
+        t0 = time.perf_counter()
+        calc.doCalculation(0, False, ign, mode=mode)
+        times.append(time.perf_counter() - t0)
+    img = calc.data()
+    x0, x1, y0, y1 = calc.minX(), calc.maxX(), calc.minY(), calc.maxY()
+    if a.out:
+        write_dat(a.out, img, x0, x1, y0, y1)
+    fin = np.isfinite(img)
+    print(json.dumps({"workload": a.workload, "dims": [x0, x1, y0, y1], "mode": a.mode,
+                      "min": float(img[fin].min()) if fin.any() else None,
+                      "max": float(img[fin].max()) if fin.any() else None,
+                      "nonfinite": int((~fin).sum()), "seconds": times,
+                      "prep_ms": calc.higResTimerElapsedPrep, "calc_ms": calc.higResTimerElapsedCalc}))
+    calc.cleanup()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -10,6 +10,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -19,6 +20,7 @@
 
 #include "../../include/crystalscatter.h"
 #include "cs_launch.h"
+#include "cs_mixed.h"
 #include "cs_params_internal.h"
 #include "cs_prep.h"
 
@@ -43,6 +45,15 @@ struct cs_handle {
     int new_switch = 0;
     bool prepared = false;
     double t_prep = 0, t_calc = 0;
+
+    // mixed-precision path: compact peak tables and the FP64 redo list
+    bool peaks_valid = false;
+    cs::HostPeaks hpeaks;
+    float *d_aq = nullptr, *d_amf = nullptr, *d_iq = nullptr, *d_imf = nullptr;
+    float4 *d_av = nullptr;
+    size_t peak_cap = 0;
+    cs::MixedScratch mscratch;
+    size_t redo_cap = 0;
 
     // fit
     double *dfit = nullptr, *dfqs = nullptr;
@@ -164,6 +175,7 @@ int prepare_and_upload(cs_handle *h, int ign_new_switch, int ign_cbs, int check,
         D.d_delta = h->ddelta;
     }
     cudaEventRecord(h->upload_done, h->stream);
+    h->peaks_valid = false;
     h->t_prep = now_ms() - t0;
     h->xmin = h->hprep->xmin;
     h->xmax = h->hprep->xmax;
@@ -177,6 +189,53 @@ size_t image_count(const cs_handle *h) {
     return (size_t)(h->xmax - h->xmin) * (size_t)(h->ymax - h->ymin);
 }
 
+// Peak tables and redo scratch of the mixed path for the prepared set.
+int ensure_mixed(cs_handle *h) {
+    cudaError_t e;
+    const long npix = (long)(h->hprep->zzmax - h->hprep->zzmin) * (long)(h->hprep->iimax - h->hprep->iimin);
+    if ((size_t)npix > h->redo_cap) {
+        if (h->mscratch.d_list) cudaFree(h->mscratch.d_list);
+        if (!h->mscratch.d_count && (e = cudaMalloc(&h->mscratch.d_count, sizeof(int))) != cudaSuccess)
+            return cuda_fail(h, e, "cudaMalloc(redo count)");
+        if ((e = cudaMalloc(&h->mscratch.d_list, sizeof(int) * (size_t)npix)) != cudaSuccess)
+            return cuda_fail(h, e, "cudaMalloc(redo list)");
+        h->redo_cap = (size_t)npix;
+        h->mscratch.cap = (int)npix;
+    }
+    if (!h->peaks_valid && h->hprep->lattice) {
+        cs::build_peak_tables(*h->hprep, h->hpeaks);
+        const size_t n = std::max(h->hpeaks.aq.size(), h->hpeaks.iq.size()) + 1;
+        if (n > h->peak_cap) {
+            cudaFree(h->d_aq);
+            cudaFree(h->d_amf);
+            cudaFree(h->d_iq);
+            cudaFree(h->d_imf);
+            cudaFree(h->d_av);
+            if ((e = cudaMalloc(&h->d_aq, sizeof(float) * n)) != cudaSuccess ||
+                (e = cudaMalloc(&h->d_amf, sizeof(float) * n)) != cudaSuccess ||
+                (e = cudaMalloc(&h->d_iq, sizeof(float) * n)) != cudaSuccess ||
+                (e = cudaMalloc(&h->d_imf, sizeof(float) * n)) != cudaSuccess ||
+                (e = cudaMalloc(&h->d_av, sizeof(float4) * n)) != cudaSuccess)
+                return cuda_fail(h, e, "cudaMalloc(peak tables)");
+            h->peak_cap = n;
+        }
+        const cs::HostPeaks &H = h->hpeaks;
+        // synchronous copies: the host vectors are rebuilt on the next preparation
+        if (!H.aq.empty()) {
+            cudaMemcpy(h->d_aq, H.aq.data(), sizeof(float) * H.aq.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(h->d_amf, H.amf.data(), sizeof(float) * H.amf.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(h->d_av, H.av.data(), sizeof(float4) * H.av.size(), cudaMemcpyHostToDevice);
+        }
+        if (!H.iq.empty()) {
+            cudaMemcpy(h->d_iq, H.iq.data(), sizeof(float) * H.iq.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(h->d_imf, H.imf.data(), sizeof(float) * H.imf.size(), cudaMemcpyHostToDevice);
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(h, e, "upload peak tables");
+    }
+    h->peaks_valid = true;
+    return CS_OK;
+}
+
 int run_image(cs_handle *h, double *d_out, cudaStream_t s, int mode) {
     cs::DevSet D;
     D.d_prep = h->dprep;
@@ -188,10 +247,25 @@ int run_image(cs_handle *h, double *d_out, cudaStream_t s, int mode) {
         if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync");
     }
     int rc;
-    if (mode == CS_MODE_FP64)
+    if (mode == CS_MODE_FP64) {
         rc = cs::launch_image(D, *h->hprep, d_out, s);
-    else
-        return fail(h, CS_ERR_UNSUPPORTED, "mixed precision mode not available in this build");
+    } else if (mode == CS_MODE_MIXED) {
+        if ((rc = ensure_mixed(h))) return rc;
+        csm::PeakTab T;
+        if (h->hprep->lattice) {
+            T.n_aniso = (int)h->hpeaks.aq.size();
+            T.aq = h->d_aq;
+            T.av = h->d_av;
+            T.amf = h->d_amf;
+            T.n_iso = (int)h->hpeaks.iq.size();
+            T.iq = h->d_iq;
+            T.imf = h->d_imf;
+        }
+        rc = cs::launch_image_mixed(D, T, *h->hprep, d_out, h->mscratch, s);
+        if (rc == CS_ERR_UNSUPPORTED) return fail(h, rc, "no mixed-precision kernel for this combination");
+    } else {
+        return fail(h, CS_ERR_PARAM, "unknown precision mode");
+    }
     if (rc != CS_OK) {
         cudaError_t e = cudaGetLastError();
         return rc == CS_ERR_CUDA ? cuda_fail(h, e, "kernel launch") : fail(h, rc, "no kernel for this combination");
@@ -235,6 +309,13 @@ void cs_destroy(cs_handle *h) {
     if (h->red.d_nan) cudaFree(h->red.d_nan);
     if (h->hprep) cudaFreeHost(h->hprep);
     if (h->hdelta) cudaFreeHost(h->hdelta);
+    cudaFree(h->d_aq);
+    cudaFree(h->d_amf);
+    cudaFree(h->d_iq);
+    cudaFree(h->d_imf);
+    cudaFree(h->d_av);
+    cudaFree(h->mscratch.d_count);
+    cudaFree(h->mscratch.d_list);
     if (h->himg) cudaFreeHost(h->himg);
     if (h->upload_done) cudaEventDestroy(h->upload_done);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -452,6 +533,18 @@ int cs_fit_chi2(cs_handle *h, int num_threads, int bstop, int border, int mode, 
 }
 
 const char *cs_last_error(cs_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+int cs_mixed_redo_pixels(cs_handle *h, long *n) {
+    if (!h || !n) return CS_ERR_PARAM;
+    *n = 0;
+    if (!h->mscratch.d_count) return CS_OK;
+    int v = 0;
+    cudaStreamSynchronize(h->stream);
+    cudaError_t e = cudaMemcpy(&v, h->mscratch.d_count, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(h, e, "read redo count");
+    *n = v;
+    return CS_OK;
+}
 
 // Host preparation alone (prepareCalculation, Source/sc_calc_generic_cpu.cpp:319),
 // without any CUDA call: used by tests and by the CPU oracle to obtain the

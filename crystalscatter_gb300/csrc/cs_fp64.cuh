@@ -83,7 +83,7 @@ __device__ __forceinline__ double series_q(const double *__restrict__ c, double 
 }
 
 // ------------------------------------------------------------------ spheres
-__device__ double formpq_sphere(const cs_prepared &P, double q) {
+__device__ inline double formpq_sphere(const cs_prepared &P, double q) {
     double zr = (1 - sqr(P.sigma)) / (sqr(P.sigma));
     const double radiusm = P.radius / P.p1;
     const double zz = zr;
@@ -163,7 +163,7 @@ __device__ double formpq_sphere(const cs_prepared &P, double q) {
     return 0.0;
 }
 
-__device__ double formfq_sphere(const cs_prepared &P, double q) {
+__device__ inline double formfq_sphere(const cs_prepared &P, double q) {
     const double zr = (1 - sqr(P.sigma)) / sqr(P.sigma);
     if (P.cs == 0) {
         if (q < (0.4 * P.limqf[4])) {
@@ -244,7 +244,7 @@ __device__ __forceinline__ double chi_integrand(const ChiArgs &A, double cx, dou
 }
 
 // qrombchid over chi in [0, chi_b] for one delta node (cd = cos(delta), sd = sin(delta)).
-__device__ double qromb_chi(const Ctx &C, const ChiArgs &A, double cd, double sd) {
+__device__ inline double qromb_chi(const Ctx &C, const ChiArgs &A, double cd, double sd) {
     const double a = 0.0, b = C.P->romb_chi_b;
     double win[5];
     double cur;
@@ -294,7 +294,7 @@ __device__ double qromb_chi(const Ctx &C, const ChiArgs &A, double cd, double sd
 }
 
 // qrombdeltac(i0 = 4): Gaussian-weighted delta integral of qrombchid.
-__device__ double qromb_delta_cyl(const Ctx &C, const ChiArgs &A) {
+__device__ inline double qromb_delta_cyl(const Ctx &C, const ChiArgs &A) {
     const cs_prepared &P = *C.P;
     const double a = 0.0, b = P.romb_delta_b;
     const double dbeta = P.romb_dbeta;
@@ -374,7 +374,7 @@ __device__ __forceinline__ ChiArgs chi_args(const cs_prepared &P, double qxs, do
 // ---------------------------------------------------------------- cylinders
 // double series of the general orientation (ordis 0, q < 0.4 limq1); the
 // power tables qxn/qyn live in local memory as in the reference.
-__device__ double cyl_double_series(const cs_prepared &P, double qxs, double qys, const double *__restrict__ carr1,
+__device__ inline double cyl_double_series(const cs_prepared &P, double qxs, double qys, const double *__restrict__ carr1,
                                     int variant) {
     double pql = 1.0;
     double oldpqsum = 0.0;
@@ -402,7 +402,7 @@ __device__ double cyl_double_series(const cs_prepared &P, double qxs, double qys
     return pql;
 }
 
-__device__ double formpq_cylinder(const Ctx &C, double qxs, double qys, double q) {
+__device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, double q) {
     const cs_prepared &P = *C.P;
     double pqr = 0, pql = 0;
     const double zl = P.sigmal == 1.0 ? CS_EPS9 : (1 - sqr(P.sigmal)) / sqr(P.sigmal);
@@ -468,7 +468,7 @@ __device__ double formpq_cylinder(const Ctx &C, double qxs, double qys, double q
     return 0.0;
 }
 
-__device__ double formfq_cylinder(const Ctx &C, double limql, double qxs, double qys, double q) {
+__device__ inline double formfq_cylinder(const Ctx &C, double limql, double qxs, double qys, double q) {
     const cs_prepared &P = *C.P;
     const double zl = (1 - sqr(P.sigmal)) / sqr(P.sigmal);
     const double zr = (1 - sqr(P.sigma)) / sqr(P.sigma);
@@ -532,6 +532,162 @@ __device__ double formfq_cylinder(const Ctx &C, double limql, double qxs, double
         }
         return pql * pqr;
     }
+    return 0.0;
+}
+
+// calc_partSphere_lattNone_ordisIsotropic, Source/sc_gpu_pSph_lNon_oIso.h:15-51
+__device__ inline double calc_sphere_none_iso(const Ctx &C, double qx, double qy, double qz) {
+    const cs_prepared &P = *C.P;
+    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
+    const double pq = formpq_sphere(P, q);
+    return P.base + P.izero * (pq + P.iso * pq) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+}
+
+// Peak sums shared by the FCC and BCT kernels
+// (Source/sc_gpu_pSph_pGau_lFCC_oGau.h:53-143, sc_gpu_pCyl_pGau_lBCT_oZDi.h:133-211).
+__device__ inline void peak_sums(const cs_prepared &P, double qx, double qy, double qz, double q, double &radintensity,
+                          double &intensity) {
+    double width = 1;
+    if (P.debyescherrer) width = 4.0 / P.domainsize;
+    if (P.para) width = (4.0 / P.domainsize) + sqr(P.reldis) * P.dist * sqr(q);
+    width *= P.width_zuf;
+    const double widthiso = 1.0 / P.uca;
+    radintensity = 0.0;
+    intensity = 0.0;
+    for (int ii = 1; ii <= P.peakmax1; ii++) {
+        const int mhkl = P.latpar1[ii][4];
+        const int fhkl = P.latpar1[ii][5];
+        if (mhkl == 0 || fhkl == 0) continue;
+        const double qhkl = P.latpar3[ii][5];
+        const double x2 = sqr(q - qhkl) / sqr(widthiso);
+        const double sq = exp(-4 * x2 / M_PI) / (M_PI * widthiso / 2.0);
+        radintensity += sq * mhkl * fhkl;
+    }
+    const double x2phi = 4 * q * q / (M_PI * sqr(P.phiwidth));
+    for (int ii = 1; ii <= P.peakmax2; ii++) {
+        const double qhkl = P.latpar3[ii][5];
+        const int mhkl_fhkl = P.latpar2[ii][4] * P.latpar2[ii][5];
+        if (qhkl > 0 && mhkl_fhkl != 0) {
+            const double qxhkl = P.latpar3[ii][2];
+            const double qyhkl = P.latpar3[ii][3];
+            const double qzhkl = P.latpar3[ii][4];
+            const double g3 = P.latpar3[ii][10];
+            const double peaknorm1 = P.latpar3[ii][11];
+            const double yphi = myacos((qx * qxhkl + qy * qyhkl + qz * qzhkl) / (q * qhkl));
+            const double x2 = (q - qhkl) * (q - qhkl) / (width * width);
+            const double sq = exp(-4 * x2 / M_PI) / (M_PI * width / 2.0);
+            double psiord = g3 * exp(-x2phi * yphi * yphi) / peaknorm1;
+            if (P.twin) {
+                const double qxhklt = P.latpar3[ii][7];
+                const double qyhklt = P.latpar3[ii][8];
+                const double qzhklt = P.latpar3[ii][9];
+                const double qhklt = P.latpar3[ii][14];
+                const double g3t = P.latpar3[ii][15];
+                const double peaknorm1t = P.latpar3[ii][16];
+                const double yphit = myacos((qx * qxhklt + qy * qyhklt + qz * qzhklt) / (q * qhklt));
+                const double phiord = g3t * exp(-x2phi * yphit * yphit) / peaknorm1t;
+                psiord = P.ceff * psiord + (1 - P.ceff) * phiord;
+            }
+            const double savintens = intensity;
+            intensity += sq * mhkl_fhkl * psiord;
+            if (isinf(intensity)) {
+                intensity = savintens;
+                break;
+            }
+        }
+    }
+}
+
+// calc_partSphere_peakGauss_lattFCC_ordisGauss, Source/sc_gpu_pSph_pGau_lFCC_oGau.h:15-171
+__device__ inline double calc_sphere_fcc(const Ctx &C, double qx, double qy, double qz) {
+    const cs_prepared &P = *C.P;
+    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
+    const double pq = formpq_sphere(P, q);
+    const double fq = formfq_sphere(P, q);
+    const double pqiso = pq;
+    double radintensity, intensity;
+    peak_sums(P, qx, qy, qz, q, radintensity, intensity);
+    const double sphno_cubevol = P.latpar[1] * P.latpar[2];
+    const double szqiso = (1 + (1) * (8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol) - 1) *
+                                   exp(-P.ucb * q * q));
+    const double szq = (1 + (fq / pq) * (2 * M_PI * intensity / sphno_cubevol - 1) * exp(-P.dwfactor * q * q));
+    return P.base + P.izero * (szq * pq + P.iso * szqiso * pqiso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+}
+
+// calc_partCylinder_lattNone_ordisGauss, Source/sc_gpu_pCyl_lNon_oGau.h:15-100
+// (the lattice branch for F(q) is not taken: lattice is "None").
+__device__ inline double calc_cyl_none_gauss(const Ctx &C, double qx, double qy, double qz) {
+    const cs_prepared &P = *C.P;
+    double pq = 0;
+    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
+    switch (P.orcase) {
+    case CS_ORC_GENERAL:
+        pq = formpq_cylinder(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q);
+        break;
+    case CS_ORC_XAXIS:
+    case CS_ORC_YAXIS:
+    case CS_ORC_ZAXIS:
+        pq = formpq_cylinder(C, qx, qy, q);
+        break;
+    }
+    return P.base + P.izero * (pq + P.iso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+}
+
+// calc_partCylinder_lattNone_ordisZDir, Source/sc_gpu_pCyl_lNon_oZDi.h:17-88
+__device__ inline double calc_cyl_none_zdir(const Ctx &C, double qx, double qy, double qz) {
+    const cs_prepared &P = *C.P;
+    double pq = 0;
+    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
+    switch (P.orcase) {
+    case CS_ORC_GENERAL: pq = formpq_cylinder(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q); break;
+    case CS_ORC_XAXIS: pq = formpq_cylinder(C, qx, 0, q); break;
+    case CS_ORC_YAXIS: pq = formpq_cylinder(C, 0, qy, q); break;
+    case CS_ORC_ZAXIS: pq = formpq_cylinder(C, qx, qy, q); break;
+    }
+    return P.base + P.izero * (pq + P.iso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+}
+
+// calc_partCylinder_peakGauss_lattBCT_ordisZDir, Source/sc_gpu_pCyl_pGau_lBCT_oZDi.h:16-245
+__device__ inline double calc_cyl_bct_zdir(const Ctx &C, double qx, double qy, double qz) {
+    const cs_prepared &P = *C.P;
+    double pq = 0, fq = 0;
+    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
+    const double pqiso = 1;
+    switch (P.orcase) {
+    case CS_ORC_GENERAL:
+        pq = formpq_cylinder(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q);
+        fq = formfq_cylinder(C, sqrt(P.cosphi * qx * qx + P.sinphi * qy * qy + CS_EPS9), qx * P.cosphi * P.sintheta,
+                             qy * P.sinphi * P.sintheta, q);
+        break;
+    case CS_ORC_XAXIS:
+        pq = formpq_cylinder(C, qx, 0, q);
+        fq = formfq_cylinder(C, fabs(qx), qx, 0, q);
+        break;
+    case CS_ORC_YAXIS:
+        pq = formpq_cylinder(C, 0, qy, q);
+        fq = formfq_cylinder(C, fabs(qy), 0, qy, q);
+        break;
+    case CS_ORC_ZAXIS:
+        pq = formpq_cylinder(C, qx, qy, q);
+        fq = formfq_cylinder(C, q, qx, qy, q);
+        break;
+    }
+    double radintensity, intensity;
+    peak_sums(P, qx, qy, qz, q, radintensity, intensity);
+    const double sphno_cubevol = P.latpar[1] * P.latpar[2];
+    const double szqiso = (1 + (1) * (8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol) - 1) *
+                                   exp(-P.ucb * q * q));
+    const double szq = (1 + (fq / pq) * (2 * M_PI * intensity / (sphno_cubevol)-1) * exp(-P.dwfactor * q * q));
+    return P.base + P.izero * (szq * pq + P.iso * szqiso * pqiso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+}
+
+template <int KEY>
+__device__ __forceinline__ double calc_pixel(const Ctx &C, double qx, double qy, double qz) {
+    if (KEY == CS_KEY_SPHERE_NONE_ISO) return calc_sphere_none_iso(C, qx, qy, qz);
+    if (KEY == CS_KEY_SPHERE_GAUSS_FCC_GAUSS) return calc_sphere_fcc(C, qx, qy, qz);
+    if (KEY == CS_KEY_CYL_NONE_GAUSS) return calc_cyl_none_gauss(C, qx, qy, qz);
+    if (KEY == CS_KEY_CYL_NONE_ZDIR) return calc_cyl_none_zdir(C, qx, qy, qz);
+    if (KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR) return calc_cyl_bct_zdir(C, qx, qy, qz);
     return 0.0;
 }
 

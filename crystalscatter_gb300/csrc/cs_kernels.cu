@@ -12,168 +12,9 @@
 
 #include "cs_fp64.cuh"
 #include "cs_launch.h"
+#include "cs_mixed.h"
 
 namespace cs64 {
-
-__device__ __forceinline__ double tail(const cs_prepared &P, double q, double core) {
-    return core + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
-}
-
-// calc_partSphere_lattNone_ordisIsotropic, Source/sc_gpu_pSph_lNon_oIso.h:15-51
-__device__ double calc_sphere_none_iso(const Ctx &C, double qx, double qy, double qz) {
-    const cs_prepared &P = *C.P;
-    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
-    const double pq = formpq_sphere(P, q);
-    return P.base + P.izero * (pq + P.iso * pq) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
-}
-
-// Peak sums shared by the FCC and BCT kernels
-// (Source/sc_gpu_pSph_pGau_lFCC_oGau.h:53-143, sc_gpu_pCyl_pGau_lBCT_oZDi.h:133-211).
-__device__ void peak_sums(const cs_prepared &P, double qx, double qy, double qz, double q, double &radintensity,
-                          double &intensity) {
-    double width = 1;
-    if (P.debyescherrer) width = 4.0 / P.domainsize;
-    if (P.para) width = (4.0 / P.domainsize) + sqr(P.reldis) * P.dist * sqr(q);
-    width *= P.width_zuf;
-    const double widthiso = 1.0 / P.uca;
-    radintensity = 0.0;
-    intensity = 0.0;
-    for (int ii = 1; ii <= P.peakmax1; ii++) {
-        const int mhkl = P.latpar1[ii][4];
-        const int fhkl = P.latpar1[ii][5];
-        if (mhkl == 0 || fhkl == 0) continue;
-        const double qhkl = P.latpar3[ii][5];
-        const double x2 = sqr(q - qhkl) / sqr(widthiso);
-        const double sq = exp(-4 * x2 / M_PI) / (M_PI * widthiso / 2.0);
-        radintensity += sq * mhkl * fhkl;
-    }
-    const double x2phi = 4 * q * q / (M_PI * sqr(P.phiwidth));
-    for (int ii = 1; ii <= P.peakmax2; ii++) {
-        const double qhkl = P.latpar3[ii][5];
-        const int mhkl_fhkl = P.latpar2[ii][4] * P.latpar2[ii][5];
-        if (qhkl > 0 && mhkl_fhkl != 0) {
-            const double qxhkl = P.latpar3[ii][2];
-            const double qyhkl = P.latpar3[ii][3];
-            const double qzhkl = P.latpar3[ii][4];
-            const double g3 = P.latpar3[ii][10];
-            const double peaknorm1 = P.latpar3[ii][11];
-            const double yphi = myacos((qx * qxhkl + qy * qyhkl + qz * qzhkl) / (q * qhkl));
-            const double x2 = (q - qhkl) * (q - qhkl) / (width * width);
-            const double sq = exp(-4 * x2 / M_PI) / (M_PI * width / 2.0);
-            double psiord = g3 * exp(-x2phi * yphi * yphi) / peaknorm1;
-            if (P.twin) {
-                const double qxhklt = P.latpar3[ii][7];
-                const double qyhklt = P.latpar3[ii][8];
-                const double qzhklt = P.latpar3[ii][9];
-                const double qhklt = P.latpar3[ii][14];
-                const double g3t = P.latpar3[ii][15];
-                const double peaknorm1t = P.latpar3[ii][16];
-                const double yphit = myacos((qx * qxhklt + qy * qyhklt + qz * qzhklt) / (q * qhklt));
-                const double phiord = g3t * exp(-x2phi * yphit * yphit) / peaknorm1t;
-                psiord = P.ceff * psiord + (1 - P.ceff) * phiord;
-            }
-            const double savintens = intensity;
-            intensity += sq * mhkl_fhkl * psiord;
-            if (isinf(intensity)) {
-                intensity = savintens;
-                break;
-            }
-        }
-    }
-}
-
-// calc_partSphere_peakGauss_lattFCC_ordisGauss, Source/sc_gpu_pSph_pGau_lFCC_oGau.h:15-171
-__device__ double calc_sphere_fcc(const Ctx &C, double qx, double qy, double qz) {
-    const cs_prepared &P = *C.P;
-    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
-    const double pq = formpq_sphere(P, q);
-    const double fq = formfq_sphere(P, q);
-    const double pqiso = pq;
-    double radintensity, intensity;
-    peak_sums(P, qx, qy, qz, q, radintensity, intensity);
-    const double sphno_cubevol = P.latpar[1] * P.latpar[2];
-    const double szqiso = (1 + (1) * (8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol) - 1) *
-                                   exp(-P.ucb * q * q));
-    const double szq = (1 + (fq / pq) * (2 * M_PI * intensity / sphno_cubevol - 1) * exp(-P.dwfactor * q * q));
-    return P.base + P.izero * (szq * pq + P.iso * szqiso * pqiso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
-}
-
-// calc_partCylinder_lattNone_ordisGauss, Source/sc_gpu_pCyl_lNon_oGau.h:15-100
-// (the lattice branch for F(q) is not taken: lattice is "None").
-__device__ double calc_cyl_none_gauss(const Ctx &C, double qx, double qy, double qz) {
-    const cs_prepared &P = *C.P;
-    double pq = 0;
-    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
-    switch (P.orcase) {
-    case CS_ORC_GENERAL:
-        pq = formpq_cylinder(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q);
-        break;
-    case CS_ORC_XAXIS:
-    case CS_ORC_YAXIS:
-    case CS_ORC_ZAXIS:
-        pq = formpq_cylinder(C, qx, qy, q);
-        break;
-    }
-    return P.base + P.izero * (pq + P.iso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
-}
-
-// calc_partCylinder_lattNone_ordisZDir, Source/sc_gpu_pCyl_lNon_oZDi.h:17-88
-__device__ double calc_cyl_none_zdir(const Ctx &C, double qx, double qy, double qz) {
-    const cs_prepared &P = *C.P;
-    double pq = 0;
-    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
-    switch (P.orcase) {
-    case CS_ORC_GENERAL: pq = formpq_cylinder(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q); break;
-    case CS_ORC_XAXIS: pq = formpq_cylinder(C, qx, 0, q); break;
-    case CS_ORC_YAXIS: pq = formpq_cylinder(C, 0, qy, q); break;
-    case CS_ORC_ZAXIS: pq = formpq_cylinder(C, qx, qy, q); break;
-    }
-    return P.base + P.izero * (pq + P.iso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
-}
-
-// calc_partCylinder_peakGauss_lattBCT_ordisZDir, Source/sc_gpu_pCyl_pGau_lBCT_oZDi.h:16-245
-__device__ double calc_cyl_bct_zdir(const Ctx &C, double qx, double qy, double qz) {
-    const cs_prepared &P = *C.P;
-    double pq = 0, fq = 0;
-    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
-    const double pqiso = 1;
-    switch (P.orcase) {
-    case CS_ORC_GENERAL:
-        pq = formpq_cylinder(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q);
-        fq = formfq_cylinder(C, sqrt(P.cosphi * qx * qx + P.sinphi * qy * qy + CS_EPS9), qx * P.cosphi * P.sintheta,
-                             qy * P.sinphi * P.sintheta, q);
-        break;
-    case CS_ORC_XAXIS:
-        pq = formpq_cylinder(C, qx, 0, q);
-        fq = formfq_cylinder(C, fabs(qx), qx, 0, q);
-        break;
-    case CS_ORC_YAXIS:
-        pq = formpq_cylinder(C, 0, qy, q);
-        fq = formfq_cylinder(C, fabs(qy), 0, qy, q);
-        break;
-    case CS_ORC_ZAXIS:
-        pq = formpq_cylinder(C, qx, qy, q);
-        fq = formfq_cylinder(C, q, qx, qy, q);
-        break;
-    }
-    double radintensity, intensity;
-    peak_sums(P, qx, qy, qz, q, radintensity, intensity);
-    const double sphno_cubevol = P.latpar[1] * P.latpar[2];
-    const double szqiso = (1 + (1) * (8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol) - 1) *
-                                   exp(-P.ucb * q * q));
-    const double szq = (1 + (fq / pq) * (2 * M_PI * intensity / (sphno_cubevol)-1) * exp(-P.dwfactor * q * q));
-    return P.base + P.izero * (szq * pq + P.iso * szqiso * pqiso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
-}
-
-template <int KEY>
-__device__ __forceinline__ double calc_pixel(const Ctx &C, double qx, double qy, double qz) {
-    if (KEY == CS_KEY_SPHERE_NONE_ISO) return calc_sphere_none_iso(C, qx, qy, qz);
-    if (KEY == CS_KEY_SPHERE_GAUSS_FCC_GAUSS) return calc_sphere_fcc(C, qx, qy, qz);
-    if (KEY == CS_KEY_CYL_NONE_GAUSS) return calc_cyl_none_gauss(C, qx, qy, qz);
-    if (KEY == CS_KEY_CYL_NONE_ZDIR) return calc_cyl_none_zdir(C, qx, qy, qz);
-    if (KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR) return calc_cyl_bct_zdir(C, qx, qy, qz);
-    return 0.0;
-}
 
 // Image kernel: pixel (ihex, i) over [zzmin,zzmax) x [iimin,iimax), written at
 // IDX(ihex,i) = (ihex-xmin) + (xmax-xmin)*(i-ymin) (sc_calc_generic_gpu.h:575-578).
@@ -247,6 +88,26 @@ __global__ void __launch_bounds__(256) k_fit(Ctx C, const double *__restrict__ d
             fqs[idx] = d * d;
         } else
             fqs[idx] = 0.0;
+    }
+}
+
+// FP64 recomputation of the pixels that the mixed kernel flagged (list of
+// linear pixel indices t of the calculated region, count on the device).
+template <int KEY>
+__global__ void __launch_bounds__(128) k_redo(Ctx C, double *__restrict__ out, int nx,
+                                              const int *__restrict__ redo_count, const int *__restrict__ redo_list,
+                                              int redo_cap) {
+    const cs_prepared &P = *C.P;
+    const int xstride = P.xmax - P.xmin;
+    int n = *redo_count;
+    if (n > redo_cap) n = redo_cap;
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const long t = redo_list[r];
+        const int ihex = P.zzmin + (int)(t % nx);
+        const int i = P.iimin + (int)(t / nx);
+        double qx, qy, qz;
+        convert_idx2q(P, ihex, i, qx, qy, qz);
+        out[(long)(ihex - P.xmin) + (long)xstride * (long)(i - P.ymin)] = calc_pixel<KEY>(C, qx, qy, qz);
     }
 }
 
@@ -400,12 +261,34 @@ int launch_image(const DevSet &D, const cs_prepared &P, double *d_out, cudaStrea
     case CS_KEY_CYL_GAUSS_BCT_ZDIR: launch_image_key<CS_KEY_CYL_GAUSS_BCT_ZDIR>(D, P, d_out, s); break;
     default: return CS_ERR_UNSUPPORTED;
     }
-    if (P.expand && P.calc_quadrants != CS_RADQ4 && P.calc_quadrants != CS_RAD1D) {
-        const int q1 = P.calc_quadrants == CS_RADQ1;
-        const long total = (long)P.zmax * (q1 ? P.zmax : 2 * P.zmax);
-        k_mirror<<<grid_for(total, 256), 256, 0, s>>>(d_out, P.zmax, P.xmin, P.xmax, P.ymin, q1);
-    }
+    if (P.expand && P.calc_quadrants != CS_RADQ4 && P.calc_quadrants != CS_RAD1D) launch_mirror(P, d_out, s);
     return cudaGetLastError() == cudaSuccess ? CS_OK : CS_ERR_CUDA;
+}
+
+void launch_mirror(const cs_prepared &P, double *d_out, cudaStream_t s) {
+    const int q1 = P.calc_quadrants == CS_RADQ1;
+    const long total = (long)P.zmax * (q1 ? P.zmax : 2 * P.zmax);
+    k_mirror<<<grid_for(total, 256), 256, 0, s>>>(d_out, P.zmax, P.xmin, P.xmax, P.ymin, q1);
+}
+
+template <int KEY>
+static void launch_redo_key(const DevSet &D, const cs_prepared &P, double *d_out, const MixedScratch &S,
+                            cudaStream_t s) {
+    const int nx = P.zzmax - P.zzmin;
+    cs64::Ctx C{D.d_prep, D.d_chi, D.d_delta};
+    cs64::k_redo<KEY><<<sm_count() * 4, 128, 0, s>>>(C, d_out, nx, S.d_count, S.d_list, S.cap);
+}
+
+int launch_redo(const DevSet &D, const cs_prepared &P, double *d_out, const MixedScratch &S, cudaStream_t s) {
+    switch (P.key) {
+    case CS_KEY_SPHERE_NONE_ISO: launch_redo_key<CS_KEY_SPHERE_NONE_ISO>(D, P, d_out, S, s); break;
+    case CS_KEY_SPHERE_GAUSS_FCC_GAUSS: launch_redo_key<CS_KEY_SPHERE_GAUSS_FCC_GAUSS>(D, P, d_out, S, s); break;
+    case CS_KEY_CYL_NONE_GAUSS: launch_redo_key<CS_KEY_CYL_NONE_GAUSS>(D, P, d_out, S, s); break;
+    case CS_KEY_CYL_NONE_ZDIR: launch_redo_key<CS_KEY_CYL_NONE_ZDIR>(D, P, d_out, S, s); break;
+    case CS_KEY_CYL_GAUSS_BCT_ZDIR: launch_redo_key<CS_KEY_CYL_GAUSS_BCT_ZDIR>(D, P, d_out, S, s); break;
+    default: return CS_ERR_UNSUPPORTED;
+    }
+    return CS_OK;
 }
 
 template <int KEY>

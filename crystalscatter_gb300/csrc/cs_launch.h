@@ -31,7 +31,6 @@ bool key_supported(const cs_prepared &P);
 bool needs_delta_table(const cs_prepared &P);
 
 int launch_image(const DevSet &D, const cs_prepared &P, double *d_out, cudaStream_t s);
-int launch_image_mixed(const DevSet &D, const cs_prepared &P, double *d_out, cudaStream_t s);
 int launch_fit(const DevSet &D, const cs_prepared &P, const double *d_data, double *d_fqs, long nbuf, FitReduce &R,
                cudaStream_t s);
 

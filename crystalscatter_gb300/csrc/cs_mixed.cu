@@ -1,0 +1,674 @@
+// cs_mixed.cu — mixed-precision pixel kernels (CS_MODE_MIXED).
+//
+// GB300 executes FP64 at a small fraction of its FP32 rate, so the bulk of the
+// per-pixel work runs in FP32 here, with FP64 kept where the reference's
+// numerics need it:
+//   * FP64: detector geometry q, the small-qR Schulz-Zimm power series of
+//     P(q)/F(q) (alternating series with cancellation up to 1e9 near their
+//     switch points), the Romberg extrapolation (polint) and every stop/branch
+//     decision, the final combination of the structure factor.
+//   * FP32: the large-qR asymptotes, the lattice peak sums (compensated
+//     accumulation, radial distance from a float-float q), the orientation
+//     quadrature integrand (with a Taylor form where its closed form cancels)
+//     and the trapezoid sums (compensated).
+// A pixel whose FP64 decision lies within a guard band of its threshold (where
+// FP32 rounding could flip the reference's discrete choice: series vs.
+// asymptote, Romberg convergence) is flagged; a second kernel recomputes the
+// flagged pixels with the FP64 drop-in functions. The image written is then
+// within ~1e-6 of the FP64 path everywhere (bar <= 1e-5).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "cs_fp64.cuh"
+#include "cs_launch.h"
+#include "cs_mixed.h"
+
+namespace csm {
+
+using cs64::Ctx;
+
+#define LOG2E_F 1.4426950408889634f
+
+// (1+x)^e for x >= 0 in FP32 via log1p (no rounding of 1+x)
+__device__ __forceinline__ float powp1f(float x, float e) { return exp2f(e * log1pf(x) * LOG2E_F); }
+
+// decision guard: true when v is within `band` relative of threshold t
+__device__ __forceinline__ bool near(double v, double t, double band) { return fabs(v - t) <= band * fabs(t); }
+
+// Detector geometry in FP64 without transcendentals: cos(phi)sin(theta) =
+// xdet/L, sin(phi)sin(theta) = ydet/L, cos(theta) = det/L, L = |(xdet,ydet,det)|.
+// Agrees with the reference's atan2/sin/cos form to a few ulp.
+__device__ __forceinline__ void q_of_pixel(const cs_prepared &P, int ihex, int i, double &qx, double &qy, double &qz) {
+    if (P.use1d || !P.usebeamstop) {
+        cs64::convert_idx2q(P, ihex, i, qx, qy, qz);
+        return;
+    }
+    const double mdet = (ihex)*P.pixnoy / (2.0 * P.zmax);
+    const double ndet = (i)*P.pixnox / (2.0 * P.zmax);
+    const double xdet = P.pixx_m * (ndet - P.beamx0);
+    const double ydet = P.pixy_m * (mdet - P.beamy0);
+    const double r2 = xdet * xdet + ydet * ydet;
+    const double L = sqrt(r2 + P.det * P.det);
+    const double k = 2 * M_PI / P.wave;
+    qx = k * xdet / L;
+    qy = k * ydet / L;
+    // 1 - cos(theta) = r^2 / (L (L + det)), free of cancellation
+    qz = k * r2 / (L * (L + P.det));
+}
+
+// ---------------------------------------------------------------- asymptotes
+// sphere P(q), q >= 0.4 limq4 (Source/sc_lib_formpq_partSphere.h:263-269)
+__device__ float sphere_pq_asym(float argq, float zr) {
+    const float t = atanf(2.0f * argq);
+    const float x2 = 4.0f * argq * argq;
+    const float pqr = (1.0f / (2.0f * zr * (zr - 1) * (zr - 2) * (zr - 3))) / (argq * argq * argq * argq);
+    const float pq1 = pqr * (1 + cosf((zr - 3) * t) / powp1f(x2, (zr - 3) / 2.0f));
+    const float pq2 = (pqr / ((zr - 4) * argq)) * sinf((zr - 4) * t) / powp1f(x2, (zr - 4) / 2.0f);
+    // the reference divides by 2 outside the pow (reproduced)
+    const float pq3 = (pqr / ((zr - 4) * (zr - 5) * argq * argq)) * (1 - cosf((zr - 5) * t) / powp1f(x2, zr - 5) / 2.0f);
+    return 9.0f * (pq1 - 2.0f * pq2 + pq3);
+}
+
+// sphere F(q), q >= 0.4 limq4f (Source/sc_lib_formfq_partSphere.h:443-448)
+__device__ float sphere_fq_asym(float argq, float zr) {
+    const float t = atanf(argq);
+    const float x2 = argq * argq;
+    const float pqr = 1.0f / (zr * (zr - 1)) / (argq * argq);
+    const float pq1 = pqr * cosf((zr - 1) * t) / powp1f(x2, (zr - 1) / 2.0f);
+    const float pq2 = (pqr / ((zr - 2) * argq)) * sinf((zr - 2) * t) / powp1f(x2, (zr - 2) / 2.0f);
+    const float pq3 = 3 * (pq2 - pq1);
+    return pq3 * pq3;
+}
+
+// cylinder cross-section P(q), q >= 0.65 limq4 (Source/sc_lib_formpq_partCylinder.h:271-275)
+__device__ float cyl_pqr_asym(float argpq, float zr) {
+    const float t = atanf(2.0f * argpq);
+    const float x2 = 4.0f * argpq * argpq;
+    const float a3 = argpq * argpq * argpq;
+    const float pqr1 = (1.0f / (zr * (zr - 1) * (zr - 2))) / a3;
+    const float pqr2 = pqr1 * sinf((zr - 2) * t) / powp1f(x2, (zr - 2) / 2.0f);
+    const float pqr3 = (1.0f / (zr * (zr - 1) * (zr - 2) * (zr - 3))) / (a3 * argpq) * cosf((zr - 3) * t) /
+                       powp1f(x2, (zr - 3) / 2.0f);
+    return (4.0f / (float)M_PI) * (pqr1 - pqr2 - (9.0f / 8.0f) * pqr3);
+}
+
+// Length factor of the Schulz cylinder P(q) along its axis,
+//   (1/(2z(z-1) a^2)) (1 - cos((z-1) atan 2a) / (1+4a^2)^((z-1)/2)),
+// which tends to 1 for a -> 0 with cancellation in the bracket. With m = z-1
+// the bracket is 1 - Re (1+2ia)^(-m) = -sum_{j>=1} C(m+2j-1, 2j) (-4a^2)^j, so
+// for small m*a the function is the series 1 - (m+3)(m+2)/3 a^2 + ... obtained
+// from the term ratio below; otherwise the closed form is used.
+__device__ float cyl_len_factor(float a, float z) {
+    const float m = z - 1.0f;
+    if (fabsf(m * a) < 0.35f) {
+        // P = sum_j T_j with T_0 = 1, T_j/T_(j-1) = -4a^2 (m+2j)(m+2j+1)/((2j+1)(2j+2))
+        const float x = -4.0f * a * a;
+        float term = 1.0f, sum = 1.0f;
+#pragma unroll
+        for (int j = 1; j <= 9; j++) {
+            term *= x * (m + 2 * j) * (m + 2 * j + 1) / ((2 * j + 1) * (2 * j + 2));
+            sum += term;
+        }
+        return sum;
+    }
+    const float a1 = 1.0f / (2.0f * z * m);
+    return (a1 / (a * a)) * (1.0f - cosf(m * atanf(2.0f * a)) / powp1f(4.0f * a * a, m / 2.0f));
+}
+
+// ------------------------------------------------------ compensated addition
+struct Kahan {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// ------------------------------------------------------- FP32 Romberg (chi)
+struct ChiArgsF {
+    float qx, qy, lz;  // lz = l/(z+1)
+    float z;
+    float p11, p12, p13, p21, p22, p23;
+    int i1;
+};
+
+__device__ __forceinline__ float chi_integrand_f(const ChiArgsF &A, float cx, float sx, float cd, float sd) {
+    const float eps = 1e-10f;
+    float s;
+    switch (A.i1) {
+    case 1: {
+        const float mlx1 = A.p11 * cx * sd + A.p12 * sx * sd + A.p13 * cd;
+        const float mlx2 = A.p21 * sx * sd + A.p22 * cx * sd + A.p23 * cd;
+        s = A.qx * mlx1 + A.qy * mlx2 + eps;
+        break;
+    }
+    case 2: s = A.qx * cd - A.qy * sx * sd + eps; break;
+    case 3: s = A.qx * sx * sd + A.qy * cd + eps; break;
+    case 4: s = A.qx * sx * sd - A.qy * cx * sd + eps; break;
+    default: return 0.0f;
+    }
+    return cyl_len_factor(s * A.lz, A.z);
+}
+
+// Romberg convergence test of the reference in FP64 on the FP32-accurate
+// estimates; `guard` flags a decision inside the band where FP32 rounding of
+// the estimates could change it.
+__device__ __forceinline__ bool romb_stop(const double win[5], double &pq, double tiny, bool &guard) {
+    double dss;
+    cs64::polint5(win, pq, dss);
+    const double lhs = fabs(dss), rhs = 1.0e-4 * fabs(pq);
+    if (fabs(lhs - rhs) <= 3e-3 * rhs + 1e-300) guard = true;
+    if (lhs < rhs) return true;
+    if (fabs(pq) < tiny) return true;
+    return false;
+}
+
+__device__ double qromb_chi_f(const Ctx &C, const ChiArgsF &A, float cd, float sd, bool &guard) {
+    const double b = C.P->romb_chi_b;
+    double win[5];
+    double cur;
+    int cnt;
+    double pq = 0.0;
+    {
+        const cs_chi_node n0 = C.chi[0], n1 = C.chi[1];
+        const float pa = chi_integrand_f(A, (float)n0.c, (float)n0.s, cd, sd);
+        const float pb = chi_integrand_f(A, (float)n1.c, (float)n1.s, cd, sd);
+        cur = 0.5 * b * ((double)pa + (double)pb);
+        cnt = 1;
+    }
+    win[4] = cur;
+    for (int j = 2; j <= 20; j++) {
+        Kahan sum;
+        if (j <= CS_NODE_LEVELS) {
+            const cs_chi_node *nd = C.chi + CS_NODE_OFFSET(j);
+            for (int k = 0; k < cnt; k++) {
+                const cs_chi_node n = nd[k];
+                sum.add(chi_integrand_f(A, (float)n.c, (float)n.s, cd, sd));
+            }
+        } else {
+            const double del = b / cnt;
+            double x = 0.5 * del;
+            for (int k = 0; k < cnt; k++) {
+                float s, c;
+                sincosf((float)x, &s, &c);
+                sum.add(chi_integrand_f(A, c, s, cd, sd));
+                x += del;
+            }
+        }
+        cur = 0.5 * (cur + b * sum.value() / cnt);
+        cnt *= 2;
+        win[0] = win[1];
+        win[1] = win[2];
+        win[2] = win[3];
+        win[3] = win[4];
+        win[4] = cur;
+        if (j >= 5 && romb_stop(win, pq, 1.0e-300, guard)) break;
+    }
+    return pq;
+}
+
+__device__ double qromb_delta_f(const Ctx &C, const ChiArgsF &A, bool &guard) {
+    const cs_prepared &P = *C.P;
+    const double b = P.romb_delta_b;
+    const double dbeta = P.romb_dbeta;
+    double win[5];
+    double cur;
+    int cnt;
+    double pq = 0.0;
+    {
+        const cs_delta_node n0 = C.dnode[0], n1 = C.dnode[1];
+        const double pa = n0.w * qromb_chi_f(C, A, (float)n0.c, (float)n0.s, guard) / (2.0 * M_PI);
+        const double pb = n1.w * qromb_chi_f(C, A, (float)n1.c, (float)n1.s, guard) / (2.0 * M_PI);
+        cur = 0.5 * b * (pa + pb);
+        cnt = 1;
+    }
+    win[4] = cur;
+    for (int j = 2; j <= 20; j++) {
+        double sump = 0.0;
+        if (j <= CS_NODE_LEVELS) {
+            const cs_delta_node *nd = C.dnode + CS_NODE_OFFSET(j);
+            for (int k = 0; k < cnt; k++) {
+                const cs_delta_node n = nd[k];
+                sump += n.w * qromb_chi_f(C, A, (float)n.c, (float)n.s, guard) / (2.0 * M_PI);
+            }
+        } else {
+            const double del = b / cnt;
+            double x = 0.5 * del;
+            for (int k = 0; k < cnt; k++) {
+                double s, c;
+                sincos(x, &s, &c);
+                sump += s * exp(-x * x / (dbeta * dbeta)) * qromb_chi_f(C, A, (float)c, (float)s, guard) / (2.0 * M_PI);
+                x += del;
+            }
+        }
+        cur = 0.5 * (cur + b * sump / cnt);
+        cnt *= 2;
+        win[0] = win[1];
+        win[1] = win[2];
+        win[2] = win[3];
+        win[3] = win[4];
+        win[4] = cur;
+        if (j >= 5 && romb_stop(win, pq, 1.0e-100, guard)) break;
+    }
+    return pq;
+}
+
+// ----------------------------------------------------------- peak sums FP32
+// Lattice peak sums of the FCC/BCT pixel functions over sorted, compacted
+// reflection tables. The radial Gaussian of every reflection underflows FP32
+// for |q - q_hkl| beyond ~9.3 widths; those reflections are skipped (a binary
+// search bounds the window). q is carried as a float pair (qf + ql) so that
+// q - q_hkl is formed exactly (Sterbenz) before squaring.
+__device__ __forceinline__ int lower_bound_f(const float *__restrict__ a, int n, float v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(a + mid) < v)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, double qy, double qz, double q,
+                            double &radint, double &intens, bool &guard) {
+    double width = 1;
+    if (P.debyescherrer) width = 4.0 / P.domainsize;
+    if (P.para) width = (4.0 / P.domainsize) + cs64::sqr(P.reldis) * P.dist * cs64::sqr(q);
+    width *= P.width_zuf;
+    const double widthiso = 1.0 / P.uca;
+    const float qf = (float)q;
+    const float ql = (float)(q - (double)qf);
+    // isotropic peaks: exp(-4 x2/pi) / (pi widthiso/2), x2 = (q-qhkl)^2/widthiso^2
+    {
+        const float k = (float)(4.0 / M_PI / (widthiso * widthiso) * 1.4426950408889634);
+        const float dmax = (float)(9.4 * widthiso);
+        int i = lower_bound_f(T.iq, T.n_iso, qf - dmax);
+        Kahan s;
+        for (; i < T.n_iso; i++) {
+            const float qh = __ldg(T.iq + i);
+            const float d = (qf - qh) + ql;
+            if (d < -dmax) break;
+            s.add(exp2f(-k * d * d) * __ldg(T.imf + i));
+        }
+        radint = s.value() / (M_PI * widthiso / 2.0);
+    }
+    // anisotropic peaks
+    {
+        const float k = (float)(4.0 / M_PI / (width * width) * 1.4426950408889634);
+        const float dmax = (float)(9.4 * width);
+        const float kphi = (float)(4 * q * q / (M_PI * cs64::sqr(P.phiwidth)) * 1.4426950408889634);
+        const float invq = (float)(1.0 / q);
+        const float fx = (float)qx * invq, fy = (float)qy * invq, fz = (float)qz * invq;
+        int i = lower_bound_f(T.aq, T.n_aniso, qf - dmax);
+        Kahan s;
+        for (; i < T.n_aniso; i++) {
+            const float qh = __ldg(T.aq + i);
+            const float d = (qf - qh) + ql;
+            if (d < -dmax) break;
+            const float4 v = __ldg(T.av + i);  // unit q_hkl (x,y,z) and g3/peaknorm1
+            const float c = fx * v.x + fy * v.y + fz * v.z;
+            // myacos: the reference maps c < -1 to 0 and c > 1 to pi
+            const float yphi = (c < -1.0f) ? 0.0f : ((c > 1.0f) ? (float)M_PI : acosf(c));
+            const float e = exp2f(-k * d * d - kphi * yphi * yphi);
+            s.add(e * v.w * __ldg(T.amf + i));
+        }
+        intens = s.value() / (M_PI * width / 2.0);
+        if (!isfinite(intens)) guard = true;  // the reference stops at an infinite sum
+    }
+}
+
+// ---------------------------------------------------------------- pixels
+__device__ __forceinline__ double zr_asym(const cs_prepared &P) {
+    double zr = (1 - cs64::sqr(P.sigma)) / cs64::sqr(P.sigma);
+    if (zr * (zr - 1) * (zr - 2) * (zr - 3) * (zr - 4) * (zr - 5) == 0) zr += CS_EPS3;
+    return zr;
+}
+
+__device__ double sphere_pq_mixed(const cs_prepared &P, double q, bool &guard) {
+    if (P.cs != 0) {
+        guard = true;
+        return 0.0;
+    }
+    const double thr = 0.4 * P.limq[4];
+    if (near(q, thr, 1e-12)) guard = true;
+    if (q < thr) return cs64::series_q(P.carrp[3], q, 100);
+    const double zr = zr_asym(P);
+    return sphere_pq_asym((float)(q * P.radius / (zr + 1)), (float)zr);
+}
+
+__device__ double sphere_fq_mixed(const cs_prepared &P, double q, bool &guard) {
+    const double thr = 0.4 * P.limqf[4];
+    if (near(q, thr, 1e-12)) guard = true;
+    if (q < thr) return cs64::series_q(P.carrf[3], q, 100);
+    const double zr = (1 - cs64::sqr(P.sigma)) / cs64::sqr(P.sigma);
+    return sphere_fq_asym((float)(q * P.radius / (zr + 1)), (float)zr);
+}
+
+// formpq_partCylinder, ordis 0 and 6, cs 0 (mixed)
+__device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, bool &guard) {
+    const cs_prepared &P = *C.P;
+    if (P.cs != 0) {
+        guard = true;
+        return 0.0;
+    }
+    const double zl = P.sigmal == 1.0 ? CS_EPS9 : (1 - cs64::sqr(P.sigmal)) / cs64::sqr(P.sigmal);
+    const double zr = P.sigma == 1.0 ? CS_EPS9 : (1 - cs64::sqr(P.sigma)) / cs64::sqr(P.sigma);
+    double pql = 0, pqr = 0;
+    if (P.ordis == 6) {
+        const double thr = 0.6 * P.limq[1];
+        if (near(q, thr, 1e-12)) guard = true;
+        if (q < thr) {
+            pql = 1.0;
+            double old = 0.0, qqnn = 1.0;
+            for (int nser = 1; nser <= 120; nser++) {
+                qqnn = qqnn * (qxs + qys) * (qxs + qys);
+                pql += P.carrp[0][nser] * qqnn;
+                if (fabs((pql - old) / pql) < 0.0001) break;
+                old = pql;
+            }
+        } else {
+            const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
+            pql = cyl_len_factor((float)arglq, (float)zl);
+        }
+    } else if (P.ordis == 0) {
+        const double thr = 0.4 * P.limq[1];
+        if (near(q, thr, 1e-12)) guard = true;
+        if (q < thr) {
+            pql = 1.0;
+            if (P.orcase == 1 || P.orcase == 2)
+                pql = cs64::cyl_double_series(P, qxs, qys, P.carrp[0], 0);
+            else if (P.orcase == 3)
+                pql = cs64::cyl_double_series(P, qxs, qys, P.carrp[0], 1);
+        } else {
+            ChiArgsF A;
+            const double s = P.sigmal;
+            const double z = (1 - s * s) / (s * s);
+            A.qx = (float)qxs;
+            A.qy = (float)qys;
+            A.lz = (float)(P.length / (z + 1));
+            A.z = (float)z;
+            A.p11 = (float)P.romb_p[0];
+            A.p12 = (float)P.romb_p[1];
+            A.p13 = (float)P.romb_p[2];
+            A.p21 = (float)P.romb_p[3];
+            A.p22 = (float)P.romb_p[4];
+            A.p23 = (float)P.romb_p[5];
+            A.i1 = P.orcase;
+            pql = qromb_delta_f(C, A, guard) / P.norm;
+        }
+    } else {
+        guard = true;
+        return 0.0;
+    }
+    if ((P.length / P.radius) < 2)
+        pqr = 1;
+    else {
+        const double thr = 0.65 * P.limq[4];
+        if (near(q, thr, 1e-12)) guard = true;
+        if (q < thr)
+            pqr = cs64::series_q(P.carrp[3], q, 120);
+        else
+            pqr = cyl_pqr_asym((float)(q * P.radius / (zr + 1)), (float)zr);
+    }
+    return pql * pqr;
+}
+
+
+// formfq_partCylinder, ordis 0 and 6, cs 0 (mixed)
+__device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qys, double q, bool &guard) {
+    const cs_prepared &P = *C.P;
+    if (P.cs != 0) {
+        guard = true;
+        return 0.0;
+    }
+    const double zl = (1 - cs64::sqr(P.sigmal)) / cs64::sqr(P.sigmal);
+    const double zr = (1 - cs64::sqr(P.sigma)) / cs64::sqr(P.sigma);
+    double pql = 0, pqr = 0;
+    if (P.ordis == 6) {
+        const double thr = 0.6 * P.limqf[1];
+        if (near(limql, thr, 1e-12)) guard = true;
+        if (limql < thr) {
+            double pqsum = 1.0, old = 0.0, qqnn = 1.0;
+            for (int nser = 1; nser <= 120; nser++) {
+                qqnn = qqnn * (qxs + qys) * (qxs + qys);
+                pqsum = pqsum + P.carrf[0][nser] * qqnn;
+                if (fabs((pqsum - old) / pqsum) < 0.0001) break;
+                old = pqsum;
+            }
+            pql = pqsum;
+        } else {
+            const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
+            pql = cyl_len_factor((float)arglq, (float)zl);
+        }
+    } else if (P.ordis == 0) {
+        const double thr = 0.2 * P.limqf[1];
+        if (near(limql, thr, 1e-12)) guard = true;
+        if (limql < thr) {
+            double pqsum = 1.0;
+            if (P.orcase == 1) pqsum = cs64::cyl_double_series(P, qxs, qys, P.carrf[0], 2);
+            if (P.orcase == 2) pqsum = cs64::cyl_double_series(P, qxs, qys, P.carrf[0], 0);
+            if (P.orcase == 3) pqsum = cs64::cyl_double_series(P, qxs, qys, P.carrf[0], 3);
+            pql = pqsum;
+        } else {
+            ChiArgsF A;
+            const double s = P.sigmal;
+            const double z = (1 - s * s) / (s * s);
+            A.qx = (float)qxs;
+            A.qy = (float)qys;
+            A.lz = (float)(P.length / (z + 1));
+            A.z = (float)z;
+            A.p11 = (float)P.romb_p[0];
+            A.p12 = (float)P.romb_p[1];
+            A.p13 = (float)P.romb_p[2];
+            A.p21 = (float)P.romb_p[3];
+            A.p22 = (float)P.romb_p[4];
+            A.p23 = (float)P.romb_p[5];
+            A.i1 = P.orcase;
+            pql = qromb_delta_f(C, A, guard) / P.norm;
+        }
+    } else {
+        guard = true;
+        return 0.0;
+    }
+    const double thr = 1.0 * P.limqf[4];
+    if (near(q, thr, 1e-12)) guard = true;
+    if (q < thr) {
+        pqr = cs64::series_q(P.carrf[3], q, 120);
+    } else {
+        const float a = (float)(q * P.radius / (zr + 1));
+        const float z = (float)zr;
+        const float t = atanf(a);
+        const float a2 = a * a;
+        const float s1 = (z - 0.5f) * t, s2 = (z - 1.5f) * t;
+        const float pqr1 = (float)P.gamma_ratio[0] * rsqrtf(a2 * a) * (sinf(s1) - cosf(s1)) / powp1f(a2, (z - 0.5f) / 2.0f);
+        const float pqr2 = (float)P.gamma_ratio[1] * rsqrtf(a2 * a2 * a) * (sinf(s2) + cosf(s2)) / powp1f(a2, (z - 1.5f) / 2.0f);
+        const float pqr3 = (2.0f / sqrtf((float)M_PI)) * (pqr1 + (9.0f / 16.0f) * pqr2);
+        pqr = (double)pqr3 * (double)pqr3;
+    }
+    return pql * pqr;
+}
+
+template <int KEY>
+__device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double qy, double qz, bool &guard) {
+    const cs_prepared &P = *C.P;
+    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
+    const double tailv = P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+    if (KEY == CS_KEY_SPHERE_NONE_ISO) {
+        const double pq = sphere_pq_mixed(P, q, guard);
+        return P.base + P.izero * (pq + P.iso * pq) + tailv;
+    }
+    if (KEY == CS_KEY_SPHERE_GAUSS_FCC_GAUSS) {
+        const double pq = sphere_pq_mixed(P, q, guard);
+        const double fq = sphere_fq_mixed(P, q, guard);
+        double radint, intens;
+        peak_sums_f(P, T, qx, qy, qz, q, radint, intens, guard);
+        const double v = P.latpar[1] * P.latpar[2];
+        const double szqiso = 1 + (8 * M_PI * M_PI * M_PI * radint / (4 * M_PI * v) - 1) * exp(-P.ucb * q * q);
+        const double szq = 1 + (fq / pq) * (2 * M_PI * intens / v - 1) * exp(-P.dwfactor * q * q);
+        return P.base + P.izero * (szq * pq + P.iso * szqiso * pq) + tailv;
+    }
+    if (KEY == CS_KEY_CYL_NONE_GAUSS) {
+        double pq;
+        if (P.orcase == CS_ORC_GENERAL)
+            pq = cyl_pq_mixed(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q, guard);
+        else
+            pq = cyl_pq_mixed(C, qx, qy, q, guard);
+        return P.base + P.izero * (pq + P.iso) + tailv;
+    }
+    if (KEY == CS_KEY_CYL_NONE_ZDIR) {
+        double pq;
+        switch (P.orcase) {
+        case CS_ORC_GENERAL: pq = cyl_pq_mixed(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard); break;
+        case CS_ORC_XAXIS: pq = cyl_pq_mixed(C, qx, 0, q, guard); break;
+        case CS_ORC_YAXIS: pq = cyl_pq_mixed(C, 0, qy, q, guard); break;
+        default: pq = cyl_pq_mixed(C, qx, qy, q, guard); break;
+        }
+        return P.base + P.izero * (pq + P.iso) + tailv;
+    }
+    if (KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR) {
+        double pq = 0, fq = 0;
+        switch (P.orcase) {
+        case CS_ORC_GENERAL:
+            pq = cyl_pq_mixed(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard);
+            fq = cyl_fq_mixed(C, sqrt(P.cosphi * qx * qx + P.sinphi * qy * qy + CS_EPS9), qx * P.cosphi * P.sintheta,
+                              qy * P.sinphi * P.sintheta, q, guard);
+            break;
+        case CS_ORC_XAXIS:
+            pq = cyl_pq_mixed(C, qx, 0, q, guard);
+            fq = cyl_fq_mixed(C, fabs(qx), qx, 0, q, guard);
+            break;
+        case CS_ORC_YAXIS:
+            pq = cyl_pq_mixed(C, 0, qy, q, guard);
+            fq = cyl_fq_mixed(C, fabs(qy), 0, qy, q, guard);
+            break;
+        default:
+            pq = cyl_pq_mixed(C, qx, qy, q, guard);
+            fq = cyl_fq_mixed(C, q, qx, qy, q, guard);
+            break;
+        }
+        double radint, intens;
+        peak_sums_f(P, T, qx, qy, qz, q, radint, intens, guard);
+        const double v = P.latpar[1] * P.latpar[2];
+        const double szqiso = 1 + (8 * M_PI * M_PI * M_PI * radint / (4 * M_PI * v) - 1) * exp(-P.ucb * q * q);
+        const double szq = 1 + (fq / pq) * (2 * M_PI * intens / v - 1) * exp(-P.dwfactor * q * q);
+        return P.base + P.izero * (szq * pq + P.iso * szqiso * 1.0) + tailv;
+    }
+    guard = true;
+    return 0.0;
+}
+
+// Mixed image kernel: writes every pixel; pixels with a guarded decision are
+// appended to the redo list (device counter) and rewritten by k_redo.
+template <int KEY>
+__global__ void __launch_bounds__(256) k_image_mixed(Ctx C, PeakTab T, double *__restrict__ out, int nx, long npix,
+                                                      int *__restrict__ redo_count, int *__restrict__ redo_list,
+                                                      int redo_cap) {
+    const cs_prepared &P = *C.P;
+    const int xstride = P.xmax - P.xmin;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < npix; t += (long)gridDim.x * blockDim.x) {
+        const int ihex = P.zzmin + (int)(t % nx);
+        const int i = P.iimin + (int)(t / nx);
+        double qx, qy, qz;
+        q_of_pixel(P, ihex, i, qx, qy, qz);
+        bool guard = false;
+        const double v = calc_mixed<KEY>(C, T, qx, qy, qz, guard);
+        out[(long)(ihex - P.xmin) + (long)xstride * (long)(i - P.ymin)] = v;
+        if (guard) {
+            const int pos = atomicAdd(redo_count, 1);
+            if (pos < redo_cap) redo_list[pos] = (int)t;
+        }
+    }
+}
+
+}  // namespace csm
+
+namespace cs {
+
+// Compact, sorted reflection tables from the prepared block (see PeakTab).
+void build_peak_tables(const cs_prepared &P, HostPeaks &H) {
+    H.aq.clear(); H.amf.clear(); H.av.clear(); H.iq.clear(); H.imf.clear();
+    struct A { float q; float4 v; float mf; int idx; };
+    std::vector<A> an;
+    for (int ii = 1; ii <= P.peakmax2 && ii < CS_LATPARLEN; ii++) {
+        const float qh = P.latpar3[ii][5];
+        const int mf = P.latpar2[ii][4] * P.latpar2[ii][5];
+        if (!(qh > 0) || mf == 0) continue;
+        const double q = qh;
+        A a;
+        a.q = qh;
+        a.v = make_float4((float)(P.latpar3[ii][2] / q), (float)(P.latpar3[ii][3] / q), (float)(P.latpar3[ii][4] / q),
+                          (float)((double)P.latpar3[ii][10] / (double)P.latpar3[ii][11]));
+        a.mf = (float)mf;
+        a.idx = ii;
+        an.push_back(a);
+    }
+    std::stable_sort(an.begin(), an.end(), [](const A &x, const A &y) { return x.q < y.q; });
+    for (auto &a : an) {
+        H.aq.push_back(a.q);
+        H.av.push_back(a.v);
+        H.amf.push_back(a.mf);
+    }
+    struct I { float q; float mf; };
+    std::vector<I> is;
+    for (int ii = 1; ii <= P.peakmax1 && ii < CS_LATPARLEN; ii++) {
+        const int mhkl = P.latpar1[ii][4], fhkl = P.latpar1[ii][5];
+        if (mhkl == 0 || fhkl == 0) continue;
+        is.push_back({P.latpar3[ii][5], (float)mhkl * (float)fhkl});
+    }
+    std::stable_sort(is.begin(), is.end(), [](const I &x, const I &y) { return x.q < y.q; });
+    for (auto &i : is) {
+        H.iq.push_back(i.q);
+        H.imf.push_back(i.mf);
+    }
+}
+
+static int sm_count_m() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <int KEY>
+static void launch_mixed_key(const DevSet &D, const csm::PeakTab &T, const cs_prepared &P, double *d_out,
+                             MixedScratch &S, cudaStream_t s) {
+    const int nx = P.zzmax - P.zzmin;
+    const long npix = (long)nx * (long)(P.iimax - P.iimin);
+    cs64::Ctx C{D.d_prep, D.d_chi, D.d_delta};
+    const long need = (npix + 255) / 256;
+    const long cap = (long)sm_count_m() * 8;
+    const int grid = (int)(need < cap ? (need < 1 ? 1 : need) : cap);
+    cudaMemsetAsync(S.d_count, 0, sizeof(int), s);
+    csm::k_image_mixed<KEY><<<grid, 256, 0, s>>>(C, T, d_out, nx, npix, S.d_count, S.d_list, S.cap);
+    launch_redo(D, P, d_out, S, s);
+}
+
+int launch_image_mixed(const DevSet &D, const csm::PeakTab &T, const cs_prepared &P, double *d_out, MixedScratch &S,
+                       cudaStream_t s) {
+    const int nx = P.zzmax - P.zzmin, ny = P.iimax - P.iimin;
+    if (nx <= 0 || ny <= 0) return CS_OK;
+    if (P.twin) return CS_ERR_UNSUPPORTED;
+    switch (P.key) {
+    case CS_KEY_SPHERE_NONE_ISO: launch_mixed_key<CS_KEY_SPHERE_NONE_ISO>(D, T, P, d_out, S, s); break;
+    case CS_KEY_SPHERE_GAUSS_FCC_GAUSS: launch_mixed_key<CS_KEY_SPHERE_GAUSS_FCC_GAUSS>(D, T, P, d_out, S, s); break;
+    case CS_KEY_CYL_NONE_GAUSS: launch_mixed_key<CS_KEY_CYL_NONE_GAUSS>(D, T, P, d_out, S, s); break;
+    case CS_KEY_CYL_NONE_ZDIR: launch_mixed_key<CS_KEY_CYL_NONE_ZDIR>(D, T, P, d_out, S, s); break;
+    case CS_KEY_CYL_GAUSS_BCT_ZDIR: launch_mixed_key<CS_KEY_CYL_GAUSS_BCT_ZDIR>(D, T, P, d_out, S, s); break;
+    default: return CS_ERR_UNSUPPORTED;
+    }
+    if (P.expand && P.calc_quadrants != CS_RADQ4 && P.calc_quadrants != CS_RAD1D) launch_mirror(P, d_out, s);
+    return cudaGetLastError() == cudaSuccess ? CS_OK : CS_ERR_CUDA;
+}
+
+}  // namespace cs

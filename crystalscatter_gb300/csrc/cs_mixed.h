@@ -1,0 +1,51 @@
+// cs_mixed.h — mixed-precision path: compact peak tables and redo scratch (internal).
+#ifndef CS_MIXED_H
+#define CS_MIXED_H
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "cs_launch.h"
+#include "cs_prepared.h"
+
+namespace csm {
+
+// Reflection tables of one parameter set in the form the FP32 peak sums read:
+// entries that the reference would skip are dropped, the rest sorted by q_hkl.
+struct PeakTab {
+    int n_aniso = 0;
+    const float *aq = nullptr;   // q_hkl
+    const float4 *av = nullptr;  // unit q_hkl vector (x, y, z), g3/peaknorm1
+    const float *amf = nullptr;  // multiplicity * structure factor
+    int n_iso = 0;
+    const float *iq = nullptr;
+    const float *imf = nullptr;
+};
+
+}  // namespace csm
+
+namespace cs {
+
+// Redo list of the mixed kernels (pixels recomputed in FP64).
+struct MixedScratch {
+    int *d_count = nullptr;
+    int *d_list = nullptr;
+    int cap = 0;
+};
+
+// Host form of the compact peak tables (built from the prepared block).
+struct HostPeaks {
+    std::vector<float> aq, amf, iq, imf;
+    std::vector<float4> av;
+};
+void build_peak_tables(const cs_prepared &P, HostPeaks &H);
+
+int launch_image_mixed(const DevSet &D, const csm::PeakTab &T, const cs_prepared &P, double *d_out, MixedScratch &S,
+                       cudaStream_t s);
+int launch_redo(const DevSet &D, const cs_prepared &P, double *d_out, const MixedScratch &S, cudaStream_t s);
+void launch_mirror(const cs_prepared &P, double *d_out, cudaStream_t s);
+
+}  // namespace cs
+
+#endif

@@ -461,6 +461,15 @@ bool Prep::coefficients() {
             const double p11 = -std::cos(P.polphi * M_PI / 180.0) * std::cos(P.poltheta * M_PI / 180.0);
             const double p13 = std::cos(P.polphi * M_PI / 180.0) * std::sin(P.poltheta * M_PI / 180.0);
             const double p21 = -std::cos(P.polphi * M_PI / 180.0);
+            // The powers below are the same pow() calls as in the reference's
+            // innermost loop (:4705-4719), evaluated once per exponent.
+            double pw11[kNmax + 1], pw13[kNmax + 1], pw4[kNmax + 1], pw21[kNmax + 1];
+            for (int e = 0; e <= nmax; e++) {
+                pw11[e] = std::pow(p11 * p11, e);
+                pw13[e] = std::pow(p13 * p13, e);
+                pw4[e] = std::pow(4.0, e);
+                pw21[e] = std::pow(sqr(p21), e);
+            }
             if (P.cs == 0) {
                 double z12v[kNmax + 1];
                 z12v[0] = 1.0;
@@ -476,10 +485,14 @@ bool Prep::coefficients() {
                     xrn_n = -xrn_n * xr2z;
                     for (int m = 0; m <= n; m++) {
                         double sump = 0.0;
-                        for (int ll = 0; ll <= m; ll++)
-                            sump += std::pow(p11 * p11, ll) * std::pow(p13 * p13, m - ll) * intl_const /
-                                    (std::pow(4.0, ll) * fk2v[m - ll] * fkv[n - m + ll] * fkv[ll] * P.norm);
-                        P.carr11pm[n][m] = std::pow(4.0, m) * std::pow(sqr(p21), n - m) * sump / (fkv[n - m]);
+                        for (int ll = 0; ll <= m; ll++) {
+                            const double num = pw11[ll] * pw13[m - ll] * intl_const;
+                            // a zero numerator adds exactly 0 (the long-double
+                            // denominator is finite and non-zero): skipped
+                            if (num == 0.0) continue;
+                            sump += num / (pw4[ll] * fk2v[m - ll] * fkv[n - m + ll] * fkv[ll] * P.norm);
+                        }
+                        P.carr11pm[n][m] = pw4[m] * pw21[n - m] * sump / (fkv[n - m]);
                     }
                     carr1p[n] = std::pow(4.0, n) * z12vl[n] * xln_n / ((2.0 * n + 1) * (n + 1));
                     carr2p[n] = std::pow(4.0, n + 1) * gam3[n] * z12vl[n] * xln_n /

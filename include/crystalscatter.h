@@ -144,6 +144,11 @@ int cs_fit_chi2(cs_handle *h, int num_threads, int bstop, int border, int mode, 
 
 const char *cs_last_error(cs_handle *h);
 
+/* Pixels of the last mixed-precision calculation whose FP32 result sat inside
+   a decision guard band and were recomputed in FP64 (no counterpart in the
+   reference; reported alongside accuracy figures). */
+int cs_mixed_redo_pixels(cs_handle *h, long *n);
+
 /* Host preparation alone, without any CUDA call (the reference's private
    prepareCalculation, Source/sc_calc_generic_cpu.cpp:319-988): fills the
    prepared constant block (layout: crystalscatter_gb300/csrc/cs_prepared.h,

@@ -11,16 +11,24 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "cs_oracle.c")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liboracle_cs.so")
+PROBE = os.path.join(OUT, "liboracle_cs_probe.so")
 HDR = os.path.join(HERE, "..", "crystalscatter_gb300", "csrc", "cs_prepared.h")
 
 
-def build(force=False):
-    os.makedirs(OUT, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(HDR)):
-        return LIB
-    cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fPIC", "-shared", "-ffp-contract=off", "-Wall", SRC, "-o",
-           LIB, "-lpthread", "-lm"]
+def _compile(out, extra):
+    cmd = ["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fPIC", "-shared", "-ffp-contract=off", "-Wall"] + extra + [
+        SRC, "-o", out, "-lpthread", "-lm"]
     subprocess.run(cmd, check=True)
+
+
+def build(force=False):
+    """liboracle_cs.so (the oracle) and liboracle_cs_probe.so (the same code
+    with the one-ulp conditioning probe compiled in)."""
+    os.makedirs(OUT, exist_ok=True)
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(HDR))
+    for out, extra in ((LIB, []), (PROBE, ["-DCS_ORACLE_PROBE"])):
+        if force or not os.path.exists(out) or os.path.getmtime(out) < newest:
+            _compile(out, extra)
     return LIB
 
 

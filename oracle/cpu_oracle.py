@@ -17,7 +17,12 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 LIB = os.path.join(HERE, "_build", "liboracle_cs.so")
+PROBE = os.path.join(HERE, "_build", "liboracle_cs_probe.so")
 _lib = None
+_probe = None
+# probe modes: bit k set = function k (sin cos atan atan2 pow exp sqrt log acos)
+# rounded one ulp up, clear = one ulp down
+PROBE_MODES = (0x1FF, 0x100, 0x155, 0x0AA)
 
 
 def load():
@@ -37,6 +42,44 @@ def load():
         lib.oracle_fit.restype = ctypes.c_double
         _lib = lib
     return _lib
+
+
+def load_probe():
+    global _probe
+    if _probe is None:
+        if not os.path.exists(PROBE):
+            from oracle import build_oracle
+            build_oracle.build()
+        lib = ctypes.CDLL(PROBE)
+        lib.oracle_image_rows.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        lib.oracle_image_rows.restype = ctypes.c_long
+        lib.oracle_set_probe.argtypes = [ctypes.c_int]
+        _probe = lib
+    return _probe
+
+
+def condition(params, ign_cbs=0, nthreads=None, modes=PROBE_MODES):
+    """Per-pixel sensitivity of the reference computation to last-bit libm
+    differences: max over probe modes of |I_mode - I| / max(|I|, tau), with the
+    unperturbed image I. Non-finite disagreements count as inf."""
+    P = prepare(params, ign_cbs)
+    base, _ = image_prepared(P, nthreads)
+    lib = load_probe()
+    cond = np.zeros(base.shape)
+    fin = np.isfinite(base)
+    tau = 1e-30 * (np.max(np.abs(base[fin])) if fin.any() else 1.0)
+    for m in modes:
+        out = np.zeros(base.shape, dtype=np.float64)
+        lib.oracle_set_probe(int(m))
+        lib.oracle_image_rows(ctypes.byref(P), out.ctypes.data, 0, 0, int(nthreads or os.cpu_count() or 1))
+        with np.errstate(invalid="ignore", over="ignore"):
+            d = np.abs(out - base) / np.maximum(np.abs(base), tau)
+        same_nf = (~np.isfinite(base)) & ((np.isnan(base) & np.isnan(out)) | (base == out))
+        d[same_nf] = 0.0
+        d[~np.isfinite(d)] = np.inf
+        cond = np.maximum(cond, d)
+    lib.oracle_set_probe(0)
+    return cond
 
 
 def prepare(params, ign_cbs=0):

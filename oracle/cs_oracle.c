@@ -44,6 +44,30 @@
 
 #include "../crystalscatter_gb300/csrc/cs_prepared.h"
 
+#ifdef CS_ORACLE_PROBE
+/* Conditioning probe build (liboracle_cs_probe.so, test infrastructure): every
+   math-library result is moved by one ulp, up or down per function as the
+   probe mode selects. The spread of images over a few modes measures how much
+   the reference's own result depends on last-bit differences of the math
+   library; pixels with a large spread cannot be reproduced to 1e-10 by any
+   other libm and are reported separately. Mode 0 disables the probe. */
+static int g_probe_mode = 0;
+void oracle_set_probe(int mode) { g_probe_mode = mode; }
+static double probe_(double r, int fn) {
+    if (!g_probe_mode || !isfinite(r)) return r;
+    return nextafter(r, ((g_probe_mode >> fn) & 1) ? INFINITY : -INFINITY);
+}
+#define sin(x) probe_(sin(x), 0)
+#define cos(x) probe_(cos(x), 1)
+#define atan(x) probe_(atan(x), 2)
+#define atan2(y, x) probe_(atan2(y, x), 3)
+#define pow(x, y) probe_(pow(x, y), 4)
+#define exp(x) probe_(exp(x), 5)
+#define sqrt(x) probe_(sqrt(x), 6)
+#define log(x) probe_(log(x), 7)
+#define acos(x) probe_(acos(x), 8)
+#endif
+
 #define EPS9 0.000000001
 #define EPS3 0.001
 

@@ -8,6 +8,12 @@ the chi^2 sums. Usage (needs the reference sources and the built oracle/_ref):
 
     python tests/golden/make_golden.py
 
+Each case also stores "cond", the per-pixel sensitivity of the reference's
+result to one-ulp differences of the math library (oracle.cpu_oracle.condition,
+measured with the reference-pinned oracle): pixels where the reference's own
+result moves by more than 1e-12 under such perturbations cannot be reproduced
+to 1e-10 by another math library and are compared against that envelope.
+
 The cases are the benchmark workloads on coarser grids with the same q-range
 (crystalscatter_gb300.configs.scaled) plus variants that reach other branches
 (quadrant mirroring, midpoint geometry, beam offset, core/shell spheres,
@@ -24,7 +30,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from crystalscatter_gb300 import configs as C  # noqa: E402
-from oracle import refbind  # noqa: E402
+from oracle import cpu_oracle, refbind  # noqa: E402
 
 ARRAYS = ["carr1p", "carr2p", "carr3p", "carr4p", "carr5p", "carr6p", "carr1f", "carr4f", "carr5f", "carr6f",
           "carr11pm"]
@@ -91,7 +97,10 @@ def main():
         rc, err = r.run(nthreads=8, ign_cbs=ign)
         assert rc == 0, (name, err)
         img = r.image()
-        rec = {"image": img, "dims": np.array(r.dims())}
+        # per-pixel conditioning of the reference computation: spread of the
+        # (reference-pinned) oracle under one-ulp math-library perturbations
+        cond = cpu_oracle.condition(p, ign_cbs=ign, nthreads=8)
+        rec = {"image": img, "dims": np.array(r.dims()), "cond": cond.astype(np.float32)}
         for a in ARRAYS:
             rec[a] = r.array(a)
         for s in SCALARS:
@@ -103,8 +112,10 @@ def main():
             rec["latpar3"] = r.latpar(3)[: pm2 + 1]
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
         out[name] = {"params": p, "ign_cbs": ign, "shape": list(img.shape),
-                     "nonfinite": int((~np.isfinite(img)).sum()), "zeros": int((img == 0).sum())}
-        print(name, img.shape, "nonfinite", out[name]["nonfinite"], "zeros", out[name]["zeros"])
+                     "nonfinite": int((~np.isfinite(img)).sum()), "zeros": int((img == 0).sum()),
+                     "ill_conditioned": int((cond > 1e-12).sum())}
+        print(name, img.shape, "nonfinite", out[name]["nonfinite"], "zeros", out[name]["zeros"],
+              "ill-conditioned", out[name]["ill_conditioned"])
         r.close()
 
     # fit cases: target = reference image * deterministic multiplicative noise

@@ -70,3 +70,36 @@ def written_mask(params, shape):
         if params.get("RadioButtonQ2", 0) and not params.get("RadioButtonQ1", 0):
             m[0, :zmax] = False  # y = -zmax, x < 0
     return m
+
+
+ILL = 1e-12  # a pixel is ill-conditioned when one-ulp libm changes move the reference by more
+
+
+def compare_to_reference(got, ref, cond, mask=None, tol=1e-10, envelope=100.0):
+    """Compares an image with the reference's own image.
+
+    Well-conditioned pixels (cond <= 1e-12) must agree to `tol`. Ill-conditioned
+    pixels, whose reference value itself moves by `cond` under one-ulp changes
+    of the math library, must agree to envelope*cond (and to tol at least).
+    Non-finite pixels must match in class unless the reference's own probe
+    turned them finite (cond = inf). Returns a dict of counts and maxima."""
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    cond = np.asarray(cond, dtype=np.float64)
+    if mask is None:
+        mask = np.ones(ref.shape, dtype=bool)
+    rel, _ = rel_error(got, ref)
+    ill = cond > ILL
+    allowed = np.maximum(tol, envelope * cond)
+    bad = mask & (rel > allowed)
+    well = mask & ~ill
+    fin_well = well & np.isfinite(rel)
+    return {
+        "n": int(mask.sum()),
+        "n_ill": int((mask & ill).sum()),
+        "n_bad": int(bad.sum()),
+        "max_rel_well": float(rel[fin_well].max()) if fin_well.any() else 0.0,
+        "median_rel": float(np.median(rel[mask])) if mask.any() else 0.0,
+        "max_rel_all": float(np.nanmax(np.where(np.isfinite(rel[mask]), rel[mask], 0))) if mask.any() else 0.0,
+        "n_above_tol": int((mask & (rel > tol)).sum()),
+    }
