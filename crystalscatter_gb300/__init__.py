@@ -14,8 +14,8 @@ import os
 import numpy as np
 
 __all__ = [
-    "CsParams", "SasCalc_GENERIC_calculation", "CrystalScatterError", "load_library", "library_path",
-    "CS_MODE_FP64", "CS_MODE_MIXED",
+    "CsParams", "SasCalc_GENERIC_calculation", "SasCalcBatch", "CrystalScatterError", "load_library",
+    "library_path", "params_from_mapping", "CS_MODE_FP64", "CS_MODE_MIXED", "CS_SCHED_PLAIN", "CS_SCHED_PERSISTENT",
 ]
 
 CS_OK = 0
@@ -28,6 +28,8 @@ CS_ERR_STATE = 6
 CS_ERR_SIZE = 7
 CS_MODE_FP64 = 0
 CS_MODE_MIXED = 1
+CS_SCHED_PLAIN = 0
+CS_SCHED_PERSISTENT = 1
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -121,6 +123,25 @@ def _sig(lib):
     lib.cs_prepared_size.restype = ctypes.c_size_t
     lib.cs_prepare_params.argtypes = [P(CsParams), ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t,
                                       ctypes.c_char_p, ctypes.c_size_t]
+    B = ctypes.c_void_p
+    lib.cs_batch_create.restype = B
+    lib.cs_batch_destroy.argtypes = [B]
+    lib.cs_batch_last_error.restype = ctypes.c_char_p
+    lib.cs_batch_last_error.argtypes = [B]
+    lib.cs_batch_prepare.argtypes = [B, P(CsParams), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    lib.cs_batch_info.argtypes = [B, P(ctypes.c_size_t), P(ctypes.c_long), P(ctypes.c_int)]
+    lib.cs_batch_layout.argtypes = [B, ctypes.c_int, P(ctypes.c_size_t)] + [P(ctypes.c_int)] * 4
+    lib.cs_batch_launch.argtypes = [B, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    lib.cs_batch_capture.argtypes = [B, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
+    lib.cs_batch_replay.argtypes = [B, ctypes.c_void_p]
+    lib.cs_batch_graph_nodes.argtypes = [B, P(ctypes.c_size_t)]
+    lib.cs_batch_redo_pixels.argtypes = [B, ctypes.c_void_p, P(ctypes.c_long), P(ctypes.c_long)]
+    lib.cs_batch_set_redo_capacity.argtypes = [B, ctypes.c_long]
+    lib.cs_batch_timer_ms.restype = ctypes.c_double
+    lib.cs_batch_timer_ms.argtypes = [B]
+    lib.cs_batch_run_host.argtypes = [B, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
+    lib.cs_calc_batch.argtypes = [B, P(CsParams), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_void_p, ctypes.c_size_t]
     return lib
 
 
@@ -320,3 +341,121 @@ class SasCalc_GENERIC_calculation:
         n = ctypes.c_long()
         self._check(self._lib.cs_prepared_pixels(self._h, ctypes.byref(n)))
         return n.value
+
+
+def params_from_mapping(mapping):
+    """A cs_params from reference keys, applied to the console defaults."""
+    c = SasCalc_GENERIC_calculation()
+    try:
+        c.setParams(mapping)
+        return c.params()
+    finally:
+        c.cleanup()
+
+
+class SasCalcBatch:
+    """Many parameter sets per launch (cs_batch_* of the C ABI).
+
+    ``prepare(sets)`` takes reference-key dictionaries or CsParams; the images
+    of all sets then lie in one float64 buffer (``info()``, ``layout(k)``).
+    ``launch`` / ``capture`` + ``replay`` enqueue all images into a device
+    buffer; ``calc`` is the host-buffer form returning one 2D array per set."""
+
+    def __init__(self):
+        self._lib = load_library()
+        self._b = self._lib.cs_batch_create()
+        if not self._b:
+            raise CrystalScatterError(CS_ERR_ALLOC, "cs_batch_create failed")
+        self.n = 0
+
+    def __del__(self):
+        self.cleanup()
+
+    def cleanup(self):
+        if getattr(self, "_b", None):
+            self._lib.cs_batch_destroy(self._b)
+            self._b = None
+
+    def _check(self, rc):
+        if rc != CS_OK:
+            raise CrystalScatterError(rc, self._lib.cs_batch_last_error(self._b).decode())
+        return rc
+
+    @staticmethod
+    def _array(sets):
+        arr = (CsParams * len(sets))()
+        for i, s in enumerate(sets):
+            arr[i] = s if isinstance(s, CsParams) else params_from_mapping(s)
+        return arr
+
+    def prepare(self, sets, bIgnoreNewSwitch=False, bIgnoreCbs=False, host_threads=0):
+        arr = self._array(sets)
+        self._check(self._lib.cs_batch_prepare(self._b, arr, len(sets), int(bool(bIgnoreNewSwitch)),
+                                               int(bool(bIgnoreCbs)), int(host_threads)))
+        self.n = len(sets)
+        return self
+
+    def prep_ms(self):
+        return self._lib.cs_batch_timer_ms(self._b)
+
+    def info(self):
+        """(total doubles of the image buffer, calculated pixels, key groups)"""
+        d, p, g = ctypes.c_size_t(), ctypes.c_long(), ctypes.c_int()
+        self._check(self._lib.cs_batch_info(self._b, ctypes.byref(d), ctypes.byref(p), ctypes.byref(g)))
+        return d.value, p.value, g.value
+
+    def layout(self, k):
+        """(offset, xmin, xmax, ymin, ymax) of set k's image in the buffer"""
+        o = ctypes.c_size_t()
+        d = [ctypes.c_int() for _ in range(4)]
+        self._check(self._lib.cs_batch_layout(self._b, int(k), ctypes.byref(o), *[ctypes.byref(x) for x in d]))
+        return (o.value,) + tuple(x.value for x in d)
+
+    def launch(self, d_out_ptr, n_doubles, stream_ptr=0, mode=CS_MODE_FP64, schedule=CS_SCHED_PERSISTENT):
+        self._check(self._lib.cs_batch_launch(self._b, ctypes.c_void_p(d_out_ptr), int(n_doubles),
+                                              ctypes.c_void_p(stream_ptr), int(mode), int(schedule)))
+
+    def capture(self, d_out_ptr, n_doubles, mode=CS_MODE_FP64, schedule=CS_SCHED_PERSISTENT):
+        self._check(self._lib.cs_batch_capture(self._b, ctypes.c_void_p(d_out_ptr), int(n_doubles), int(mode),
+                                               int(schedule)))
+
+    def replay(self, stream_ptr=0):
+        self._check(self._lib.cs_batch_replay(self._b, ctypes.c_void_p(stream_ptr)))
+
+    def graph_nodes(self):
+        n = ctypes.c_size_t()
+        self._check(self._lib.cs_batch_graph_nodes(self._b, ctypes.byref(n)))
+        return n.value
+
+    def redo_pixels(self, stream_ptr=0):
+        """(guarded pixels of the last mixed persistent run, list capacity per group)"""
+        n, cap = ctypes.c_long(), ctypes.c_long()
+        self._check(self._lib.cs_batch_redo_pixels(self._b, ctypes.c_void_p(stream_ptr), ctypes.byref(n),
+                                                   ctypes.byref(cap)))
+        return n.value, cap.value
+
+    def set_redo_capacity(self, entries_per_group):
+        self._check(self._lib.cs_batch_set_redo_capacity(self._b, int(entries_per_group)))
+
+    def split(self, flat):
+        """Per-set 2D views of a flat image buffer laid out by this batch."""
+        out = []
+        for k in range(self.n):
+            o, x0, x1, y0, y1 = self.layout(k)
+            out.append(flat[o:o + (x1 - x0) * (y1 - y0)].reshape(y1 - y0, x1 - x0))
+        return out
+
+    def run_host(self, mode=CS_MODE_FP64, out=None):
+        """Computes the prepared sets (persistent schedule) into a host buffer
+        (flat float64, allocated when not given) and returns it."""
+        total = self.info()[0]
+        if out is None:
+            out = np.empty(total, dtype=np.float64)
+        self._check(self._lib.cs_batch_run_host(self._b, int(mode), out.ctypes.data, out.size))
+        return out
+
+    def calc(self, sets, bIgnoreNewSwitch=False, bIgnoreCbs=False, mode=CS_MODE_FP64):
+        """Host in, host out: prepares and computes all sets and returns one
+        image per set."""
+        self.prepare(sets, bIgnoreNewSwitch, bIgnoreCbs)
+        return [a.copy() for a in self.split(self.run_host(mode))]

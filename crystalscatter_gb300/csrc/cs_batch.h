@@ -1,0 +1,73 @@
+// cs_batch.h — many parameter sets in one launch (internal).
+//
+// A batch holds N prepared parameter sets of possibly different detector
+// sizes; their images lie one after another in one output buffer. Sets are
+// grouped by dispatch key (one specialised kernel per key). Within a group the
+// calculated pixels of all sets are cut into tiles of CS_BATCH_TILE pixels,
+// numbered set after set. A persistent kernel (one resident grid) takes the
+// next tile from a device counter until the group's tiles run out, so uneven
+// set sizes and uneven per-pixel cost balance across the SMs without the host.
+// The mixed form appends guarded pixels, as (set, pixel) pairs, to one redo
+// list shared by all sets; a second persistent kernel recomputes them in FP64.
+#ifndef CS_BATCH_H
+#define CS_BATCH_H
+
+#include <cuda_runtime.h>
+
+#include "cs_launch.h"
+#include "cs_mixed.h"
+
+namespace cs {
+
+#define CS_BATCH_TILE 256
+
+// The keys that have batch kernels (X-macro over the specialised pixel functions).
+#define CS_FOR_EACH_KEY(M)           \
+    M(CS_KEY_SPHERE_NONE_ISO)        \
+    M(CS_KEY_SPHERE_GAUSS_FCC_GAUSS) \
+    M(CS_KEY_CYL_NONE_GAUSS)         \
+    M(CS_KEY_CYL_NONE_ZDIR)          \
+    M(CS_KEY_CYL_GAUSS_BCT_ZDIR)
+
+// One set as the batch kernels see it (array in device memory).
+struct BatchSetDev {
+    const cs_prepared *prep;     // the set's prepared block
+    const cs_delta_node *delta;  // the set's delta node table (orientation average only) or null
+    csm::PeakTab peaks;          // compact reflection tables (mixed form)
+    long out_offset;             // first double of the set's image in the output buffer
+    long tile_begin;             // first tile of the set within its group
+    long npix;                   // calculated pixels (zzmax-zzmin)*(iimax-iimin)
+    int nx;                      // zzmax - zzmin
+    int key;                     // dispatch key
+};
+
+// Sets [set_begin, set_end) of the device array share one key and own tiles
+// [0, tiles) of the group.
+struct BatchGroup {
+    int key = 0;
+    int set_begin = 0, set_end = 0;
+    long tiles = 0;
+};
+
+struct BatchRedo {
+    int *d_count = nullptr;   // one counter per group
+    int2 *d_list = nullptr;   // per group a slice of cap entries: (set, pixel of the calculated region)
+    long cap = 0;             // entries per group
+};
+
+// Persistent mixed-precision launch over one group followed by the FP64 redo
+// of its guarded pixels. counter must be zero when the launch starts.
+int launch_batch_mixed(const BatchSetDev *d_sets, const BatchGroup &g, int group_index, unsigned long long *d_counter,
+                       const cs_chi_node *d_chi, double *d_out, const BatchRedo &R, int grid, cudaStream_t s);
+// Persistent FP64 launch over one group (the drop-in arithmetic).
+int launch_batch_fp64(const BatchSetDev *d_sets, const BatchGroup &g, unsigned long long *d_counter,
+                      const cs_chi_node *d_chi, double *d_out, int grid, cudaStream_t s);
+int launch_batch_redo(const BatchSetDev *d_sets, int key, const cs_chi_node *d_chi, double *d_out,
+                      const int *d_count, const int2 *d_list, long cap, cudaStream_t s);
+// Resident blocks per SM of the persistent kernels for a key (0 if unsupported).
+int batch_blocks_per_sm_fp64(int key);
+int batch_blocks_per_sm_mixed(int key);
+
+}  // namespace cs
+
+#endif

@@ -68,18 +68,43 @@ __device__ __forceinline__ void convert_idx2q(const cs_prepared &P, int ihex, in
 // power series 1 + sum_n c[n] (q^2)^n with the reference's qq = qq*q*q
 // and its stop at relative increment < 1e-4 (the loops of the formpq/formfq
 // libraries)
+// The power series below stop at the first term whose relative increment is
+// below 1e-4, a discrete decision on a sum that can cancel by many orders of
+// magnitude; a different rounding of one partial sum can move the stop by one
+// term (a jump of ~1e-4 relative). Their products and sums are therefore
+// written with __dmul_rn/__dadd_rn, which are never fused into a
+// multiply-add, so they round as the reference's separate operations in every
+// translation unit, also in those compiled with contraction.
 __device__ __forceinline__ double series_q(const double *__restrict__ c, double q, int nmax) {
     double pqsum = 1.0;
     double oldpqsum = 0.0;
     double qq = 1.0;
     for (int nser = 1; nser <= nmax; nser++) {
-        qq = qq * q * q;
-        pqsum = pqsum + c[nser] * qq;
+        qq = __dmul_rn(__dmul_rn(qq, q), q);
+        pqsum = __dadd_rn(pqsum, __dmul_rn(c[nser], qq));
         double delser = fabs((pqsum - oldpqsum) / pqsum);
         if (delser < 0.0001) break;
         oldpqsum = pqsum;
     }
     return pqsum;
+}
+
+// 1D series in (qxs+qys)^2 of the z-direction cylinder (formpq_partCylinder
+// ordis 6, Source/sc_lib_formpq_partCylinder.h:93-124; formfq_partCylinder
+// ordis 6, Source/sc_lib_formfq_partCylinder.h:55-87).
+__device__ __forceinline__ double series_zdir(const double *__restrict__ c, double qxs, double qys) {
+    double pql = 1.0;
+    double oldpqsum = 0.0;
+    double qqnn = 1.0;
+    const double s = qxs + qys;
+    for (int nser = 1; nser <= 120; nser++) {
+        qqnn = __dmul_rn(__dmul_rn(qqnn, s), s);
+        pql = __dadd_rn(pql, __dmul_rn(c[nser], qqnn));
+        const double delser = fabs((pql - oldpqsum) / pql);
+        if (delser < 0.0001) break;
+        oldpqsum = pql;
+    }
+    return pql;
 }
 
 // ------------------------------------------------------------------ spheres
@@ -295,6 +320,12 @@ __device__ inline double qromb_chi(const Ctx &C, const ChiArgs &A, double cd, do
 
 // qrombdeltac(i0 = 4): Gaussian-weighted delta integral of qrombchid.
 __device__ inline double qromb_delta_cyl(const Ctx &C, const ChiArgs &A) {
+    // Orientation cases outside 1..4 (the 0-based general case) reach no
+    // branch of the chi integrand, which is then 0 at every node: every
+    // trapezoid estimate is +0, the Neville extrapolation gives +0, and the
+    // reference's loop stops at j = 5 on |I| < 1e-100 with +0. That value is
+    // returned directly.
+    if (A.i1 < 1 || A.i1 > 4) return 0.0;
     const cs_prepared &P = *C.P;
     const double a = 0.0, b = P.romb_delta_b;
     const double dbeta = P.romb_dbeta;
@@ -382,19 +413,24 @@ __device__ inline double cyl_double_series(const cs_prepared &P, double qxs, dou
     qxn[0] = 1.0;
     qyn[0] = 1.0;
     for (int nser = 1; nser <= 120; nser++) {
-        qxn[nser] = qxn[nser - 1] * qxs * qxs;
-        qyn[nser] = qyn[nser - 1] * qys * qys;
+        qxn[nser] = __dmul_rn(__dmul_rn(qxn[nser - 1], qxs), qxs);
+        qyn[nser] = __dmul_rn(__dmul_rn(qyn[nser - 1], qys), qys);
         double binsum = 0.0;
+        // binsum += c * a * b, rounded as ((c*a)*b) then the sum
         if (variant == 0) {
-            for (int mser = 0; mser <= nser; mser++) binsum += P.carr11pm[nser - mser][mser] * qxn[mser] * qyn[nser - mser];
+            for (int mser = 0; mser <= nser; mser++)
+                binsum = __dadd_rn(binsum, __dmul_rn(__dmul_rn(P.carr11pm[nser - mser][mser], qxn[mser]), qyn[nser - mser]));
         } else if (variant == 1) {
-            for (int mser = 0; mser <= nser; mser++) binsum += P.carr11pm[nser - mser][mser] * qyn[mser] * qxn[nser - mser];
+            for (int mser = 0; mser <= nser; mser++)
+                binsum = __dadd_rn(binsum, __dmul_rn(__dmul_rn(P.carr11pm[nser - mser][mser], qyn[mser]), qxn[nser - mser]));
         } else if (variant == 2) {
-            for (int mser = 0; mser <= nser; mser++) binsum += P.carr11pm[mser][nser - mser] * qyn[mser] * qxn[nser - mser];
+            for (int mser = 0; mser <= nser; mser++)
+                binsum = __dadd_rn(binsum, __dmul_rn(__dmul_rn(P.carr11pm[mser][nser - mser], qyn[mser]), qxn[nser - mser]));
         } else {
-            for (int mser = 0; mser <= nser; mser++) binsum += P.carr11pm[mser][nser - mser] * qxn[mser] * qyn[nser - mser];
+            for (int mser = 0; mser <= nser; mser++)
+                binsum = __dadd_rn(binsum, __dmul_rn(__dmul_rn(P.carr11pm[mser][nser - mser], qxn[mser]), qyn[nser - mser]));
         }
-        pql += carr1[nser] * binsum;
+        pql = __dadd_rn(pql, __dmul_rn(carr1[nser], binsum));
         double delser = fabs((pql - oldpqsum) / pql);
         if (delser < 0.0001) break;
         oldpqsum = pql;
@@ -412,16 +448,7 @@ __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, d
             pql = 1.0;
         else {
             if (q < (0.6 * P.limq[1])) {
-                pql = 1.0;
-                double oldpqsum = 0.0;
-                double qqnn = 1.0;
-                for (int nser = 1; nser <= 120; nser++) {
-                    qqnn = qqnn * (qxs + qys) * (qxs + qys);
-                    pql += P.carrp[0][nser] * qqnn;
-                    const double delser = fabs((pql - oldpqsum) / pql);
-                    if (delser < 0.0001) break;
-                    oldpqsum = pql;
-                }
+                pql = series_zdir(P.carrp[0], qxs, qys);
             } else {
                 const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
                 pql = (1 / (2.0 * zl * (zl - 1))) * (1 / (arglq * arglq)) *
@@ -478,17 +505,7 @@ __device__ inline double formfq_cylinder(const Ctx &C, double limql, double qxs,
             pql = 1.0;
         else {
             if (limql < (0.6 * P.limqf[1])) {
-                double pqsum = 1.0;
-                double oldpqsum = 0.0;
-                double qqnn = 1.0;
-                for (int nser = 1; nser <= 120; nser++) {
-                    qqnn = qqnn * (qxs + qys) * (qxs + qys);
-                    pqsum = pqsum + P.carrf[0][nser] * qqnn;
-                    const double delser = fabs((pqsum - oldpqsum) / pqsum);
-                    if (delser < 0.0001) break;
-                    oldpqsum = pqsum;
-                }
-                pql = pqsum;
+                pql = series_zdir(P.carrf[0], qxs, qys);
             } else {
                 const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
                 pql = (1 / (2.0 * zl * (zl - 1))) * (1 / (arglq * arglq)) *

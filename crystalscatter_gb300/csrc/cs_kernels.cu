@@ -10,6 +10,7 @@
 
 #include <cstdint>
 
+#include "cs_batch.cuh"
 #include "cs_fp64.cuh"
 #include "cs_launch.h"
 #include "cs_mixed.h"
@@ -108,6 +109,57 @@ __global__ void __launch_bounds__(128) k_redo(Ctx C, double *__restrict__ out, i
         double qx, qy, qz;
         convert_idx2q(P, ihex, i, qx, qy, qz);
         out[(long)(ihex - P.xmin) + (long)xstride * (long)(i - P.ymin)] = calc_pixel<KEY>(C, qx, qy, qz);
+    }
+}
+
+
+// Persistent FP64 kernel over one group of a batch: tiles of CS_BATCH_TILE
+// pixels from the group's counter, pixel arithmetic as k_image.
+template <int KEY>
+__global__ void __launch_bounds__(CS_BATCH_TILE) k_batch_fp64(const cs::BatchSetDev *__restrict__ sets, int set_begin,
+                                                              int set_end, long tiles,
+                                                              unsigned long long *__restrict__ counter,
+                                                              const cs_chi_node *__restrict__ chi,
+                                                              double *__restrict__ out) {
+    int cur = set_begin;
+    long tile;
+    int k;
+    while (cs::batch_next_tile(sets, set_begin, set_end, tiles, counter, cur, tile, k)) {
+        const cs::BatchSetDev &S = sets[k];
+        const long t = (tile - S.tile_begin) * CS_BATCH_TILE + threadIdx.x;
+        if (t >= S.npix) continue;
+        const cs_prepared &P = *S.prep;
+        const Ctx C{S.prep, chi, S.delta};
+        const int ihex = P.zzmin + (int)(t % S.nx);
+        const int i = P.iimin + (int)(t / S.nx);
+        double qx, qy, qz;
+        convert_idx2q(P, ihex, i, qx, qy, qz);
+        const double v = calc_pixel<KEY>(C, qx, qy, qz);
+        out[S.out_offset + (long)(ihex - P.xmin) + (long)(P.xmax - P.xmin) * (long)(i - P.ymin)] = v;
+    }
+}
+
+// FP64 recomputation of the guarded pixels of a batch group: list entries are
+// (set, linear pixel of the set's calculated region).
+template <int KEY>
+__global__ void __launch_bounds__(128) k_batch_redo(const cs::BatchSetDev *__restrict__ sets,
+                                                    const cs_chi_node *__restrict__ chi, double *__restrict__ out,
+                                                    const int *__restrict__ redo_count,
+                                                    const int2 *__restrict__ redo_list, long redo_cap) {
+    long n = *redo_count;
+    if (n > redo_cap) n = redo_cap;
+    for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += (long)gridDim.x * blockDim.x) {
+        const int2 e = redo_list[r];
+        const cs::BatchSetDev &S = sets[e.x];
+        const cs_prepared &P = *S.prep;
+        const Ctx C{S.prep, chi, S.delta};
+        const long t = e.y;
+        const int ihex = P.zzmin + (int)(t % S.nx);
+        const int i = P.iimin + (int)(t / S.nx);
+        double qx, qy, qz;
+        convert_idx2q(P, ihex, i, qx, qy, qz);
+        out[S.out_offset + (long)(ihex - P.xmin) + (long)(P.xmax - P.xmin) * (long)(i - P.ymin)] =
+            calc_pixel<KEY>(C, qx, qy, qz);
     }
 }
 
@@ -313,6 +365,50 @@ int launch_fit(const DevSet &D, const cs_prepared &P, const double *d_data, doub
     k_fit_reduce1<<<nb, 256, 0, s>>>(d_fqs, nbuf, R.d_psum, R.d_pcnt, R.d_pnan);
     k_fit_reduce2<<<1, 32, 0, s>>>(R.d_psum, R.d_pcnt, R.d_pnan, nb, R.d_sum, R.d_cnt, R.d_nan);
     return cudaGetLastError() == cudaSuccess ? CS_OK : CS_ERR_CUDA;
+}
+
+
+// ---- batch launchers -------------------------------------------------------
+
+int launch_batch_fp64(const BatchSetDev *d_sets, const BatchGroup &g, unsigned long long *d_counter,
+                      const cs_chi_node *d_chi, double *d_out, int grid, cudaStream_t s) {
+    if (g.tiles <= 0) return CS_OK;
+    switch (g.key) {
+#define CS_CASE(K)                                                                                              \
+    case K:                                                                                                     \
+        cs64::k_batch_fp64<K><<<grid, CS_BATCH_TILE, 0, s>>>(d_sets, g.set_begin, g.set_end, g.tiles, d_counter, \
+                                                             d_chi, d_out);                                     \
+        break;
+        CS_FOR_EACH_KEY(CS_CASE)
+#undef CS_CASE
+    default: return CS_ERR_UNSUPPORTED;
+    }
+    return cudaGetLastError() == cudaSuccess ? CS_OK : CS_ERR_CUDA;
+}
+
+int launch_batch_redo(const BatchSetDev *d_sets, int key, const cs_chi_node *d_chi, double *d_out, const int *d_count,
+                      const int2 *d_list, long cap, cudaStream_t s) {
+    const int grid = sm_count() * 4;
+    switch (key) {
+#define CS_CASE(K)                                                                                  \
+    case K: cs64::k_batch_redo<K><<<grid, 128, 0, s>>>(d_sets, d_chi, d_out, d_count, d_list, cap); break;
+        CS_FOR_EACH_KEY(CS_CASE)
+#undef CS_CASE
+    default: return CS_ERR_UNSUPPORTED;
+    }
+    return cudaGetLastError() == cudaSuccess ? CS_OK : CS_ERR_CUDA;
+}
+
+int batch_blocks_per_sm_fp64(int key) {
+    int n = 0;
+    switch (key) {
+#define CS_CASE(K) \
+    case K: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cs64::k_batch_fp64<K>, CS_BATCH_TILE, 0); break;
+        CS_FOR_EACH_KEY(CS_CASE)
+#undef CS_CASE
+    default: return 0;
+    }
+    return n;
 }
 
 }  // namespace cs

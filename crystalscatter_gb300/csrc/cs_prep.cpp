@@ -14,6 +14,7 @@
 // value decides branches per pixel. This translation unit must be compiled
 // without floating-point contraction (-ffp-contract=off).
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -34,6 +35,28 @@ constexpr double kEps9 = 0.000000001; // eps9, Source/sc_math.h:45
 constexpr double kEps3 = 0.001;       // eps3, Source/sc_math.h:39
 
 inline double sqr(double x) { return x * x; }
+
+// log2 of a positive double, good to ~1e-15 absolute: the exponent from frexp
+// (exact), the mantissa in [0.5, 1) through log2.
+inline double lg2(double v) {
+    int e;
+    const double m = std::frexp(v, &e);
+    return e + std::log2(m);
+}
+
+// log2 of the largest term that `acc += term` (term computed in long double,
+// sum rounded to double) provably leaves unchanged, with a factor 16 to spare:
+// a term below 1/8 ulp of a non-zero acc keeps the long-double sum strictly
+// inside acc's rounding interval (also below a power of two, where the
+// interval is ulp/4 wide on the lower side); a non-negative term below 2^-1075
+// added to +0 rounds back to +0.
+inline double negligible_lg2(double acc) {
+    if (acc == 0.0) return -1076.0 - 4.0;
+    int e;
+    std::frexp(acc, &e);
+    const int ulp = std::max(e - 53, -1074);
+    return ulp - 3 - 4.0;
+}
 
 // cospi(v) of Source/sc_math.h:52 (1-2*(v&1)).
 inline int cospi_i(int v) { return 1 - 2 * (v & 1); }
@@ -475,22 +498,50 @@ bool Prep::coefficients() {
                 z12v[0] = 1.0;
                 double xrn_n = 1.0;
                 long double xln_n = 1.0;
+                // log2 of the denominator factors, for the negligible-term test
+                // (sums of log2 k: the long-double factorials overflow double)
+                double lgfkv[kNmax + 1], lgfk2v[kNmax + 1];
+                lgfkv[0] = 0.0;   // fkv[0] = 1
+                lgfk2v[0] = 0.0;  // fk2v[0] = 1
+                const double lgnorm = P.norm > 0 ? lg2(P.norm) : 0.0;
+                const double lgintl = intl_const > 0 ? lg2(intl_const) : 0.0;
+                const double lim0 = negligible_lg2(0.0);
+                double lgpw11[kNmax + 1], lgpw13[kNmax + 1];
+                for (int e = 0; e <= nmax; e++) {
+                    lgpw11[e] = pw11[e] > 0 ? lg2(pw11[e]) : 0.0;  // unused where the product is 0
+                    lgpw13[e] = pw13[e] > 0 ? lg2(pw13[e]) : 0.0;
+                }
                 for (int n = 1; n <= nmax; n++) {
                     z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
                     z12vl[n] = z12vl[n - 1] * ((zl + 1) - 2 + 2 * n) * ((zl + 1) - 1 + 2 * n);
                     fkv[n] = fkv[n - 1] * n;
                     fk2v[n] = fk2v[n - 1] * (2 * n - 1) * (2 * n);
+                    lgfkv[n] = lgfkv[n - 1] + std::log2((double)n);
+                    lgfk2v[n] = lgfk2v[n - 1] + std::log2((double)(2 * n - 1)) + std::log2((double)(2 * n));
                     gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
                     xln_n = -xln_n * xl2z;
                     xrn_n = -xrn_n * xr2z;
                     for (int m = 0; m <= n; m++) {
                         double sump = 0.0;
+                        double lim = lim0;  // negligible_lg2(sump)
                         for (int ll = 0; ll <= m; ll++) {
                             const double num = pw11[ll] * pw13[m - ll] * intl_const;
                             // a zero numerator adds exactly 0 (the long-double
                             // denominator is finite and non-zero): skipped
                             if (num == 0.0) continue;
+                            // A positive term too small to change the double sum
+                            // is skipped as well (the result is the same bits).
+                            // With the polar axis in the detector plane the terms
+                            // ll >= 1 carry pw11 = (cos 90deg)^(2ll) ~ 1e-33^ll.
+                            if (num > 0.0 && P.norm > 0) {
+                                // log2 of the two-rounding product from its factors
+                                // (directly where subnormal rounding could matter)
+                                const double lgnum = num < 1e-290 ? lg2(num) : lgpw11[ll] + lgpw13[m - ll] + lgintl;
+                                if (lgnum - (2.0 * ll + lgfk2v[m - ll] + lgfkv[n - m + ll] + lgfkv[ll] + lgnorm) < lim)
+                                    continue;
+                            }
                             sump += num / (pw4[ll] * fk2v[m - ll] * fkv[n - m + ll] * fkv[ll] * P.norm);
+                            lim = negligible_lg2(sump);
                         }
                         P.carr11pm[n][m] = pw4[m] * pw21[n - m] * sump / (fkv[n - m]);
                     }

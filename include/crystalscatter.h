@@ -159,6 +159,52 @@ size_t cs_prepared_size(void);
 int cs_prepare_params(const cs_params *p, int ign_new_switch, int ign_cbs, void *out, size_t out_size, char *err,
                       size_t errlen);
 
+/* ---- Batches: many parameter sets per launch --------------------------------
+   The reference evaluates parameter sets one at a time (a sweep, or the
+   simplex fit's vertices, Source/sc_simplexfit2d.cpp:54-62, each through
+   doCalculation). A batch prepares N sets at once (host threads), keeps them
+   resident on the device, and computes all their images either with one
+   launch per set (CS_SCHED_PLAIN, what N calls of the single-set interface
+   issue) or with one persistent launch per dispatch key fed by a device tile
+   queue (CS_SCHED_PERSISTENT). Each set is checked as doCalculation checks it
+   (checkAllParameters(bIgnoreCbs)); the first rejected set fails the batch
+   with its index in the message. Quadrant flags of each set apply to the
+   default quadrant state (as cs_prepare_params). Images lie one after another
+   in one buffer, each starting at a multiple of 32 doubles; cs_batch_layout
+   gives offset and extents per set. cs_calc_batch is the host-buffer form.
+   Results are the same as the single-set calls give for each set. */
+typedef struct cs_batch cs_batch;
+#define CS_SCHED_PLAIN 0
+#define CS_SCHED_PERSISTENT 1
+cs_batch *cs_batch_create(void);
+void cs_batch_destroy(cs_batch *b);
+const char *cs_batch_last_error(cs_batch *b);
+/* host_threads: threads for the host preparation (0 = all hardware threads). */
+int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_switch, int ign_cbs, int host_threads);
+int cs_batch_info(cs_batch *b, size_t *total_doubles, long *total_pixels, int *ngroups);
+int cs_batch_layout(cs_batch *b, int k, size_t *offset, int *xmin, int *xmax, int *ymin, int *ymax);
+/* Enqueue all images of the prepared batch into d_out (device memory,
+   n_doubles capacity) on stream (NULL = the batch's stream); asynchronous. */
+int cs_batch_launch(cs_batch *b, double *d_out, size_t n_doubles, void *stream, int mode, int schedule);
+/* Capture the same work as a CUDA graph (once) and replay it. The graph
+   writes into the d_out given at capture; preparing the batch again drops it. */
+int cs_batch_capture(cs_batch *b, double *d_out, size_t n_doubles, int mode, int schedule);
+int cs_batch_replay(cs_batch *b, void *stream);
+int cs_batch_graph_nodes(cs_batch *b, size_t *n);
+/* Mixed persistent form: guarded pixels of the last run (waits for stream).
+   CS_ERR_SIZE when the redo list overflowed (some pixels then keep their
+   FP32 value): raise the capacity (entries per key group, 0 = automatic:
+   a quarter of the group's pixels, at least 2^20) and run again. */
+int cs_batch_redo_pixels(cs_batch *b, void *stream, long *n, long *capacity);
+int cs_batch_set_redo_capacity(cs_batch *b, long entries_per_group);
+double cs_batch_timer_ms(cs_batch *b); /* host preparation time of the last cs_batch_prepare */
+/* Host-buffer forms: run the prepared batch (persistent schedule, a redo
+   overflow handled internally) and copy all images into out; cs_calc_batch
+   prepares first. */
+int cs_batch_run_host(cs_batch *b, int mode, double *out, size_t n_doubles);
+int cs_calc_batch(cs_batch *b, const cs_params *sets, int nsets, int ign_new_switch, int ign_cbs, int mode,
+                  double *out, size_t n_doubles);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,7 +94,15 @@ def compare_to_reference(got, ref, cond, mask=None, tol=1e-10, envelope=100.0):
     bad = mask & (rel > allowed)
     well = mask & ~ill
     fin_well = well & np.isfinite(rel)
+    worst = []
+    if bad.any():
+        idx = np.flatnonzero(bad.ravel())
+        order = np.argsort(-np.nan_to_num(rel.ravel()[idx], nan=np.inf))[:5]
+        for j in idx[order]:
+            worst.append((int(j), float(rel.ravel()[j]), float(cond.ravel()[j]), float(got.ravel()[j]),
+                          float(ref.ravel()[j])))
     return {
+        "worst_bad": worst,
         "n": int(mask.sum()),
         "n_ill": int((mask & ill).sum()),
         "n_bad": int(bad.sum()),

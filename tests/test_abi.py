@@ -53,3 +53,16 @@ def test_cpu_thread_count_is_rejected():
         raised = e.code == cs.CS_ERR_PARAM
     assert raised
     c.cleanup()
+
+
+def test_batch_without_gpu_fails_loudly():
+    # no CPU path: preparing a batch needs the device (pinned staging, device arena)
+    import pytest
+    if cs.SasCalc_GENERIC_calculation.gpuAvailable():
+        pytest.skip("a GPU is present")
+    b = cs.SasCalcBatch()
+    with pytest.raises(cs.CrystalScatterError) as e:
+        b.prepare([{"ComboBoxParticle": 0, "GridPoints": 8}])
+    assert e.value.code == cs.CS_ERR_CUDA
+    assert "no CUDA device" in str(e.value)
+    b.cleanup()
