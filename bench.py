@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-extra", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--sweep-sets", type=int, default=4096, help="parameter sets of the batched sweep (0 = skip)")
+    ap.add_argument("--sweep-steps", type=int, default=2)
     return ap.parse_args()
 
 
@@ -140,6 +142,123 @@ def time_kernel(calc, torch, d_out, n, steps, warmup, flush, mode=0):
     return sum(times), times
 
 
+def fp_peaks():
+    """Nominal arithmetic peaks of the GPU from its SM count and clock: FP64
+    (2 DFMA per SM per clock, FMA = 2 flops) and FP32 (128 lanes per SM)."""
+    import torch
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    sms = props.multi_processor_count
+    mhz = 2070.0
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            mhz = float(json.load(f).get("sm_max_mhz", mhz))
+    return {"fp64_tflops": sms * 2 * 2 * mhz * 1e6 / 1e12, "fp32_tflops": sms * 128 * 2 * mhz * 1e6 / 1e12,
+            "sms": sms, "sm_mhz": mhz, "kind": "nominal (SMs x lanes x max clock)"}
+
+
+def load_ops():
+    p = os.path.join(ROOT, "crystalscatter_gb300", "config_ops.json")
+    with open(p) as f:
+        return json.load(f)["workloads"]
+
+
+def rel_stats(img, ref):
+    import numpy as np
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rel = np.abs(img - ref) / np.maximum(np.abs(ref), 1e-300)
+    fin = np.isfinite(ref) & np.isfinite(img)
+    mism = int(((~np.isfinite(ref)) != (~np.isfinite(img))).sum())
+    r = rel[fin]
+    return {"max": float(r.max()) if r.size else 0.0, "median": float(np.median(r)) if r.size else 0.0,
+            "p99_99": float(np.quantile(r, 0.9999)) if r.size else 0.0, "nonfinite_mismatch": mism}
+
+
+def config_row(cs, torch, name, params, flush, ops, peaks, steps):
+    """Mixed and FP64 kernel rates of one workload, accuracy of mixed vs FP64
+    over the full image, and the compute roofline fractions."""
+    c = cs.SasCalc_GENERIC_calculation()
+    c.setParams(params)
+    c.doCalculation(0, False, False, mode=cs.CS_MODE_FP64)
+    ref = c.data()
+    c.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)
+    img = c.data()
+    redo = c.mixed_redo_pixels()
+    n = img.size
+    npix = c.prepared_pixels()
+    d = torch.empty(n, dtype=torch.float64, device="cuda")
+    row = {"pixels": npix, "accuracy_mixed_vs_fp64": rel_stats(img, ref), "fp64_redo_pixels": redo}
+    for mname, mode, k in (("mixed", cs.CS_MODE_MIXED, steps), ("fp64", cs.CS_MODE_FP64, max(2, steps // 4))):
+        tk, _ = time_kernel(c, torch, d, n, k, 2, flush, mode=mode)
+        row[mname + "_pixels_per_s"] = npix * k / tk
+        row[mname + "_ms_per_image"] = 1e3 * tk / k
+    row["speedup_mixed_over_fp64"] = row["mixed_pixels_per_s"] / row["fp64_pixels_per_s"]
+    fl = ops[name]["flops_per_pixel"]
+    row["compute"] = {"flops_per_pixel": fl,
+                      "fp64_dropin_tflops": row["fp64_pixels_per_s"] * fl / 1e12,
+                      "fp64_dropin_frac_of_fp64_peak": row["fp64_pixels_per_s"] * fl / 1e12 / peaks["fp64_tflops"],
+                      "mixed_tflops": row["mixed_pixels_per_s"] * fl / 1e12,
+                      "mixed_frac_of_fp32_peak": row["mixed_pixels_per_s"] * fl / 1e12 / peaks["fp32_tflops"]}
+    c.cleanup()
+    return row
+
+
+def sweep(cs, torch, C, nsets, ops, peaks, steps):
+    """Config 4: nsets seeded cylinder/BCT parameter sets of detector size
+    128..1024 in one batch; one persistent launch per step (captured as a CUDA
+    graph) against one plain launch per set, in both precision modes."""
+    import numpy as np
+    sets = C.bct_sweep(nsets)
+    b = cs.SasCalcBatch()
+    t0 = time.perf_counter()
+    b.prepare(sets, bIgnoreCbs=True)
+    t_prep = time.perf_counter() - t0
+    total, npix, groups = b.info()
+    out = torch.empty(total, dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream()
+    sp = s.cuda_stream
+
+    def timed(fn, k):
+        fn()
+        s.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(k):
+            fn()
+        e.record(s)
+        e.synchronize()
+        return a.elapsed_time(e) / 1e3 / k
+
+    row = {"sets": nsets, "pixels": npix, "key_groups": groups, "host_prep_s": t_prep,
+           "image_buffer_gb": total * 8 / 1e9}
+    b.capture(out.data_ptr(), total, mode=cs.CS_MODE_MIXED, schedule=cs.CS_SCHED_PERSISTENT)
+    row["graph_nodes_persistent"] = b.graph_nodes()
+    t_graph = timed(lambda: b.replay(sp), steps)
+    redo, cap = b.redo_pixels(sp)
+    mixed = out.cpu().numpy()
+    t_mp = timed(lambda: b.launch(out.data_ptr(), total, sp, cs.CS_MODE_MIXED, cs.CS_SCHED_PLAIN), 1)
+    t_fp = timed(lambda: b.launch(out.data_ptr(), total, sp, cs.CS_MODE_FP64, cs.CS_SCHED_PERSISTENT), 1)
+    fp64 = out.cpu().numpy()
+    t_fplain = timed(lambda: b.launch(out.data_ptr(), total, sp, cs.CS_MODE_FP64, cs.CS_SCHED_PLAIN), 1)
+    fl = ops["bct_sweep"]["flops_per_pixel"]
+    row.update({
+        "mixed_persistent_graph_s": t_graph, "mixed_persistent_graph_pixels_per_s": npix / t_graph,
+        "mixed_plain_launches_s": t_mp, "fp64_persistent_s": t_fp, "fp64_plain_launches_s": t_fplain,
+        "fp64_plain_launches_pixels_per_s": npix / t_fplain,
+        "speedup_graph_mixed_over_plain_fp64": t_fplain / t_graph,
+        "speedup_persistent_over_plain_fp64": t_fplain / t_fp,
+        "fp64_redo_pixels": redo, "accuracy_mixed_vs_fp64": rel_stats(mixed, fp64),
+        "compute": {"flops_per_pixel_sampled": fl,
+                    "mixed_frac_of_fp32_peak": npix / t_graph * fl / 1e12 / peaks["fp32_tflops"],
+                    "fp64_plain_frac_of_fp64_peak": npix / t_fplain * fl / 1e12 / peaks["fp64_tflops"]},
+        "launches": {"persistent_graph": 2 * groups, "plain": nsets},
+    })
+    b.cleanup()
+    del out
+    return row, redo
+
+
 def native(args):
     import numpy as np
     import torch
@@ -154,6 +273,8 @@ def native(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     params = C.WORKLOADS[WORKLOAD]
+    ops = load_ops()
+    peaks = fp_peaks()
 
     calc = cs.SasCalc_GENERIC_calculation()
     calc.setParams(params)
@@ -175,11 +296,8 @@ def native(args):
     calc.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)
     mixed_img = calc.data()
     redo = calc.mixed_redo_pixels()
-    with np.errstate(invalid="ignore", divide="ignore"):
-        rel = np.abs(mixed_img - ref_img) / np.maximum(np.abs(ref_img), 1e-300)
-    rel = rel[np.isfinite(rel)]
-    max_rel = float(rel.max()) if rel.size else 0.0
-    assert max_rel <= 1e-5, f"mixed path exceeds 1e-5 vs FP64: {max_rel}"
+    acc = rel_stats(mixed_img, ref_img)
+    assert acc["max"] <= 1e-5 and acc["nonfinite_mismatch"] == 0, f"mixed path exceeds 1e-5 vs FP64: {acc}"
 
     clocks = ClockSampler(local)
     if world > 1:
@@ -198,6 +316,7 @@ def native(args):
         calc.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)
         _ = calc.data()
     t_e2e = time.perf_counter() - t0
+    prep_ms = calc.higResTimerElapsedPrep
     clk = clocks.stop()
     if world > 1:
         import torch.distributed as dist
@@ -214,6 +333,7 @@ def native(args):
     launch_s = t_kernel / args.steps
     bytes_per_launch = 8.0 * npix
     achieved = bytes_per_launch / launch_s / 1e9
+    fl = ops[WORKLOAD]["flops_per_pixel"]
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -221,34 +341,30 @@ def native(args):
         "config": {"workload": "pCyl_lNon_oGau 512x512 (cylinder r=5 L=60, Gaussian 15 deg, phi=30)",
                    "pixels_per_step": npix, "mode": "mixed FP32/FP64, <=1e-5 vs FP64",
                    "l2": "256 MB write between timed steps (flush)", "parallelism": f"replicas x{world}"},
-        "accuracy": {"max_rel_vs_fp64": max_rel, "fp64_redo_pixels": redo},
+        "accuracy": {"mixed_vs_fp64": acc, "fp64_redo_pixels": redo},
         "fp64_dropin": {"value": npix * args.steps * world / t_fp64, "unit": UNIT,
                         "ms_per_step": 1e3 * t_fp64 / args.steps},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(calc._lib.cs_prepared_size()),
-                "d2h_bytes_per_step": int(8 * n)},
+                "d2h_bytes_per_step": int(8 * n), "host_prep_ms": prep_ms},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
-                     "note": f"peak {peak_kind}; 8 B written per pixel: the kernels are bound by arithmetic "
-                             f"(FP64 pipe for the drop-in, FP32/SFU for the mixed path), see profiles/"},
+                     "note": f"peak {peak_kind}; 8 B written per pixel: the kernels are bound by arithmetic, "
+                             f"see compute_roofline and profiles/"},
+        "compute_roofline": {"flops_per_pixel": fl, "achieved_tflops": value * fl / 1e12,
+                             "fp32_peak_tflops": peaks["fp32_tflops"],
+                             "frac_of_fp32_peak": value * fl / 1e12 / peaks["fp32_tflops"],
+                             "fp64_peak_tflops": peaks["fp64_tflops"], "peaks": peaks["kind"],
+                             "flops_source": "crystalscatter_gb300/config_ops.json (counted on the oracle)"},
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
     }
     if not args.no_extra and rank == 0:
-        extra = {}
-        for name in ("sphere", "cyl_gauss_x", "sphere_fcc"):
-            c2 = cs.SasCalc_GENERIC_calculation()
-            c2.setParams(C.WORKLOADS[name])
-            c2.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)
-            n2 = c2.data().size
-            d2 = torch.empty(n2, dtype=torch.float64, device="cuda")
-            rec = {"pixels": c2.prepared_pixels()}
-            for mname, mode, k in (("mixed", cs.CS_MODE_MIXED, max(3, args.steps // 4)), ("fp64", cs.CS_MODE_FP64, 2)):
-                tk, _ = time_kernel(c2, torch, d2, n2, k, 1, flush, mode=mode)
-                rec[mname + "_pixels_per_s"] = rec["pixels"] * k / tk
-                rec[mname + "_ms_per_image"] = 1e3 * tk / k
-            extra[name] = rec
-            c2.cleanup()
-        result["extra"] = extra
+        rows = {}
+        for name in ("sphere", "cyl_gauss", "cyl_gauss_x", "sphere_fcc"):
+            rows[name] = config_row(cs, torch, name, C.WORKLOADS[name], flush, ops, peaks, max(3, args.steps // 2))
+        result["configs"] = rows
+        if args.sweep_sets > 0:
+            result["sweep"], _ = sweep(cs, torch, C, args.sweep_sets, ops, peaks, max(1, args.sweep_steps))
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(params, args.cpu_seconds)
         print(json.dumps(result))
@@ -260,15 +376,16 @@ def native(args):
 
 def cpu_baseline(params, seconds):
     """The oracle port of the reference on all host cores, on a bounded sample
-    of the same workload: whole images repeated until `seconds` elapse."""
+    of the same workload: whole calculations (host preparation, as the
+    reference's doCalculation runs it, then the image) repeated until
+    `seconds` elapse."""
     from oracle import cpu_oracle
-    import numpy as np
-    P = cpu_oracle.prepare(params)
     nthreads = os.cpu_count() or 1
     t0 = time.perf_counter()
     pix = 0
     reps = 0
     while True:
+        P = cpu_oracle.prepare(params)
         _, n = cpu_oracle.image_prepared(P, nthreads)
         pix += n
         reps += 1
@@ -276,7 +393,7 @@ def cpu_baseline(params, seconds):
             break
     dt = time.perf_counter() - t0
     return {"value": pix / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{reps} full 512x512 images of the same workload, {dt:.1f} s"}
+            "sample": f"{reps} full 512x512 calculations (preparation + image) of the same workload, {dt:.1f} s"}
 
 
 def reference(args):
@@ -286,13 +403,13 @@ def reference(args):
     from crystalscatter_gb300 import configs as C
     from oracle import cpu_oracle
     params = C.WORKLOADS[WORKLOAD]
-    P = cpu_oracle.prepare(params)
     nthreads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_oracle.image_prepared(P, nthreads)
+        cpu_oracle.image_prepared(cpu_oracle.prepare(params), nthreads)
     t0 = time.perf_counter()
     pix = 0
     for _ in range(args.steps):
+        P = cpu_oracle.prepare(params)  # doCalculation prepares on every call
         _, n = cpu_oracle.image_prepared(P, nthreads)
         pix += n
     dt = time.perf_counter() - t0
@@ -305,8 +422,8 @@ def reference(args):
                    "pixels_per_step": pix // args.steps, "parallelism": f"{nthreads} host threads"},
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": f"{args.steps} full images, the reference's algorithm restated in C "
-                                   f"(oracle/cs_oracle.c), row-parallel over host threads"},
+                         "sample": f"{args.steps} full calculations (host preparation + image), the reference's "
+                                   f"algorithm restated in C (oracle/cs_oracle.c), row-parallel over host threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))

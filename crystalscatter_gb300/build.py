@@ -19,9 +19,11 @@ LIB = os.path.join(OUT, "libcrystalscatter.so")
 
 HOST_SOURCES = ["cs_prep.cpp", "cs_params.cpp", "cs_capi.cpp", "cs_batch.cpp"]
 CUDA_SOURCES = ["cs_kernels.cu", "cs_mixed.cu"]
-# the FP64 drop-in keeps the reference's separate multiply and add roundings;
-# the mixed kernels use fused multiply-add
-FMAD = {"cs_kernels.cu": "false", "cs_mixed.cu": "true"}
+# No automatic multiply-add contraction in either unit: the FP64 drop-in keeps
+# the reference's separate multiply and add roundings, and the mixed kernels
+# share its FP64 functions (pixel geometry, power series, math library calls),
+# which must round identically there; FP32 code asks for fmaf where it wants one
+FMAD = {"cs_kernels.cu": "false", "cs_mixed.cu": "false"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -19,8 +19,6 @@ Values that the benchmark text leaves open are fixed here and stated: HKLmax 5
 for FCC and 3 for BCT, Debye-Scherrer peak width on, beam centre at the image
 centre (CenterBeam with BeamPos 0,0), all four quadrants, no image expansion.
 """
-import math
-import random
 
 BASE = dict(
     ComboBoxInterior=0, I0=1.0, Base=0.0, iso=0.0, ifluc=0.0, rfluc=0.0,
@@ -70,25 +68,69 @@ def scaled(cfg, gridpoints):
     return c
 
 
+class MT19937_64:
+    """The 64-bit Mersenne Twister (std::mt19937_64: Matsumoto & Nishimura's
+    MT19937-64 parameters), so the sweep's parameter sets follow from the
+    stated seeds exactly as a C++ std::mt19937_64 would draw them."""
+
+    N, M = 312, 156
+    A = 0xB5026F5AA96619E9
+    UPPER, LOWER = 0xFFFFFFFF80000000, 0x7FFFFFFF
+    MASK = (1 << 64) - 1
+
+    def __init__(self, seed=5489):
+        mt = [0] * self.N
+        mt[0] = seed & self.MASK
+        for i in range(1, self.N):
+            mt[i] = (6364136223846793005 * (mt[i - 1] ^ (mt[i - 1] >> 62)) + i) & self.MASK
+        self.mt, self.i = mt, self.N
+
+    def _twist(self):
+        mt = self.mt
+        for i in range(self.N):
+            x = (mt[i] & self.UPPER) | (mt[(i + 1) % self.N] & self.LOWER)
+            xa = x >> 1
+            if x & 1:
+                xa ^= self.A
+            mt[i] = mt[(i + self.M) % self.N] ^ xa
+        self.i = 0
+
+    def __call__(self):
+        if self.i >= self.N:
+            self._twist()
+        y = self.mt[self.i]
+        self.i += 1
+        y ^= (y >> 29) & 0x5555555555555555
+        y ^= (y << 17) & 0x71D67FFFEDA60000
+        y ^= (y << 37) & 0xFFF7EEE000000000
+        y ^= y >> 43
+        return y & self.MASK
+
+    def uniform(self, a, b):
+        """a + (b-a) u with u = the top 53 bits of one draw times 2^-53, in [0, 1)."""
+        return a + (b - a) * ((self() >> 11) * (1.0 / 9007199254740992.0))
+
+    def choice4(self, seq):
+        """one of four items from the top two bits of one draw"""
+        return seq[self() >> 62]
+
+
 def bct_set(k, sizes=(128, 256, 512, 1024)):
-    """Parameter set k of the BCT sweep: a generator seeded with 0xC5A70000+k
-    draws the detector size and the particle/lattice parameters uniformly in
-    the stated ranges (radius 3-10 nm, length 20-100 nm, a 20-60 nm,
-    c/a 1.0-1.6, Schulz sigma 0.05-0.20 for radius and length, orientation
-    width 2-20 deg)."""
-    rng = random.Random(0xC5A70000 + k)
-    n = sizes[rng.randrange(len(sizes))]
+    """Parameter set k of the cylinder/BCT sweep: std::mt19937_64 seeded with
+    0xC5A70000+k draws, in this order, the detector size N (uniform over
+    128/256/512/1024), radius U[3,10] nm, length U[20,100] nm, a U[20,60] nm,
+    c/a U[1.0,1.6], the Schulz sigma of radius and length U[0.05,0.20] and the
+    orientation width U[2,20] deg. Pixel 0.172 mm, 3 m, 0.154 nm, HKLmax 3."""
+    rng = MT19937_64(0xC5A70000 + k)
+    n = rng.choice4(sizes)
     radius = rng.uniform(3.0, 10.0)
     length = rng.uniform(20.0, 100.0)
     a = rng.uniform(20.0, 60.0)
     c = a * rng.uniform(1.0, 1.6)
     sig = rng.uniform(0.05, 0.20)
     azi = rng.uniform(2.0, 20.0)
-    cfg = dict(CYL_BCT_FIXED, EditRadius=radius, Length=length, uca=a, ucb=a, ucc=c, EditSigma=sig, SigmaL=sig,
-               EditAzi=azi, GridPoints=n // 2, EditPixelNoX=n, EditPixelNoY=n)
-    # keep the q-range of a 1024 detector at 0.172 mm
-    cfg["EditPixelX"] = cfg["EditPixelY"] = 0.172 * 1024 / n
-    return cfg
+    return dict(CYL_BCT_FIXED, EditRadius=radius, Length=length, uca=a, ucb=a, ucc=c, EditSigma=sig, SigmaL=sig,
+                EditAzi=azi, GridPoints=n // 2, EditPixelNoX=n, EditPixelNoY=n)
 
 
 def bct_sweep(count=4096):

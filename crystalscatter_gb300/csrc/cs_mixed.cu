@@ -38,11 +38,18 @@ __device__ __forceinline__ float powp1f(float x, float e) { return exp2f(e * log
 // decision guard: true when v is within `band` relative of threshold t
 __device__ __forceinline__ bool near(double v, double t, double band) { return fabs(v - t) <= band * fabs(t); }
 
-// Detector geometry in FP64 without transcendentals: cos(phi)sin(theta) =
-// xdet/L, sin(phi)sin(theta) = ydet/L, cos(theta) = det/L, L = |(xdet,ydet,det)|.
-// Agrees with the reference's atan2/sin/cos form to a few ulp.
+// Detector geometry. The sphere without lattice (a cheap pixel whose series
+// is well conditioned) takes it in FP64 without transcendentals:
+// cos(phi)sin(theta) = xdet/L, sin(phi)sin(theta) = ydet/L, cos(theta) = det/L,
+// L = |(xdet,ydet,det)|, which agrees with the reference's atan2/sin/cos form to
+// a few ulp. Every other key takes the drop-in's own convert_idx2q (same
+// rounding, this unit is compiled without contraction as the drop-in is): their
+// power series can cancel by up to 1e15, where a few-ulp change of q moves the
+// reference's own value by O(1), and the mixed path then reproduces the FP64
+// value exactly instead of a different rounding of it.
+template <int KEY>
 __device__ __forceinline__ void q_of_pixel(const cs_prepared &P, int ihex, int i, double &qx, double &qy, double &qz) {
-    if (P.use1d || !P.usebeamstop) {
+    if (KEY != CS_KEY_SPHERE_NONE_ISO || P.use1d || !P.usebeamstop) {
         cs64::convert_idx2q(P, ihex, i, qx, qy, qz);
         return;
     }
@@ -109,7 +116,7 @@ __device__ float cyl_len_factor(float a, float z) {
         float term = 1.0f, sum = 1.0f;
 #pragma unroll
         for (int j = 1; j <= 9; j++) {
-            term *= x * (m + 2 * j) * (m + 2 * j + 1) / ((2 * j + 1) * (2 * j + 2));
+            term *= x * (m + 2 * j) * (m + 2 * j + 1) * (1.0f / ((2 * j + 1) * (2 * j + 2)));
             sum += term;
         }
         return sum;
@@ -138,22 +145,30 @@ struct ChiArgsF {
     int i1;
 };
 
-__device__ __forceinline__ float chi_integrand_f(const ChiArgsF &A, float cx, float sx, float cd, float sd) {
+// Where |m*a| < 1e-3 (m = z-1) the reference's closed form of the length
+// factor, 1 - cos(m atan 2a)/(1+4a^2)^(m/2) in FP64, cancels to below ~1e-8
+// relative accuracy: its value there is rounding noise that the FP64 drop-in
+// reproduces and this FP32 series form does not. Such a node flags the pixel
+// for the FP64 redo.
+__device__ __forceinline__ float chi_integrand_f(const ChiArgsF &A, float cx, float sx, float cd, float sd,
+                                                 bool &guard) {
     const float eps = 1e-10f;
     float s;
     switch (A.i1) {
     case 1: {
-        const float mlx1 = A.p11 * cx * sd + A.p12 * sx * sd + A.p13 * cd;
-        const float mlx2 = A.p21 * sx * sd + A.p22 * cx * sd + A.p23 * cd;
-        s = A.qx * mlx1 + A.qy * mlx2 + eps;
+        const float mlx1 = fmaf(fmaf(A.p11, cx, A.p12 * sx), sd, A.p13 * cd);
+        const float mlx2 = fmaf(fmaf(A.p21, sx, A.p22 * cx), sd, A.p23 * cd);
+        s = fmaf(A.qx, mlx1, fmaf(A.qy, mlx2, eps));
         break;
     }
-    case 2: s = A.qx * cd - A.qy * sx * sd + eps; break;
-    case 3: s = A.qx * sx * sd + A.qy * cd + eps; break;
-    case 4: s = A.qx * sx * sd - A.qy * cx * sd + eps; break;
+    case 2: s = fmaf(A.qx, cd, fmaf(-A.qy * sx, sd, eps)); break;
+    case 3: s = fmaf(A.qx * sx, sd, fmaf(A.qy, cd, eps)); break;
+    case 4: s = fmaf(fmaf(A.qx, sx, -A.qy * cx), sd, eps); break;
     default: return 0.0f;
     }
-    return cyl_len_factor(s * A.lz, A.z);
+    const float a = s * A.lz;
+    if (fabsf((A.z - 1.0f) * a) < 1e-3f) guard = true;
+    return cyl_len_factor(a, A.z);
 }
 
 // Neville extrapolation to 0 of the last five trapezoid estimates, whose
@@ -194,8 +209,8 @@ __device__ double qromb_chi_f(const Ctx &C, const ChiArgsF &A, float cd, float s
     double pq = 0.0;
     {
         const cs_chi_node n0 = C.chi[0], n1 = C.chi[1];
-        const float pa = chi_integrand_f(A, (float)n0.c, (float)n0.s, cd, sd);
-        const float pb = chi_integrand_f(A, (float)n1.c, (float)n1.s, cd, sd);
+        const float pa = chi_integrand_f(A, (float)n0.c, (float)n0.s, cd, sd, guard);
+        const float pb = chi_integrand_f(A, (float)n1.c, (float)n1.s, cd, sd, guard);
         cur = 0.5 * b * ((double)pa + (double)pb);
         cnt = 1;
     }
@@ -207,7 +222,7 @@ __device__ double qromb_chi_f(const Ctx &C, const ChiArgsF &A, float cd, float s
             const cs_chi_node *nd = C.chi + CS_NODE_OFFSET(j);
             for (int k = 0; k < cnt; k++) {
                 const cs_chi_node n = nd[k];
-                sum.add(chi_integrand_f(A, (float)n.c, (float)n.s, cd, sd));
+                sum.add(chi_integrand_f(A, (float)n.c, (float)n.s, cd, sd, guard));
             }
         } else {
             const double del = b / cnt;
@@ -215,7 +230,7 @@ __device__ double qromb_chi_f(const Ctx &C, const ChiArgsF &A, float cd, float s
             for (int k = 0; k < cnt; k++) {
                 float s, c;
                 sincosf((float)x, &s, &c);
-                sum.add(chi_integrand_f(A, c, s, cd, sd));
+                sum.add(chi_integrand_f(A, c, s, cd, sd, guard));
                 x += del;
             }
         }
@@ -246,7 +261,12 @@ __device__ double qromb_delta_f(const Ctx &C, const ChiArgsF &A, bool &guard) {
     const double inv2pi = 1.0 / (2.0 * M_PI);
     {
         const cs_delta_node n0 = C.dnode[0], n1 = C.dnode[1];
-        const double pa = n0.w * qromb_chi_f(C, A, (float)n0.c, (float)n0.s, guard) * inv2pi;
+        // the delta = 0 endpoint has weight sin(0) = 0: its chi integral only
+        // matters when it is not finite, so its nodes raise no guard
+        bool g0 = false;
+        const double c0 = qromb_chi_f(C, A, (float)n0.c, (float)n0.s, g0);
+        if (n0.w != 0.0 || !isfinite(c0)) guard = guard || g0 || !isfinite(c0);
+        const double pa = n0.w * c0 * inv2pi;
         const double pb = n1.w * qromb_chi_f(C, A, (float)n1.c, (float)n1.s, guard) * inv2pi;
         cur = 0.5 * b * (pa + pb);
         cnt = 1;
@@ -339,10 +359,10 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
             const float d = (qf - qh) + ql;
             if (d < -dmax) break;
             const float4 v = __ldg(T.av + i);  // unit q_hkl (x,y,z) and g3/peaknorm1
-            const float c = fx * v.x + fy * v.y + fz * v.z;
+            const float c = fmaf(fx, v.x, fmaf(fy, v.y, fz * v.z));
             // myacos: the reference maps c < -1 to 0 and c > 1 to pi
             const float yphi = (c < -1.0f) ? 0.0f : ((c > 1.0f) ? (float)M_PI : acosf(c));
-            const float e = exp2f(-k * d * d - kphi * yphi * yphi);
+            const float e = exp2f(fmaf(-k * d, d, -kphi * yphi * yphi));
             s.add(e * v.w * __ldg(T.amf + i));
         }
         intens = s.value() / (M_PI * width / 2.0);
@@ -507,6 +527,39 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
     return pql * pqr;
 }
 
+// Final combination of the lattice pixel functions,
+//   I = base + I0 (szq pq + iso szqiso pqi) + tail,
+//   szq = 1 + (fq/pq)(2 pi I_aniso/V - 1) e^(-dw q^2),
+//   szqiso = 1 + (8 pi^3 I_iso/(4 pi V) - 1) e^(-ucb q^2),
+// in FP64 from FP32-accurate inputs (asymptotes: relative error ~EPS_PQ,
+// peak sums: ~EPS_PEAK, a few FP32 roundings each). Where the terms cancel
+// (szq -> 0 between peaks, I0 szq pq against base) the input errors are
+// amplified; a first-order estimate of the result's error is propagated
+// alongside, and a pixel whose estimate exceeds 5e-6 of |I| (half the 1e-5 bar)
+// is recomputed in FP64.
+#define EPS_PQ 3.0e-7
+#define EPS_PEAK 6.0e-7
+__device__ __forceinline__ double lattice_combine(const cs_prepared &P, double q, double pq, double fq, double pqi,
+                                                  double radint, double intens, double tailv, bool &guard) {
+    const double v = P.latpar[1] * P.latpar[2];
+    const double r2 = 8 * M_PI * M_PI * M_PI * radint / (4 * M_PI * v);
+    const double e2 = exp(-P.ucb * q * q);
+    const double szqiso = 1 + (r2 - 1) * e2;
+    const double r1 = 2 * M_PI * intens / v;
+    const double e1 = exp(-P.dwfactor * q * q);
+    const double ratio = fq / pq;
+    const double t = ratio * (r1 - 1) * e1;
+    const double szq = 1 + t;
+    const double res = P.base + P.izero * (szq * pq + P.iso * szqiso * pqi) + tailv;
+    // first-order error bound
+    const double dt = fabs(t) * (2 * EPS_PQ) + fabs(ratio * e1 * r1) * EPS_PEAK;
+    const double d1 = fabs(pq) * dt + fabs(szq * pq) * EPS_PQ;
+    const double d2 = fabs(P.iso) * (fabs(pqi) * fabs(r2 * e2) * EPS_PEAK + fabs(szqiso * pqi) * EPS_PQ);
+    const double bound = fabs(P.izero) * (d1 + d2);
+    if (!(bound <= 5e-6 * fabs(res))) guard = true;
+    return res;
+}
+
 template <int KEY>
 __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double qy, double qz, bool &guard) {
     const cs_prepared &P = *C.P;
@@ -521,10 +574,7 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
         const double fq = sphere_fq_mixed(P, q, guard);
         double radint, intens;
         peak_sums_f(P, T, qx, qy, qz, q, radint, intens, guard);
-        const double v = P.latpar[1] * P.latpar[2];
-        const double szqiso = 1 + (8 * M_PI * M_PI * M_PI * radint / (4 * M_PI * v) - 1) * exp(-P.ucb * q * q);
-        const double szq = 1 + (fq / pq) * (2 * M_PI * intens / v - 1) * exp(-P.dwfactor * q * q);
-        return P.base + P.izero * (szq * pq + P.iso * szqiso * pq) + tailv;
+        return lattice_combine(P, q, pq, fq, pq, radint, intens, tailv, guard);
     }
     if (KEY == CS_KEY_CYL_NONE_GAUSS) {
         double pq;
@@ -567,10 +617,8 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
         }
         double radint, intens;
         peak_sums_f(P, T, qx, qy, qz, q, radint, intens, guard);
-        const double v = P.latpar[1] * P.latpar[2];
-        const double szqiso = 1 + (8 * M_PI * M_PI * M_PI * radint / (4 * M_PI * v) - 1) * exp(-P.ucb * q * q);
-        const double szq = 1 + (fq / pq) * (2 * M_PI * intens / v - 1) * exp(-P.dwfactor * q * q);
-        return P.base + P.izero * (szq * pq + P.iso * szqiso * 1.0) + tailv;
+        // the reference's BCT function multiplies szqiso by 1 instead of pq
+        return lattice_combine(P, q, pq, fq, 1.0, radint, intens, tailv, guard);
     }
     guard = true;
     return 0.0;
@@ -588,7 +636,7 @@ __global__ void __launch_bounds__(256) k_image_mixed(Ctx C, PeakTab T, double *_
         const int ihex = P.zzmin + (int)(t % nx);
         const int i = P.iimin + (int)(t / nx);
         double qx, qy, qz;
-        q_of_pixel(P, ihex, i, qx, qy, qz);
+        q_of_pixel<KEY>(P, ihex, i, qx, qy, qz);
         bool guard = false;
         const double v = calc_mixed<KEY>(C, T, qx, qy, qz, guard);
         out[(long)(ihex - P.xmin) + (long)xstride * (long)(i - P.ymin)] = v;
@@ -622,7 +670,7 @@ __global__ void __launch_bounds__(CS_BATCH_TILE) k_batch_mixed(const cs::BatchSe
         const int ihex = P.zzmin + (int)(t % S.nx);
         const int i = P.iimin + (int)(t / S.nx);
         double qx, qy, qz;
-        q_of_pixel(P, ihex, i, qx, qy, qz);
+        q_of_pixel<KEY>(P, ihex, i, qx, qy, qz);
         bool guard = false;
         const double v = calc_mixed<KEY>(C, S.peaks, qx, qy, qz, guard);
         out[S.out_offset + (long)(ihex - P.xmin) + (long)(P.xmax - P.xmin) * (long)(i - P.ymin)] = v;

@@ -12,6 +12,8 @@ SRC = os.path.join(HERE, "cs_oracle.c")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "liboracle_cs.so")
 PROBE = os.path.join(OUT, "liboracle_cs_probe.so")
+COUNT = os.path.join(OUT, "liboracle_cs_count.so")
+COUNT_SRC = os.path.join(HERE, "count_ops.cpp")
 HDR = os.path.join(HERE, "..", "crystalscatter_gb300", "csrc", "cs_prepared.h")
 
 
@@ -29,6 +31,10 @@ def build(force=False):
     for out, extra in ((LIB, []), (PROBE, ["-DCS_ORACLE_PROBE"])):
         if force or not os.path.exists(out) or os.path.getmtime(out) < newest:
             _compile(out, extra)
+    # operation-counting build (count_ops.cpp includes cs_oracle.c unchanged)
+    if force or not os.path.exists(COUNT) or os.path.getmtime(COUNT) < max(newest, os.path.getmtime(COUNT_SRC)):
+        subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w", COUNT_SRC, "-o",
+                        COUNT, "-lpthread"], check=True)
     return LIB
 
 
