@@ -21,6 +21,7 @@
 #include "../../include/crystalscatter.h"
 #include "cs_launch.h"
 #include "cs_mixed.h"
+#include "cs_noalloc.h"
 #include "cs_params_internal.h"
 #include "cs_prep.h"
 
@@ -409,6 +410,57 @@ int cs_launch_prepared(cs_handle *h, double *d_out, size_t n_doubles, void *stre
     cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
     if (s != h->stream) cudaStreamWaitEvent(s, h->upload_done, 0);
     return run_image(h, d_out, s, mode);
+}
+
+int cs_launch_prepared_mixed_noalloc(cs_handle *h, double *d_out, size_t n_doubles, void *stream) {
+    if (!h || !d_out) return CS_ERR_PARAM;
+    if (!h->prepared) return fail(h, CS_ERR_STATE, "no prepared calculation");
+    if (image_count(h) > n_doubles) return fail(h, CS_ERR_SIZE, "output buffer too small for the image");
+    const cs_prepared &P = *h->hprep;
+    const long npix = (long)(P.zzmax - P.zzmin) * (long)(P.iimax - P.iimin);
+    if (npix > CS_NOALLOC_MAX_PIXELS) {
+        char buf[200];
+        std::snprintf(buf, sizeof buf,
+                      "image of %ld calculated pixels exceeds the allocation-free launch's fixed scratch of %d pixels",
+                      npix, CS_NOALLOC_MAX_PIXELS);
+        return fail(h, CS_ERR_SIZE, buf);
+    }
+    if (P.lattice && !h->peaks_valid)
+        return fail(h, CS_ERR_STATE,
+                    "reflection tables of this preparation are not on the device: run one CS_MODE_MIXED calculation "
+                    "on it first");
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetDevice");
+    if (cur != h->device) return fail(h, CS_ERR_STATE, "the handle's device is not the current device");
+    cs::MixedScratch S;
+    if ((e = cs::noalloc_scratch(h->device, S)) != cudaSuccess) return cuda_fail(h, e, "cudaGetSymbolAddress(scratch)");
+    cudaStream_t s = stream ? (cudaStream_t)stream : h->stream;
+    if (s != h->stream) cudaStreamWaitEvent(s, h->upload_done, 0);
+    cs::DevSet D;
+    D.d_prep = h->dprep;
+    D.d_chi = g_dchi[h->device];
+    D.d_delta = cs::needs_delta_table(P) ? h->ddelta : nullptr;
+    if (P.expand) {
+        // pixels the mirroring never writes read as 0
+        if ((e = cudaMemsetAsync(d_out, 0, sizeof(double) * image_count(h), s)) != cudaSuccess)
+            return cuda_fail(h, e, "cudaMemsetAsync");
+    }
+    csm::PeakTab T;
+    if (P.lattice) {
+        T.n_aniso = (int)h->hpeaks.aq.size();
+        T.aq = h->d_aq;
+        T.av = h->d_av;
+        T.amf = h->d_amf;
+        T.n_iso = (int)h->hpeaks.iq.size();
+        T.iq = h->d_iq;
+        T.imf = h->d_imf;
+    }
+    // clears the static counter on s, then the mixed kernel and the FP64 redo
+    const int rc = cs::launch_image_mixed(D, T, P, d_out, S, s);
+    if (rc == CS_ERR_UNSUPPORTED) return fail(h, rc, "no mixed-precision kernel for this combination");
+    if (rc != CS_OK) return cuda_fail(h, cudaGetLastError(), "kernel launch");
+    return CS_OK;
 }
 
 int cs_prepared_pixels(cs_handle *h, long *npix) {

@@ -132,6 +132,35 @@ int cs_calc_image_device(cs_handle *h, double *d_out, size_t n_doubles, void *st
                          int ign_cbs, int mode);
 /* Re-launch the last prepared calculation into d_out without host work. */
 int cs_launch_prepared(cs_handle *h, double *d_out, size_t n_doubles, void *stream, int mode);
+
+/* Allocation-free mixed-precision launch. No counterpart in the reference:
+   it exists for callers that must not allocate while they calculate, such as
+   a fit or monitoring loop that keeps its device memory fixed after set-up, or
+   one that runs work on other streams and cannot accept the device-wide
+   synchronisation of cudaFree. cs_launch_prepared(..., CS_MODE_MIXED) may
+   allocate the handle's redo list (the pixels recomputed in FP64) on first use
+   or when a larger image comes along; this variant keeps that list in a fixed
+   static device array of CS_NOALLOC_MAX_PIXELS entries instead.
+   - It calls no cudaMalloc/cudaFree and no allocating library routine (no
+     PyTorch): it enqueues memsets and kernels on `stream` (NULL = the
+     handle's stream) and returns.
+   - Requirements: a prepared handle (cs_calc_image, cs_calc_image_device or
+     cs_launch_prepared ran for the current parameters); for parameter sets
+     with a lattice, one earlier CS_MODE_MIXED call on that preparation, which
+     uploads the reflection tables (otherwise CS_ERR_STATE); the handle's
+     device is the current device (otherwise CS_ERR_STATE).
+   - Images of more than CS_NOALLOC_MAX_PIXELS calculated pixels are rejected
+     with CS_ERR_SIZE and a message naming the limit.
+   - The first call on a device does the set-up: it looks up the address of
+     the static array (cudaGetSymbolAddress), which may load the library's
+     device module. Make that first call before any stream capture.
+   - The static list is cleared (a memset on `stream`) at the start of every
+     call; the result is the same as cs_launch_prepared(..., CS_MODE_MIXED).
+   - There is one static list per device: calls whose work overlaps on the GPU
+     (other streams, other handles, other threads) race on it. Order them on
+     one stream or synchronise between them. */
+#define CS_NOALLOC_MAX_PIXELS 1048576
+int cs_launch_prepared_mixed_noalloc(cs_handle *h, double *d_out, size_t n_doubles, void *stream);
 int cs_prepared_pixels(cs_handle *h, long *npix);
 
 /* 2D fit support: setFitData (sc_calc_generic_cpu.cpp:8220), setNoFitRect

@@ -1,0 +1,100 @@
+"""The allocation-free mixed launch (cs_launch_prepared_mixed_noalloc), called
+through the C ABI, against the existing entry point (cs_calc_image with
+CS_MODE_MIXED) on the same prepared handle: two calls in a row, each within
+the mixed path's 1e-5 bar (the same kernels run, so the images agree exactly
+in practice). Also its documented rejections: images beyond the fixed scratch
+(CS_ERR_SIZE) and a lattice preparation whose reflection tables were never
+uploaded by a mixed call (CS_ERR_STATE). Independent of test order: the static
+scratch is cleared by every call."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import crystalscatter_gb300 as cs
+from crystalscatter_gb300 import configs as C
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+def entry():
+    lib = cs.load_library()
+    f = lib.cs_launch_prepared_mixed_noalloc
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    return f
+
+
+def rel(a, b):
+    with np.errstate(invalid="ignore", divide="ignore"):
+        r = np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+    fin = np.isfinite(a) & np.isfinite(b)
+    same_class = np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(np.isinf(a), np.isinf(b))
+    return (float(r[fin].max()) if fin.any() else 0.0), same_class
+
+
+CASES = {
+    "sphere_256": C.SPHERE,                                   # no lattice, algebraic geometry
+    "sphere_fcc_128": C.scaled(C.SPHERE_FCC, 64),             # lattice: reflection tables
+    "cyl_gauss_x_64": C.scaled(C.CYL_GAUSS_X, 32),            # orientation average with FP64 redo
+    "sphere_q1_expand_64": dict(C.scaled(C.SPHERE, 32), RadioButtonQ1=1, RadioButtonQ4=0, ExpandImage=1),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_noalloc_matches_existing_entry_twice(name):
+    import torch
+    f = entry()
+    c = cs.SasCalc_GENERIC_calculation()
+    c.setParams(CASES[name])
+    c.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)  # existing entry point
+    ref = c.data()
+    n = ref.size
+    d = torch.empty(n, dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    for _ in range(2):
+        d.fill_(float("nan"))
+        torch.cuda.synchronize()
+        rc = f(c._h, d.data_ptr(), n, s.cuda_stream)
+        assert rc == cs.CS_OK, c.getLastErrorMessage()
+        s.synchronize()
+        got = d.cpu().numpy().reshape(ref.shape)
+        worst, same_class = rel(got, ref)
+        assert same_class, name
+        assert worst <= TOL, (name, worst)
+    c.cleanup()
+
+
+def test_noalloc_rejects_image_beyond_scratch():
+    import torch
+    f = entry()
+    c = cs.SasCalc_GENERIC_calculation()
+    c.setParams(C.scaled(C.SPHERE, 1024))  # 2048 x 2048 = 4,194,304 pixels
+    c.doCalculation(0, False, False, mode=cs.CS_MODE_FP64)
+    n = c.data().size
+    assert n > 1048576
+    d = torch.empty(n, dtype=torch.float64, device="cuda")
+    rc = f(c._h, d.data_ptr(), n, None)
+    assert rc == cs.CS_ERR_SIZE
+    assert "1048576" in c.getLastErrorMessage()
+    c.cleanup()
+
+
+def test_noalloc_needs_uploaded_reflection_tables():
+    import torch
+    f = entry()
+    c = cs.SasCalc_GENERIC_calculation()
+    c.setParams(C.scaled(C.SPHERE_FCC, 16))
+    c.doCalculation(0, False, False, mode=cs.CS_MODE_FP64)  # prepared, tables never uploaded
+    n = c.data().size
+    d = torch.empty(n, dtype=torch.float64, device="cuda")
+    assert f(c._h, d.data_ptr(), n, None) == cs.CS_ERR_STATE
+    c.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)
+    ref = c.data()
+    assert f(c._h, d.data_ptr(), n, None) == cs.CS_OK
+    torch.cuda.synchronize()
+    worst, same_class = rel(d.cpu().numpy().reshape(ref.shape), ref)
+    assert same_class and worst <= TOL
+    c.cleanup()
