@@ -15,7 +15,8 @@ import numpy as np
 
 __all__ = [
     "CsParams", "SasCalc_GENERIC_calculation", "SasCalcBatch", "CrystalScatterError", "load_library",
-    "library_path", "params_from_mapping", "CS_MODE_FP64", "CS_MODE_MIXED", "CS_SCHED_PLAIN", "CS_SCHED_PERSISTENT",
+    "library_path", "params_from_mapping", "simplex_fit", "simplex_minimize", "CS_MODE_FP64", "CS_MODE_MIXED", "CS_SCHED_PLAIN",
+    "CS_SCHED_PERSISTENT", "CS_FIT_SEQUENTIAL", "CS_FIT_BATCHED",
 ]
 
 CS_OK = 0
@@ -30,6 +31,8 @@ CS_MODE_FP64 = 0
 CS_MODE_MIXED = 1
 CS_SCHED_PLAIN = 0
 CS_SCHED_PERSISTENT = 1
+CS_FIT_SEQUENTIAL = 0
+CS_FIT_BATCHED = 1
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -88,6 +91,23 @@ class CsParams(ctypes.Structure):
 _lib = None
 
 
+class CsFitParam(ctypes.Structure):
+    """cs_fit_param (include/crystalscatter.h)"""
+    _fields_ = [("key", ctypes.c_char * 48), ("min", ctypes.c_double), ("max", ctypes.c_double),
+                ("fitstart", ctypes.c_double), ("fitres", ctypes.c_double), ("used", ctypes.c_int),
+                ("fitvalid", ctypes.c_int)]
+
+
+class CsFitReport(ctypes.Structure):
+    """cs_fit_report (include/crystalscatter.h)"""
+    _fields_ = [("repetitions", ctypes.c_int), ("aborted", ctypes.c_int), ("images", ctypes.c_long),
+                ("chi2", ctypes.c_double), ("ms", ctypes.c_double), ("info", ctypes.c_char * 256)]
+
+
+_OBJECTIVE = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_int,
+                              ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
+
+
 def _sig(lib):
     H = ctypes.c_void_p
     P = ctypes.POINTER
@@ -140,6 +160,15 @@ def _sig(lib):
     lib.cs_batch_timer_ms.restype = ctypes.c_double
     lib.cs_batch_timer_ms.argtypes = [B]
     lib.cs_batch_run_host.argtypes = [B, ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t]
+    lib.cs_batch_set_fit.argtypes = [B, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_void_p]
+    lib.cs_batch_fit_chi2.argtypes = [B, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.cs_simplex_fit.argtypes = [P(CsParams), ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                   P(CsFitParam), ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P(CsFitReport)]
+    lib.cs_launch_prepared_mixed_noalloc.argtypes = [H, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    lib.cs_simplex_minimize.argtypes = [_OBJECTIVE, ctypes.c_void_p, P(CsFitParam), ctypes.c_int, ctypes.c_double,
+                                        ctypes.c_int, ctypes.c_double, ctypes.c_int, P(CsFitReport)]
     lib.cs_calc_batch.argtypes = [B, P(CsParams), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                   ctypes.c_void_p, ctypes.c_size_t]
     return lib
@@ -445,6 +474,26 @@ class SasCalcBatch:
             out.append(flat[o:o + (x1 - x0) * (y1 - y0)].reshape(y1 - y0, x1 - x0))
         return out
 
+    def set_fit(self, data, bstop=0, border=0, nofit=None):
+        """Target image (2D, the image's size) and masks of doFitCalculation;
+        nofit: up to 4 rectangles (x0, y0, x1, y1). Prepare the batch after it."""
+        a = np.ascontiguousarray(data, dtype=np.float64)
+        h, w = a.shape
+        nf = np.full(16, -1, dtype=np.int32)
+        for i, r in enumerate(nofit or []):
+            nf[4 * i:4 * i + 4] = r
+        self._check(self._lib.cs_batch_set_fit(self._b, int(w), int(h), a.ctypes.data, int(bstop), int(border),
+                                               nf.ctypes.data))
+
+    def fit_chi2(self, mode=CS_MODE_FP64):
+        """(chi2, cnt, nancnt) arrays over the prepared sets."""
+        chi2 = np.empty(self.n, dtype=np.float64)
+        cnt = np.empty(self.n, dtype=np.int64)
+        nan = np.empty(self.n, dtype=np.int64)
+        self._check(self._lib.cs_batch_fit_chi2(self._b, int(mode), chi2.ctypes.data, cnt.ctypes.data,
+                                                nan.ctypes.data))
+        return chi2, cnt, nan
+
     def run_host(self, mode=CS_MODE_FP64, out=None):
         """Computes the prepared sets (persistent schedule) into a host buffer
         (flat float64, allocated when not given) and returns it."""
@@ -459,3 +508,66 @@ class SasCalcBatch:
         image per set."""
         self.prepare(sets, bIgnoreNewSwitch, bIgnoreCbs)
         return [a.copy() for a in self.split(self.run_host(mode))]
+
+
+def _fit_table(fit_params):
+    arr = (CsFitParam * len(fit_params))()
+    for i, fp in enumerate(fit_params):
+        arr[i].key = fp["key"].encode()
+        arr[i].min = float(fp["min"])
+        arr[i].max = float(fp["max"])
+        arr[i].fitstart = float(fp["start"])
+        arr[i].used = 1 if fp.get("used", True) else 0
+    return arr
+
+
+def _report(rep):
+    return {"repetitions": rep.repetitions, "aborted": rep.aborted, "images": rep.images, "chi2": rep.chi2,
+            "ms": rep.ms}
+
+
+def simplex_minimize(fn, fit_params, stp=0.1, maxit=100, ftol=1e-4, schedule=CS_FIT_SEQUENTIAL):
+    """The library's simplex (cs_simplex_minimize) over a Python objective:
+    fn(points) with points an (n, nparams) array in the simplex's table order
+    (fitted keys sorted, then fixed keys sorted) returns n values."""
+    lib = load_library()
+
+    def cb(points, n, m, values, ctx):
+        pts = np.ctypeslib.as_array(points, shape=(n, m)).copy()
+        v = np.asarray(fn(pts), dtype=np.float64)
+        for i in range(n):
+            values[i] = float(v[i])
+
+    cfn = _OBJECTIVE(cb)
+    arr = _fit_table(fit_params)
+    rep = CsFitReport()
+    rc = lib.cs_simplex_minimize(cfn, None, arr, len(fit_params), float(stp), int(maxit), float(ftol), int(schedule),
+                                 ctypes.byref(rep))
+    if rc != CS_OK:
+        raise CrystalScatterError(rc, rep.info.decode() or "simplex failed")
+    return {arr[i].key.decode(): arr[i].fitres for i in range(len(fit_params))}, _report(rep)
+
+
+def simplex_fit(base, data, fit_params, stp=0.1, maxit=100, ftol=1e-4, border=0, bstop=0, nofit=None,
+                mode=CS_MODE_FP64, schedule=CS_FIT_SEQUENTIAL):
+    """SasCalc_SimplexFit2D::doSimplexFit2D on the GPU (cs_simplex_fit).
+
+    base: reference-key dict or CsParams; data: 2D target of the image's size;
+    fit_params: list of dicts {key, min, max, start, used}. Returns
+    ({key: fitres}, report dict)."""
+    lib = load_library()
+    p = base if isinstance(base, CsParams) else params_from_mapping(base)
+    a = np.ascontiguousarray(data, dtype=np.float64)
+    h, w = a.shape
+    nf = np.full(16, -1, dtype=np.int32)
+    for i, r in enumerate(nofit or []):
+        nf[4 * i:4 * i + 4] = r
+    arr = _fit_table(fit_params)
+    rep = CsFitReport()
+    rc = lib.cs_simplex_fit(ctypes.byref(p), a.ctypes.data, int(w), int(h), nf.ctypes.data, arr, len(fit_params),
+                            float(stp), int(maxit), float(ftol), int(border), int(bstop), int(mode), int(schedule),
+                            ctypes.byref(rep))
+    if rc != CS_OK:
+        raise CrystalScatterError(rc, rep.info.decode() or "simplex fit failed")
+    res = {arr[i].key.decode(): arr[i].fitres for i in range(len(fit_params))}
+    return res, _report(rep)

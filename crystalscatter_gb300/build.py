@@ -17,7 +17,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libcrystalscatter.so")
 
-HOST_SOURCES = ["cs_prep.cpp", "cs_params.cpp", "cs_capi.cpp", "cs_batch.cpp"]
+HOST_SOURCES = ["cs_prep.cpp", "cs_params.cpp", "cs_capi.cpp", "cs_batch.cpp", "cs_simplex.cpp"]
 CUDA_SOURCES = ["cs_kernels.cu", "cs_mixed.cu", "cs_noalloc.cu"]
 # No automatic multiply-add contraction in either unit: the FP64 drop-in keeps
 # the reference's separate multiply and add roundings, and the mixed kernels

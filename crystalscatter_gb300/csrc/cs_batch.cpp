@@ -20,6 +20,7 @@
 #include <atomic>
 #include <chrono>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <string>
 #include <thread>
@@ -65,6 +66,8 @@ struct cs_batch {
     size_t pk_cap = 0;
     float4 *d_av = nullptr;
     size_t av_cap = 0;
+    int *d_ai = nullptr;  // latpar rows of the anisotropic reflections
+    size_t ai_cap = 0;
     cs_delta_node *d_delta = nullptr;  // one table per set that needs one
     size_t delta_cap = 0;
     const cs_chi_node *d_chi = nullptr;
@@ -83,6 +86,23 @@ struct cs_batch {
     cudaGraphExec_t graph_exec = nullptr;
     int graph_mode = -1, graph_schedule = -1;
     double *graph_out = nullptr;
+
+    // fit: shared target, masks, FQS arena, reduction, cached graph of one evaluation
+    bool fit_set = false;
+    int fit_w = 0, fit_h = 0, fit_bstop = 0, fit_border = 0;
+    int nofit[4][4];
+    double *d_fit = nullptr;
+    size_t fit_cap = 0;
+    double *d_fqs = nullptr;
+    size_t fqs_cap = 0;
+    double *d_fimg = nullptr;  // images of the evaluated sets
+    size_t fimg_cap = 0;
+    cs::BatchFitReduce fred;
+    size_t fred_sets_cap = 0;
+    double *h_fit_out = nullptr;  // pinned: chi2[n], cnt[n], nan[n]
+    size_t h_fit_cap = 0;
+    cudaGraphExec_t fit_exec = nullptr;
+    std::vector<long long> fit_graph_sig;
 
     double t_prep = 0;
     bool prepared = false;
@@ -268,6 +288,7 @@ void cs_batch_destroy(cs_batch *b) {
     cudaFree(b->dsets);
     cudaFree(b->d_pk);
     cudaFree(b->d_av);
+    cudaFree(b->d_ai);
     cudaFree(b->d_delta);
     cudaFree(b->d_chi_own);
     cudaFree(b->d_counters);
@@ -275,6 +296,17 @@ void cs_batch_destroy(cs_batch *b) {
     cudaFree(b->redo.d_list);
     cudaFree(b->plain_scratch.d_count);
     cudaFree(b->plain_scratch.d_list);
+    if (b->fit_exec) cudaGraphExecDestroy(b->fit_exec);
+    cudaFree(b->d_fit);
+    cudaFree(b->d_fqs);
+    cudaFree(b->d_fimg);
+    cudaFree(b->fred.d_psum);
+    cudaFree(b->fred.d_pcnt);
+    cudaFree(b->fred.d_pnan);
+    cudaFree(b->fred.d_sum);
+    cudaFree(b->fred.d_cnt);
+    cudaFree(b->fred.d_nan);
+    if (b->h_fit_out) cudaFreeHost(b->h_fit_out);
     if (b->hprep) cudaFreeHost(b->hprep);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -320,7 +352,21 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
             int expand;
             const int cq = quadrants_of(sets[k], expand);
             cs_prepared &P = b->hprep[k];
-            status[k] = cs::prepare(sets[k], cq, expand, ign_new_switch, ign_cbs, 1, &P, errs[k]);
+            // a batch prepared for fitting skips checkAllParameters, as
+            // doFitCalculation does (Source/sc_calc_generic_cpu.cpp:1334-1341)
+            status[k] = cs::prepare(sets[k], cq, expand, ign_new_switch, ign_cbs, b->fit_set ? 0 : 1, &P, errs[k]);
+            if (status[k] == CS_OK && b->fit_set) {
+                P.fit_width = b->fit_w;
+                P.fit_height = b->fit_h;
+                P.fit_bstop = b->fit_bstop;
+                P.fit_border = b->fit_border;
+                for (int r = 0; r < 4; r++) {
+                    P.nofit_x0[r] = b->nofit[r][0];
+                    P.nofit_y0[r] = b->nofit[r][1];
+                    P.nofit_x1[r] = b->nofit[r][2];
+                    P.nofit_y1[r] = b->nofit[r][3];
+                }
+            }
             if (status[k] == CS_OK && !cs::key_supported(P)) {
                 status[k] = CS_ERR_UNSUPPORTED;
                 char buf[160];
@@ -390,12 +436,15 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
     }
     if ((rc = grow(b, b->d_pk, b->pk_cap, std::max<size_t>(nf, 1), "cudaMalloc(peak arena)"))) return rc;
     if ((rc = grow(b, b->d_av, b->av_cap, std::max<size_t>(nv, 1), "cudaMalloc(peak vectors)"))) return rc;
+    if ((rc = grow(b, b->d_ai, b->ai_cap, std::max<size_t>(nv, 1), "cudaMalloc(peak rows)"))) return rc;
     if ((rc = grow(b, b->d_delta, b->delta_cap, std::max<size_t>(nd, 1) * CS_NODE_COUNT, "cudaMalloc(delta tables)")))
         return rc;
     std::vector<float> pk;
     pk.reserve(nf);
     std::vector<float4> av;
     av.reserve(nv);
+    std::vector<int> ai;
+    ai.reserve(nv);
     std::vector<cs_delta_node> dt;
     if (nd) dt.resize(nd * CS_NODE_COUNT);
     b->hsets.assign(nsets, cs::BatchSetDev{});
@@ -424,7 +473,9 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
             S.peaks.aq = put(H.aq);
             S.peaks.amf = put(H.amf);
             S.peaks.av = b->d_av + av.size();
+            S.peaks.aidx = b->d_ai + ai.size();
             av.insert(av.end(), H.av.begin(), H.av.end());
+            ai.insert(ai.end(), H.aidx.begin(), H.aidx.end());
             S.peaks.n_iso = (int)H.iq.size();
             S.peaks.iq = put(H.iq);
             S.peaks.imf = put(H.imf);
@@ -454,6 +505,8 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
         return cuda_fail(b, e, "upload peak arena");
     if (!av.empty() && (e = cudaMemcpy(b->d_av, av.data(), sizeof(float4) * av.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
         return cuda_fail(b, e, "upload peak vectors");
+    if (!ai.empty() && (e = cudaMemcpy(b->d_ai, ai.data(), sizeof(int) * ai.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(b, e, "upload peak rows");
     if (nd && (e = cudaMemcpy(b->d_delta, dt.data(), sizeof(cs_delta_node) * dt.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
         return cuda_fail(b, e, "upload delta tables");
     if ((e = cudaMemcpy(b->dsets, b->hsets.data(), sizeof(cs::BatchSetDev) * (size_t)nsets, cudaMemcpyHostToDevice)) != cudaSuccess)
@@ -587,6 +640,144 @@ int cs_batch_redo_pixels(cs_batch *b, void *stream, long *n, long *capacity) {
 }
 
 double cs_batch_timer_ms(cs_batch *b) { return b ? b->t_prep : 0; }
+
+int cs_batch_set_fit(cs_batch *b, int width, int height, const double *data, int bstop, int border,
+                     const int *nofit) {
+    if (!b) return CS_ERR_PARAM;
+    if (!data || width <= 0 || height <= 0) return fail(b, CS_ERR_PARAM, "no fit data");
+    int rc = ensure_device(b);
+    if (rc) return rc;
+    const size_t n = (size_t)width * (size_t)height;
+    if ((rc = grow(b, b->d_fit, b->fit_cap, n, "cudaMalloc(fit data)"))) return rc;
+    cudaError_t e = cudaMemcpy(b->d_fit, data, sizeof(double) * n, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(b, e, "upload fit data");
+    b->fit_w = width;
+    b->fit_h = height;
+    b->fit_bstop = bstop;
+    b->fit_border = border;
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) b->nofit[r][c] = nofit ? nofit[4 * r + c] : -1;
+    b->fit_set = true;
+    b->prepared = false;  // the fit fields go into the prepared blocks
+    if (b->fit_exec) cudaGraphExecDestroy(b->fit_exec);
+    b->fit_exec = nullptr;
+    b->fit_graph_sig.clear();
+    return CS_OK;
+}
+
+int cs_batch_fit_chi2(cs_batch *b, int mode, double *chi2, long *cnt, long *nancnt) {
+    if (!b || !chi2) return CS_ERR_PARAM;
+    for (int k = 0; k < b->nsets; k++) chi2[k] = 1e20;  // the reference's value of a failed evaluation
+    if (!b->fit_set) return fail(b, CS_ERR_STATE, "cs_batch_set_fit has not been called");
+    if (!b->prepared) return fail(b, CS_ERR_STATE, "no batch prepared after cs_batch_set_fit");
+    if (mode != CS_MODE_FP64 && mode != CS_MODE_MIXED) return fail(b, CS_ERR_PARAM, "unknown precision mode");
+    const long nbuf = (long)b->fit_w * b->fit_h;
+    for (int k = 0; k < b->nsets; k++) {
+        const cs_prepared &P = b->hprep[k];
+        if (P.calc_quadrants != CS_RADQ4 || P.xmax - P.xmin != b->fit_w || P.ymax - P.ymin != b->fit_h ||
+            P.zzmin != P.xmin || P.zzmax != P.xmax || P.iimin != P.ymin || P.iimax != P.ymax || P.iimin != P.xmin)
+            return fail(b, CS_ERR_UNSUPPORTED,
+                        "set " + std::to_string(k) +
+                            ": a batch fit needs all four quadrants calculated and fit data of the image's size");
+    }
+    int rc;
+    const size_t ns = (size_t)b->nsets;
+    if ((rc = grow(b, b->d_fimg, b->fimg_cap, b->total_doubles, "cudaMalloc(fit images)"))) return rc;
+    if ((rc = grow(b, b->d_fqs, b->fqs_cap, (size_t)nbuf * ns, "cudaMalloc(fqs)"))) return rc;
+    if (ns > b->fred_sets_cap) {
+        cudaFree(b->fred.d_psum);
+        cudaFree(b->fred.d_pcnt);
+        cudaFree(b->fred.d_pnan);
+        cudaFree(b->fred.d_sum);
+        cudaFree(b->fred.d_cnt);
+        cudaFree(b->fred.d_nan);
+        b->fred = cs::BatchFitReduce{};
+        b->fred_sets_cap = 0;
+        const size_t np = ns * (size_t)b->fred.nblocks;
+        cudaError_t e;
+        if ((e = cudaMalloc(&b->fred.d_psum, sizeof(double) * np)) != cudaSuccess ||
+            (e = cudaMalloc(&b->fred.d_pcnt, sizeof(unsigned long long) * np)) != cudaSuccess ||
+            (e = cudaMalloc(&b->fred.d_pnan, sizeof(unsigned long long) * np)) != cudaSuccess ||
+            (e = cudaMalloc(&b->fred.d_sum, sizeof(double) * ns)) != cudaSuccess ||
+            (e = cudaMalloc(&b->fred.d_cnt, sizeof(unsigned long long) * ns)) != cudaSuccess ||
+            (e = cudaMalloc(&b->fred.d_nan, sizeof(unsigned long long) * ns)) != cudaSuccess)
+            return cuda_fail(b, e, "cudaMalloc(fit reduction)");
+        b->fred_sets_cap = ns;
+    }
+    if (3 * ns > b->h_fit_cap) {
+        if (b->h_fit_out) cudaFreeHost(b->h_fit_out);
+        b->h_fit_out = nullptr;
+        b->h_fit_cap = 0;
+        cudaError_t e = cudaMallocHost(&b->h_fit_out, sizeof(double) * 3 * ns);
+        if (e != cudaSuccess) return cuda_fail(b, e, "cudaMallocHost(fit results)");
+        b->h_fit_cap = 3 * ns;
+    }
+    if (mode == CS_MODE_MIXED && (rc = ensure_redo(b))) return rc;
+    // one evaluation as a CUDA graph: images (persistent schedule), FQS, chi^2,
+    // copies of the results; captured once per batch layout, replayed after
+    // every re-preparation of the same layout (a fit iteration)
+    std::vector<long long> sig = {(long long)mode, (long long)ns, (long long)b->total_doubles,
+                                  (long long)(intptr_t)b->dsets, (long long)(intptr_t)b->d_fimg,
+                                  (long long)(intptr_t)b->d_fqs, (long long)(intptr_t)b->fred.d_psum,
+                                  (long long)(intptr_t)b->h_fit_out, (long long)(intptr_t)b->redo.d_list,
+                                  (long long)b->redo.cap};
+    for (const auto &g : b->groups) {
+        sig.push_back(g.key);
+        sig.push_back(g.set_begin);
+        sig.push_back(g.set_end);
+        sig.push_back(g.tiles);
+    }
+    for (int k : b->expand_sets) sig.push_back(k);
+    cudaError_t e;
+    if (!b->fit_exec || sig != b->fit_graph_sig) {
+        if (b->fit_exec) cudaGraphExecDestroy(b->fit_exec);
+        b->fit_exec = nullptr;
+        cudaStreamSynchronize(b->stream);
+        if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+            return cuda_fail(b, e, "cudaStreamBeginCapture");
+        rc = enqueue(b, b->d_fimg, b->stream, mode, CS_SCHED_PERSISTENT);
+        if (rc == CS_OK) {
+            rc = cs::launch_batch_fit(b->dsets, (int)ns, b->d_fimg, b->d_fit, b->d_fqs, nbuf, nbuf, b->fred, b->stream);
+            if (rc == CS_OK) {
+                cudaMemcpyAsync(b->h_fit_out, b->fred.d_sum, sizeof(double) * ns, cudaMemcpyDeviceToHost, b->stream);
+                cudaMemcpyAsync(b->h_fit_out + ns, b->fred.d_cnt, sizeof(double) * ns, cudaMemcpyDeviceToHost,
+                                b->stream);
+                cudaMemcpyAsync(b->h_fit_out + 2 * ns, b->fred.d_nan, sizeof(double) * ns, cudaMemcpyDeviceToHost,
+                                b->stream);
+            } else {
+                b->err = "fit kernel launch";
+            }
+        }
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(b->stream, &g);
+        if (rc != CS_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc == CS_ERR_CUDA ? cuda_fail(b, cudaGetLastError(), "fit evaluation") : rc;
+        }
+        if (e != cudaSuccess) return cuda_fail(b, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&b->fit_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            b->fit_exec = nullptr;
+            return cuda_fail(b, e, "cudaGraphInstantiate");
+        }
+        b->fit_graph_sig = sig;
+    }
+    if ((e = cudaGraphLaunch(b->fit_exec, b->stream)) != cudaSuccess) return cuda_fail(b, e, "cudaGraphLaunch");
+    if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return cuda_fail(b, e, "fit evaluation");
+    if (mode == CS_MODE_MIXED) {
+        long n = 0;
+        if ((rc = cs_batch_redo_pixels(b, b->stream, &n, nullptr)) != CS_OK) return rc;
+    }
+    const unsigned long long *hc = (const unsigned long long *)(b->h_fit_out + ns);
+    const unsigned long long *hn = (const unsigned long long *)(b->h_fit_out + 2 * ns);
+    for (size_t k = 0; k < ns; k++) {
+        chi2[k] = b->h_fit_out[k];
+        if (cnt) cnt[k] = (long)hc[k];
+        if (nancnt) nancnt[k] = (long)hn[k];
+    }
+    return CS_OK;
+}
 
 // Host out: run the prepared batch (persistent schedule) and copy all images
 // into out. A redo-list overflow is handled by growing the list and running

@@ -64,6 +64,19 @@ int launch_batch_fp64(const BatchSetDev *d_sets, const BatchGroup &g, unsigned l
                       const cs_chi_node *d_chi, double *d_out, int grid, cudaStream_t s);
 int launch_batch_redo(const BatchSetDev *d_sets, int key, const cs_chi_node *d_chi, double *d_out,
                       const int *d_count, const int2 *d_list, long cap, cudaStream_t s);
+// Two-pass chi^2 reduction of a batch: partials [set][nblocks], results [set].
+struct BatchFitReduce {
+    int nblocks = 256;  // the single-set reduction's block count (same partials)
+    double *d_psum = nullptr;
+    unsigned long long *d_pcnt = nullptr, *d_pnan = nullptr;
+    double *d_sum = nullptr;
+    unsigned long long *d_cnt = nullptr, *d_nan = nullptr;
+};
+// FQS of every set's image (d_img, batch layout) against d_data (nbuf = fit
+// width x height doubles), then chi^2, count and NaN count per set.
+int launch_batch_fit(const BatchSetDev *d_sets, int nsets, const double *d_img, const double *d_data, double *d_fqs,
+                     long nfit, long nbuf, const BatchFitReduce &R, cudaStream_t s);
+
 // Resident blocks per SM of the persistent kernels for a key (0 if unsupported).
 int batch_blocks_per_sm_fp64(int key);
 int batch_blocks_per_sm_mixed(int key);

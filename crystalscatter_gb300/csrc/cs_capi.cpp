@@ -52,6 +52,7 @@ struct cs_handle {
     cs::HostPeaks hpeaks;
     float *d_aq = nullptr, *d_amf = nullptr, *d_iq = nullptr, *d_imf = nullptr;
     float4 *d_av = nullptr;
+    int *d_aidx = nullptr;
     size_t peak_cap = 0;
     cs::MixedScratch mscratch;
     size_t redo_cap = 0;
@@ -212,7 +213,9 @@ int ensure_mixed(cs_handle *h) {
             cudaFree(h->d_iq);
             cudaFree(h->d_imf);
             cudaFree(h->d_av);
-            if ((e = cudaMalloc(&h->d_aq, sizeof(float) * n)) != cudaSuccess ||
+            cudaFree(h->d_aidx);
+            if ((e = cudaMalloc(&h->d_aidx, sizeof(int) * n)) != cudaSuccess ||
+                (e = cudaMalloc(&h->d_aq, sizeof(float) * n)) != cudaSuccess ||
                 (e = cudaMalloc(&h->d_amf, sizeof(float) * n)) != cudaSuccess ||
                 (e = cudaMalloc(&h->d_iq, sizeof(float) * n)) != cudaSuccess ||
                 (e = cudaMalloc(&h->d_imf, sizeof(float) * n)) != cudaSuccess ||
@@ -226,6 +229,7 @@ int ensure_mixed(cs_handle *h) {
             cudaMemcpy(h->d_aq, H.aq.data(), sizeof(float) * H.aq.size(), cudaMemcpyHostToDevice);
             cudaMemcpy(h->d_amf, H.amf.data(), sizeof(float) * H.amf.size(), cudaMemcpyHostToDevice);
             cudaMemcpy(h->d_av, H.av.data(), sizeof(float4) * H.av.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(h->d_aidx, H.aidx.data(), sizeof(int) * H.aidx.size(), cudaMemcpyHostToDevice);
         }
         if (!H.iq.empty()) {
             cudaMemcpy(h->d_iq, H.iq.data(), sizeof(float) * H.iq.size(), cudaMemcpyHostToDevice);
@@ -258,6 +262,7 @@ int run_image(cs_handle *h, double *d_out, cudaStream_t s, int mode) {
             T.aq = h->d_aq;
             T.av = h->d_av;
             T.amf = h->d_amf;
+            T.aidx = h->d_aidx;
             T.n_iso = (int)h->hpeaks.iq.size();
             T.iq = h->d_iq;
             T.imf = h->d_imf;
@@ -315,6 +320,7 @@ void cs_destroy(cs_handle *h) {
     cudaFree(h->d_iq);
     cudaFree(h->d_imf);
     cudaFree(h->d_av);
+    cudaFree(h->d_aidx);
     cudaFree(h->mscratch.d_count);
     cudaFree(h->mscratch.d_list);
     if (h->himg) cudaFreeHost(h->himg);
@@ -452,6 +458,7 @@ int cs_launch_prepared_mixed_noalloc(cs_handle *h, double *d_out, size_t n_doubl
         T.aq = h->d_aq;
         T.av = h->d_av;
         T.amf = h->d_amf;
+        T.aidx = h->d_aidx;
         T.n_iso = (int)h->hpeaks.iq.size();
         T.iq = h->d_iq;
         T.imf = h->d_imf;

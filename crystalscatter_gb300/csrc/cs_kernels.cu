@@ -199,12 +199,13 @@ __global__ void k_mirror(double *img, int zmax, int xmin, int xmax, int ymin, in
 // Deterministic sum of the FQS array: NaN pixels are counted and skipped,
 // non-zero pixels counted (doFitCalculation, sc_calc_generic_cpu.cpp:1421-1434).
 // Pass 1: one partial per block; pass 2: one block combines the partials.
-__global__ void k_fit_reduce1(const double *__restrict__ fqs, long n, double *__restrict__ psum,
-                              unsigned long long *__restrict__ pcnt, unsigned long long *__restrict__ pnan) {
+__device__ __forceinline__ void fit_block_partial(const double *__restrict__ fqs, long n, double &s,
+                                                  unsigned long long &c, unsigned long long &nn) {
     __shared__ double ss[32];
     __shared__ unsigned long long sc[32], sn[32];
-    double s = 0.0;
-    unsigned long long c = 0, nn = 0;
+    s = 0.0;
+    c = 0;
+    nn = 0;
     for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
         const double v = fqs[t];
         if (isnan(v))
@@ -236,11 +237,33 @@ __global__ void k_fit_reduce1(const double *__restrict__ fqs, long n, double *__
             c += __shfl_down_sync(0xffffffffu, c, o);
             nn += __shfl_down_sync(0xffffffffu, nn, o);
         }
-        if (lane == 0) {
-            psum[blockIdx.x] = s;
-            pcnt[blockIdx.x] = c;
-            pnan[blockIdx.x] = nn;
-        }
+    }
+}
+
+__global__ void k_fit_reduce1(const double *__restrict__ fqs, long n, double *__restrict__ psum,
+                              unsigned long long *__restrict__ pcnt, unsigned long long *__restrict__ pnan) {
+    double s;
+    unsigned long long c, nn;
+    fit_block_partial(fqs, n, s, c, nn);
+    if (threadIdx.x == 0) {
+        psum[blockIdx.x] = s;
+        pcnt[blockIdx.x] = c;
+        pnan[blockIdx.x] = nn;
+    }
+}
+
+// Batch form: blockIdx.y selects the set's FQS array (stride nbuf) and its row
+// of partials; with the same gridDim.x every partial equals the single-set one.
+__global__ void k_batch_fit_reduce1(const double *__restrict__ fqs, long nbuf, double *__restrict__ psum,
+                                    unsigned long long *__restrict__ pcnt, unsigned long long *__restrict__ pnan) {
+    double s;
+    unsigned long long c, nn;
+    fit_block_partial(fqs + (size_t)blockIdx.y * (size_t)nbuf, nbuf, s, c, nn);
+    if (threadIdx.x == 0) {
+        const size_t o = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
+        psum[o] = s;
+        pcnt[o] = c;
+        pnan[o] = nn;
     }
 }
 
@@ -258,6 +281,51 @@ __global__ void k_fit_reduce2(const double *__restrict__ psum, const unsigned lo
     *out_sum = s;
     *out_cnt = c;
     *out_nan = nn;
+}
+
+__global__ void k_batch_fit_reduce2(const double *__restrict__ psum, const unsigned long long *__restrict__ pcnt,
+                                    const unsigned long long *__restrict__ pnan, int nb, int nsets,
+                                    double *__restrict__ out_sum, unsigned long long *__restrict__ out_cnt,
+                                    unsigned long long *__restrict__ out_nan) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nsets) return;
+    double s = 0.0;
+    unsigned long long c = 0, nn = 0;
+    for (int b = 0; b < nb; b++) {
+        s += psum[(size_t)k * nb + b];
+        c += pcnt[(size_t)k * nb + b];
+        nn += pnan[(size_t)k * nb + b];
+    }
+    out_sum[k] = s;
+    out_cnt[k] = c;
+    out_nan[k] = nn;
+}
+
+// Per-pixel FQSVERGL of every set of a batch against the shared fit data: the
+// masks and arithmetic of k_fit (doFitCalculation, KERNEL_PREWORK/POSTWORK
+// with dofit), with the pixel value read from the set's computed image, which
+// holds exactly the value k_fit computes for that pixel (the fit region is the
+// whole calculated image). blockIdx.y = set.
+__global__ void __launch_bounds__(256) k_batch_fqs(const cs::BatchSetDev *__restrict__ sets,
+                                                   const double *__restrict__ img, const double *__restrict__ data,
+                                                   double *__restrict__ fqs, long nfit, long nbuf) {
+    const cs::BatchSetDev &S = sets[blockIdx.y];
+    const cs_prepared &P = *S.prep;
+    double *f = fqs + (size_t)blockIdx.y * (size_t)nbuf;
+    const int xstride = P.xmax - P.xmin;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nfit; t += (long)gridDim.x * blockDim.x) {
+        int x = (int)(t % P.fit_width);
+        int y = (int)(t / P.fit_width);
+        if (!cs64::check_fit_ranges(P, data, f, x, y)) continue;
+        const long idx = (long)(x - P.xmin) + (long)xstride * (long)(y - P.ymin);
+        if (idx < 0 || idx >= nbuf) continue;
+        const double pixval = img[S.out_offset + idx];
+        if (pixval > 0 && data[idx] > 0) {
+            const double d = log(pixval) / log(10.) - log(data[idx]) / log(10.);
+            f[idx] = d * d;
+        } else
+            f[idx] = 0.0;
+    }
 }
 
 static int sm_count() {
@@ -409,6 +477,20 @@ int batch_blocks_per_sm_fp64(int key) {
     default: return 0;
     }
     return n;
+}
+
+
+// FQS arrays and chi^2 per set of a batch whose images are in d_img.
+int launch_batch_fit(const BatchSetDev *d_sets, int nsets, const double *d_img, const double *d_data, double *d_fqs,
+                     long nfit, long nbuf, const BatchFitReduce &R, cudaStream_t s) {
+    if (nsets <= 0) return CS_OK;
+    if (cudaMemsetAsync(d_fqs, 0, sizeof(double) * (size_t)nbuf * (size_t)nsets, s) != cudaSuccess) return CS_ERR_CUDA;
+    const int gx = grid_for(nfit, 256);
+    k_batch_fqs<<<dim3(gx, nsets), 256, 0, s>>>(d_sets, d_img, d_data, d_fqs, nfit, nbuf);
+    k_batch_fit_reduce1<<<dim3(R.nblocks, nsets), 256, 0, s>>>(d_fqs, nbuf, R.d_psum, R.d_pcnt, R.d_pnan);
+    k_batch_fit_reduce2<<<(nsets + 127) / 128, 128, 0, s>>>(R.d_psum, R.d_pcnt, R.d_pnan, R.nblocks, nsets, R.d_sum,
+                                                            R.d_cnt, R.d_nan);
+    return cudaGetLastError() == cudaSuccess ? CS_OK : CS_ERR_CUDA;
 }
 
 }  // namespace cs

@@ -35,21 +35,28 @@ using cs64::Ctx;
 // (1+x)^e for x >= 0 in FP32 via log1p (no rounding of 1+x)
 __device__ __forceinline__ float powp1f(float x, float e) { return exp2f(e * log1pf(x) * LOG2E_F); }
 
+// Relative error estimates of the form-factor parts: FP64 power series (a few
+// roundings; their own cancellation is that of the reference) and FP32
+// closed forms / quadratures (a few FP32 roundings).
+#define EPS_SERIES 1.0e-14
+#define EPS_PQ 3.0e-7
+#define EPS_PEAK 6.0e-7
+
 // decision guard: true when v is within `band` relative of threshold t
 __device__ __forceinline__ bool near(double v, double t, double band) { return fabs(v - t) <= band * fabs(t); }
 
-// Detector geometry. The sphere without lattice (a cheap pixel whose series
-// is well conditioned) takes it in FP64 without transcendentals:
-// cos(phi)sin(theta) = xdet/L, sin(phi)sin(theta) = ydet/L, cos(theta) = det/L,
-// L = |(xdet,ydet,det)|, which agrees with the reference's atan2/sin/cos form to
-// a few ulp. Every other key takes the drop-in's own convert_idx2q (same
-// rounding, this unit is compiled without contraction as the drop-in is): their
-// power series can cancel by up to 1e15, where a few-ulp change of q moves the
-// reference's own value by O(1), and the mixed path then reproduces the FP64
-// value exactly instead of a different rounding of it.
+// Detector geometry. In beam geometry it is taken in FP64 without
+// transcendentals: cos(phi)sin(theta) = xdet/L, sin(phi)sin(theta) = ydet/L,
+// cos(theta) = det/L, L = |(xdet,ydet,det)|, which agrees with the reference's
+// atan2/sin/cos form to a few ulp. The z-direction cylinder keys take the
+// drop-in's own convert_idx2q instead (same rounding: this unit is compiled
+// without contraction, as the drop-in is): their power series in (qx+qy)^2 can
+// cancel by up to 1e15, where a few-ulp change of q moves the reference's own
+// value by O(1), and the mixed path then reproduces the FP64 value exactly
+// instead of a different rounding of it.
 template <int KEY>
 __device__ __forceinline__ void q_of_pixel(const cs_prepared &P, int ihex, int i, double &qx, double &qy, double &qz) {
-    if (KEY != CS_KEY_SPHERE_NONE_ISO || P.use1d || !P.usebeamstop) {
+    if (KEY == CS_KEY_CYL_NONE_ZDIR || KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR || P.use1d || !P.usebeamstop) {
         cs64::convert_idx2q(P, ihex, i, qx, qy, qz);
         return;
     }
@@ -360,8 +367,20 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
             if (d < -dmax) break;
             const float4 v = __ldg(T.av + i);  // unit q_hkl (x,y,z) and g3/peaknorm1
             const float c = fmaf(fx, v.x, fmaf(fy, v.y, fz * v.z));
-            // myacos: the reference maps c < -1 to 0 and c > 1 to pi
-            const float yphi = (c < -1.0f) ? 0.0f : ((c > 1.0f) ? (float)M_PI : acosf(c));
+            // myacos: the reference maps c < -1 to 0 and c > 1 to pi. For q
+            // (anti)parallel to q_hkl the FP64 rounding of the reference's
+            // cosine decides between those and acos(c) ~ 0, a jump of the
+            // Gaussian; there the cosine is taken as the reference computes it.
+            float yphi;
+            if (fabsf(c) > 1.0f - 1e-5f) {
+                const int ii = __ldg(T.aidx + i);
+                const double cd = (qx * (double)P.latpar3[ii][2] + qy * (double)P.latpar3[ii][3] +
+                                   qz * (double)P.latpar3[ii][4]) /
+                                  (q * (double)P.latpar3[ii][5]);
+                yphi = (float)((cd < -1) ? 0.0 : ((cd > 1) ? M_PI : acos(cd)));
+            } else {
+                yphi = acosf(c);
+            }
             const float e = exp2f(fmaf(-k * d, d, -kphi * yphi * yphi));
             s.add(e * v.w * __ldg(T.amf + i));
         }
@@ -377,28 +396,36 @@ __device__ __forceinline__ double zr_asym(const cs_prepared &P) {
     return zr;
 }
 
-__device__ double sphere_pq_mixed(const cs_prepared &P, double q, bool &guard) {
+__device__ double sphere_pq_mixed(const cs_prepared &P, double q, bool &guard, double &err) {
     if (P.cs != 0) {
         guard = true;
         return 0.0;
     }
     const double thr = 0.4 * P.limq[4];
     if (near(q, thr, 1e-12)) guard = true;
-    if (q < thr) return cs64::series_q(P.carrp[3], q, 100);
+    if (q < thr) {
+        err = EPS_SERIES;
+        return cs64::series_q(P.carrp[3], q, 100);
+    }
     const double zr = zr_asym(P);
+    err = EPS_PQ;
     return sphere_pq_asym((float)(q * P.radius / (zr + 1)), (float)zr);
 }
 
-__device__ double sphere_fq_mixed(const cs_prepared &P, double q, bool &guard) {
+__device__ double sphere_fq_mixed(const cs_prepared &P, double q, bool &guard, double &err) {
     const double thr = 0.4 * P.limqf[4];
     if (near(q, thr, 1e-12)) guard = true;
-    if (q < thr) return cs64::series_q(P.carrf[3], q, 100);
+    if (q < thr) {
+        err = EPS_SERIES;
+        return cs64::series_q(P.carrf[3], q, 100);
+    }
     const double zr = (1 - cs64::sqr(P.sigma)) / cs64::sqr(P.sigma);
+    err = EPS_PQ;
     return sphere_fq_asym((float)(q * P.radius / (zr + 1)), (float)zr);
 }
 
 // formpq_partCylinder, ordis 0 and 6, cs 0 (mixed)
-__device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, bool &guard) {
+__device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, bool &guard, double &err) {
     const cs_prepared &P = *C.P;
     if (P.cs != 0) {
         guard = true;
@@ -407,6 +434,7 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
     const double zl = P.sigmal == 1.0 ? CS_EPS9 : (1 - cs64::sqr(P.sigmal)) / cs64::sqr(P.sigmal);
     const double zr = P.sigma == 1.0 ? CS_EPS9 : (1 - cs64::sqr(P.sigma)) / cs64::sqr(P.sigma);
     double pql = 0, pqr = 0;
+    double el = EPS_SERIES, er = EPS_SERIES;
     if (P.ordis == 6) {
         const double thr = 0.6 * P.limq[1];
         if (near(q, thr, 1e-12)) guard = true;
@@ -415,6 +443,7 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
         } else {
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
             pql = cyl_len_factor((float)arglq, (float)zl);
+            el = EPS_PQ;
         }
     } else if (P.ordis == 0) {
         const double thr = 0.4 * P.limq[1];
@@ -441,6 +470,7 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             A.p23 = (float)P.romb_p[5];
             A.i1 = P.orcase;
             pql = qromb_delta_f(C, A, guard) / P.norm;
+            el = EPS_PQ;
         }
     } else {
         guard = true;
@@ -453,15 +483,19 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
         if (near(q, thr, 1e-12)) guard = true;
         if (q < thr)
             pqr = cs64::series_q(P.carrp[3], q, 120);
-        else
+        else {
             pqr = cyl_pqr_asym((float)(q * P.radius / (zr + 1)), (float)zr);
+            er = EPS_PQ;
+        }
     }
+    err = el + er;
     return pql * pqr;
 }
 
 
 // formfq_partCylinder, ordis 0 and 6, cs 0 (mixed)
-__device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qys, double q, bool &guard) {
+__device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qys, double q, bool &guard,
+                             double &err) {
     const cs_prepared &P = *C.P;
     if (P.cs != 0) {
         guard = true;
@@ -470,6 +504,7 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
     const double zl = (1 - cs64::sqr(P.sigmal)) / cs64::sqr(P.sigmal);
     const double zr = (1 - cs64::sqr(P.sigma)) / cs64::sqr(P.sigma);
     double pql = 0, pqr = 0;
+    double el = EPS_SERIES, er = EPS_SERIES;
     if (P.ordis == 6) {
         const double thr = 0.6 * P.limqf[1];
         if (near(limql, thr, 1e-12)) guard = true;
@@ -478,6 +513,7 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
         } else {
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
             pql = cyl_len_factor((float)arglq, (float)zl);
+            el = EPS_PQ;
         }
     } else if (P.ordis == 0) {
         const double thr = 0.2 * P.limqf[1];
@@ -504,6 +540,7 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             A.p23 = (float)P.romb_p[5];
             A.i1 = P.orcase;
             pql = qromb_delta_f(C, A, guard) / P.norm;
+            el = EPS_PQ;
         }
     } else {
         guard = true;
@@ -523,7 +560,9 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
         const float pqr2 = (float)P.gamma_ratio[1] * rsqrtf(a2 * a2 * a) * (sinf(s2) + cosf(s2)) / powp1f(a2, (z - 1.5f) / 2.0f);
         const float pqr3 = (2.0f / sqrtf((float)M_PI)) * (pqr1 + (9.0f / 16.0f) * pqr2);
         pqr = (double)pqr3 * (double)pqr3;
+        er = EPS_PQ;
     }
+    err = el + er;
     return pql * pqr;
 }
 
@@ -531,16 +570,15 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
 //   I = base + I0 (szq pq + iso szqiso pqi) + tail,
 //   szq = 1 + (fq/pq)(2 pi I_aniso/V - 1) e^(-dw q^2),
 //   szqiso = 1 + (8 pi^3 I_iso/(4 pi V) - 1) e^(-ucb q^2),
-// in FP64 from FP32-accurate inputs (asymptotes: relative error ~EPS_PQ,
-// peak sums: ~EPS_PEAK, a few FP32 roundings each). Where the terms cancel
+// in FP64 from inputs with the relative error estimates errp/errf/errpi
+// (EPS_SERIES or EPS_PQ per part) and EPS_PEAK (peak sums). Where the terms cancel
 // (szq -> 0 between peaks, I0 szq pq against base) the input errors are
 // amplified; a first-order estimate of the result's error is propagated
 // alongside, and a pixel whose estimate exceeds 5e-6 of |I| (half the 1e-5 bar)
 // is recomputed in FP64.
-#define EPS_PQ 3.0e-7
-#define EPS_PEAK 6.0e-7
-__device__ __forceinline__ double lattice_combine(const cs_prepared &P, double q, double pq, double fq, double pqi,
-                                                  double radint, double intens, double tailv, bool &guard) {
+__device__ __forceinline__ double lattice_combine(const cs_prepared &P, double q, double pq, double errp, double fq,
+                                                  double errf, double pqi, double errpi, double radint, double intens,
+                                                  double tailv, bool &guard) {
     const double v = P.latpar[1] * P.latpar[2];
     const double r2 = 8 * M_PI * M_PI * M_PI * radint / (4 * M_PI * v);
     const double e2 = exp(-P.ucb * q * q);
@@ -552,9 +590,9 @@ __device__ __forceinline__ double lattice_combine(const cs_prepared &P, double q
     const double szq = 1 + t;
     const double res = P.base + P.izero * (szq * pq + P.iso * szqiso * pqi) + tailv;
     // first-order error bound
-    const double dt = fabs(t) * (2 * EPS_PQ) + fabs(ratio * e1 * r1) * EPS_PEAK;
-    const double d1 = fabs(pq) * dt + fabs(szq * pq) * EPS_PQ;
-    const double d2 = fabs(P.iso) * (fabs(pqi) * fabs(r2 * e2) * EPS_PEAK + fabs(szqiso * pqi) * EPS_PQ);
+    const double dt = fabs(t) * (errf + errp) + fabs(ratio * e1 * r1) * EPS_PEAK;
+    const double d1 = fabs(pq) * dt + fabs(szq * pq) * errp;
+    const double d2 = fabs(P.iso) * (fabs(pqi) * fabs(r2 * e2) * EPS_PEAK + fabs(szqiso * pqi) * errpi);
     const double bound = fabs(P.izero) * (d1 + d2);
     if (!(bound <= 5e-6 * fabs(res))) guard = true;
     return res;
@@ -565,32 +603,33 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
     const cs_prepared &P = *C.P;
     const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
     const double tailv = P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+    double ep = 0, ef = 0;  // relative error estimates of pq and fq
     if (KEY == CS_KEY_SPHERE_NONE_ISO) {
-        const double pq = sphere_pq_mixed(P, q, guard);
+        const double pq = sphere_pq_mixed(P, q, guard, ep);
         return P.base + P.izero * (pq + P.iso * pq) + tailv;
     }
     if (KEY == CS_KEY_SPHERE_GAUSS_FCC_GAUSS) {
-        const double pq = sphere_pq_mixed(P, q, guard);
-        const double fq = sphere_fq_mixed(P, q, guard);
+        const double pq = sphere_pq_mixed(P, q, guard, ep);
+        const double fq = sphere_fq_mixed(P, q, guard, ef);
         double radint, intens;
         peak_sums_f(P, T, qx, qy, qz, q, radint, intens, guard);
-        return lattice_combine(P, q, pq, fq, pq, radint, intens, tailv, guard);
+        return lattice_combine(P, q, pq, ep, fq, ef, pq, ep, radint, intens, tailv, guard);
     }
     if (KEY == CS_KEY_CYL_NONE_GAUSS) {
         double pq;
         if (P.orcase == CS_ORC_GENERAL)
-            pq = cyl_pq_mixed(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q, guard);
+            pq = cyl_pq_mixed(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q, guard, ep);
         else
-            pq = cyl_pq_mixed(C, qx, qy, q, guard);
+            pq = cyl_pq_mixed(C, qx, qy, q, guard, ep);
         return P.base + P.izero * (pq + P.iso) + tailv;
     }
     if (KEY == CS_KEY_CYL_NONE_ZDIR) {
         double pq;
         switch (P.orcase) {
-        case CS_ORC_GENERAL: pq = cyl_pq_mixed(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard); break;
-        case CS_ORC_XAXIS: pq = cyl_pq_mixed(C, qx, 0, q, guard); break;
-        case CS_ORC_YAXIS: pq = cyl_pq_mixed(C, 0, qy, q, guard); break;
-        default: pq = cyl_pq_mixed(C, qx, qy, q, guard); break;
+        case CS_ORC_GENERAL: pq = cyl_pq_mixed(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard, ep); break;
+        case CS_ORC_XAXIS: pq = cyl_pq_mixed(C, qx, 0, q, guard, ep); break;
+        case CS_ORC_YAXIS: pq = cyl_pq_mixed(C, 0, qy, q, guard, ep); break;
+        default: pq = cyl_pq_mixed(C, qx, qy, q, guard, ep); break;
         }
         return P.base + P.izero * (pq + P.iso) + tailv;
     }
@@ -598,27 +637,27 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
         double pq = 0, fq = 0;
         switch (P.orcase) {
         case CS_ORC_GENERAL:
-            pq = cyl_pq_mixed(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard);
+            pq = cyl_pq_mixed(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard, ep);
             fq = cyl_fq_mixed(C, sqrt(P.cosphi * qx * qx + P.sinphi * qy * qy + CS_EPS9), qx * P.cosphi * P.sintheta,
-                              qy * P.sinphi * P.sintheta, q, guard);
+                              qy * P.sinphi * P.sintheta, q, guard, ef);
             break;
         case CS_ORC_XAXIS:
-            pq = cyl_pq_mixed(C, qx, 0, q, guard);
-            fq = cyl_fq_mixed(C, fabs(qx), qx, 0, q, guard);
+            pq = cyl_pq_mixed(C, qx, 0, q, guard, ep);
+            fq = cyl_fq_mixed(C, fabs(qx), qx, 0, q, guard, ef);
             break;
         case CS_ORC_YAXIS:
-            pq = cyl_pq_mixed(C, 0, qy, q, guard);
-            fq = cyl_fq_mixed(C, fabs(qy), 0, qy, q, guard);
+            pq = cyl_pq_mixed(C, 0, qy, q, guard, ep);
+            fq = cyl_fq_mixed(C, fabs(qy), 0, qy, q, guard, ef);
             break;
         default:
-            pq = cyl_pq_mixed(C, qx, qy, q, guard);
-            fq = cyl_fq_mixed(C, q, qx, qy, q, guard);
+            pq = cyl_pq_mixed(C, qx, qy, q, guard, ep);
+            fq = cyl_fq_mixed(C, q, qx, qy, q, guard, ef);
             break;
         }
         double radint, intens;
         peak_sums_f(P, T, qx, qy, qz, q, radint, intens, guard);
         // the reference's BCT function multiplies szqiso by 1 instead of pq
-        return lattice_combine(P, q, pq, fq, 1.0, radint, intens, tailv, guard);
+        return lattice_combine(P, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, tailv, guard);
     }
     guard = true;
     return 0.0;
@@ -687,7 +726,7 @@ namespace cs {
 
 // Compact, sorted reflection tables from the prepared block (see PeakTab).
 void build_peak_tables(const cs_prepared &P, HostPeaks &H) {
-    H.aq.clear(); H.amf.clear(); H.av.clear(); H.iq.clear(); H.imf.clear();
+    H.aq.clear(); H.amf.clear(); H.av.clear(); H.iq.clear(); H.imf.clear(); H.aidx.clear();
     struct A { float q; float4 v; float mf; int idx; };
     std::vector<A> an;
     for (int ii = 1; ii <= P.peakmax2 && ii < CS_LATPARLEN; ii++) {
@@ -708,6 +747,7 @@ void build_peak_tables(const cs_prepared &P, HostPeaks &H) {
         H.aq.push_back(a.q);
         H.av.push_back(a.v);
         H.amf.push_back(a.mf);
+        H.aidx.push_back(a.idx);
     }
     struct I { float q; float mf; };
     std::vector<I> is;

@@ -18,6 +18,7 @@ struct PeakTab {
     const float *aq = nullptr;   // q_hkl
     const float4 *av = nullptr;  // unit q_hkl vector (x, y, z), g3/peaknorm1
     const float *amf = nullptr;  // multiplicity * structure factor
+    const int *aidx = nullptr;   // row of the reflection in latpar2/latpar3
     int n_iso = 0;
     const float *iq = nullptr;
     const float *imf = nullptr;
@@ -38,6 +39,7 @@ struct MixedScratch {
 struct HostPeaks {
     std::vector<float> aq, amf, iq, imf;
     std::vector<float4> av;
+    std::vector<int> aidx;
 };
 void build_peak_tables(const cs_prepared &P, HostPeaks &H);
 

@@ -227,6 +227,69 @@ int cs_batch_graph_nodes(cs_batch *b, size_t *n);
 int cs_batch_redo_pixels(cs_batch *b, void *stream, long *n, long *capacity);
 int cs_batch_set_redo_capacity(cs_batch *b, long entries_per_group);
 double cs_batch_timer_ms(cs_batch *b); /* host preparation time of the last cs_batch_prepare */
+/* Batch fit: doFitCalculation (Source/sc_calc_generic_cpu.cpp:1334-1443) for
+   every set of a batch against one target, e.g. the vertices of a simplex.
+   cs_batch_set_fit stores the target (width x height doubles, the image's
+   size) and the masks of doFitCalculation/setNoFitRect (bstop, border, nofit
+   = 4 rectangles x {x0,y0,x1,y1}, -1 = unused, NULL = none); batches prepared
+   afterwards skip checkAllParameters as doFitCalculation does.
+   cs_batch_fit_chi2 computes every set's image (persistent schedule), the
+   per-pixel FQSVERGL and its sum, count of non-zero and count of NaN terms
+   per set (chi2/cnt/nancnt arrays of nsets entries, chi2 = 1e20 on failure).
+   One evaluation is captured as a CUDA graph and replayed while the batch
+   keeps its layout (same set count, image sizes and dispatch keys), so a fit
+   iteration costs the host preparation plus one graph launch. Needs all four
+   quadrants calculated (RadioButtonQ4) and fit data of the image's size. */
+int cs_batch_set_fit(cs_batch *b, int width, int height, const double *data, int bstop, int border,
+                     const int *nofit);
+int cs_batch_fit_chi2(cs_batch *b, int mode, double *chi2, long *cnt, long *nancnt);
+
+/* 2D simplex fit: SasCalc_SimplexFit2D::doSimplexFit2D
+   (Source/sc_simplexfit2d.cpp:250-611) over the parameters listed in
+   `params` (reference keys as for cs_set_param; `used` = fitted, else held at
+   fitstart), starting from `base`, judged by the chi^2 of doFitCalculation
+   against `data` (width x height doubles) with the masks bstoppix, borderpix
+   and nofit (4 rectangles x {x0,y0,x1,y1}, -1 unused, NULL none). stp, maxit,
+   ftol: the reference's step factor, iteration limit and relative tolerance.
+   The reference's trajectory is reproduced, including its initialisation of
+   the first parameter of every initial vertex to 0 + step and its centroid
+   factor over all listed parameters. Results: fitres of every parameter (the
+   best vertex), and the report. schedule CS_FIT_SEQUENTIAL evaluates one
+   vertex at a time through the drop-in fit call; CS_FIT_BATCHED evaluates the
+   independent vertices and, per iteration, the reference's next candidate
+   vertices speculatively as one batch (same decisions and result, fewer
+   host round trips, more images). mode CS_MODE_MIXED judges vertices by the
+   mixed-precision images. */
+#define CS_FIT_SEQUENTIAL 0
+#define CS_FIT_BATCHED 1
+typedef struct cs_fit_param {
+    char key[48];     /* reference parameter key, e.g. "EditRadius" */
+    double min, max;  /* limits; min 0 and max 360 (an angle) are not checked */
+    double fitstart;  /* start value */
+    double fitres;    /* result (out) */
+    int used;         /* 1 = fitted, 0 = held fixed */
+    int fitvalid;     /* 1 after a fit (out) */
+} cs_fit_param;
+typedef struct cs_fit_report {
+    int repetitions; /* simplex iterations run */
+    int aborted;     /* 1 when the reference's NaN / zero abort ended the fit */
+    long images;     /* fit evaluations calculated on the GPU */
+    double chi2;     /* chi^2 of the best vertex */
+    double ms;       /* wall time of the fit (higResTimerElapsed) */
+    char info[256];  /* message on error */
+} cs_fit_report;
+int cs_simplex_fit(const cs_params *base, const double *data, int width, int height, const int *nofit,
+                   cs_fit_param *params, int nparams, double stp, int maxit, double ftol, int borderpix, int bstoppix,
+                   int mode, int schedule, cs_fit_report *report);
+/* The same simplex over a caller's objective instead of the image chi^2
+   (no GPU involved): fn receives npoints parameter vectors of nparams values
+   each (the table order of the simplex: fitted keys sorted, then fixed keys
+   sorted) and writes one value per point; points outside the limits get 1e20
+   without a call. CS_FIT_SEQUENTIAL passes one point per call. */
+typedef void (*cs_objective_fn)(const double *points, int npoints, int nparams, double *values, void *ctx);
+int cs_simplex_minimize(cs_objective_fn fn, void *ctx, cs_fit_param *params, int nparams, double stp, int maxit,
+                        double ftol, int schedule, cs_fit_report *report);
+
 /* Host-buffer forms: run the prepared batch (persistent schedule, a redo
    overflow handled internally) and copy all images into out; cs_calc_batch
    prepares first. */
