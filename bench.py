@@ -46,6 +46,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--sweep-sets", type=int, default=4096, help="parameter sets of the batched sweep (0 = skip)")
     ap.add_argument("--sweep-steps", type=int, default=2)
+    ap.add_argument("--surrogate", default="", help="surrogate-seeded fits of this family ('2', '2x'); off by default")
+    ap.add_argument("--surrogate-train", type=int, default=20000)
+    ap.add_argument("--surrogate-epochs", type=int, default=30)
+    ap.add_argument("--surrogate-targets", type=int, default=8)
     return ap.parse_args()
 
 
@@ -259,6 +263,22 @@ def sweep(cs, torch, C, nsets, ops, peaks, steps):
     return row, redo
 
 
+def surrogate_fits(args):
+    """Config 5: the surrogate trained on simulator patterns, then plain fits
+    (FP64, one vertex at a time, random start) against surrogate-seeded fits
+    (batched, mixed precision) run until they reach the plain fit's chi^2."""
+    from crystalscatter_gb300 import surrogate as S
+    fam = S.Family(args.surrogate)
+    t0 = time.perf_counter()
+    U, Y = S.training_set(fam, args.surrogate_train, seed=11)
+    t_data = time.perf_counter() - t0
+    sur = S.Surrogate(fam, seed=11)
+    info = sur.train(U, Y, epochs=args.surrogate_epochs)
+    res = S.compare_fits(fam, sur, n_targets=args.surrogate_targets, seed=101)
+    res.update({"train_patterns": args.surrogate_train, "pattern_seconds": t_data, "training": info})
+    return res
+
+
 def native(args):
     import numpy as np
     import torch
@@ -365,6 +385,8 @@ def native(args):
         result["configs"] = rows
         if args.sweep_sets > 0:
             result["sweep"], _ = sweep(cs, torch, C, args.sweep_sets, ops, peaks, max(1, args.sweep_steps))
+    if args.surrogate and rank == 0:
+        result["surrogate"] = surrogate_fits(args)
     if rank == 0:
         result["cpu_baseline"] = cpu_baseline(params, args.cpu_seconds)
         print(json.dumps(result))

@@ -165,10 +165,28 @@ def _sig(lib):
     lib.cs_batch_fit_chi2.argtypes = [B, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     lib.cs_simplex_fit.argtypes = [P(CsParams), ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                    P(CsFitParam), ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double,
-                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, P(CsFitReport)]
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                   P(CsFitReport)]
     lib.cs_launch_prepared_mixed_noalloc.argtypes = [H, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    M = ctypes.c_void_p
+    lib.cs_mlp_create.restype = M
+    lib.cs_mlp_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong]
+    lib.cs_mlp_destroy.argtypes = [M]
+    lib.cs_mlp_last_error.restype = ctypes.c_char_p
+    lib.cs_mlp_last_error.argtypes = [M]
+    lib.cs_mlp_forward.argtypes = [M, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.cs_mlp_gradients.argtypes = [M, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, P(ctypes.c_float),
+                                     ctypes.c_void_p]
+    lib.cs_mlp_train_step.argtypes = [M, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
+                                      P(ctypes.c_float), ctypes.c_void_p]
+    lib.cs_mlp_layer_dims.argtypes = [M, ctypes.c_int, P(ctypes.c_int), P(ctypes.c_int)]
+    lib.cs_mlp_get_layer.argtypes = [M, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p]
+    lib.cs_mlp_set_layer.argtypes = [M, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.cs_upsample_bilinear.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_void_p]
     lib.cs_simplex_minimize.argtypes = [_OBJECTIVE, ctypes.c_void_p, P(CsFitParam), ctypes.c_int, ctypes.c_double,
-                                        ctypes.c_int, ctypes.c_double, ctypes.c_int, P(CsFitReport)]
+                                        ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, P(CsFitReport)]
     lib.cs_calc_batch.argtypes = [B, P(CsParams), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                   ctypes.c_void_p, ctypes.c_size_t]
     return lib
@@ -526,7 +544,7 @@ def _report(rep):
             "ms": rep.ms}
 
 
-def simplex_minimize(fn, fit_params, stp=0.1, maxit=100, ftol=1e-4, schedule=CS_FIT_SEQUENTIAL):
+def simplex_minimize(fn, fit_params, stp=0.1, maxit=100, ftol=1e-4, schedule=CS_FIT_SEQUENTIAL, chi2_stop=0.0):
     """The library's simplex (cs_simplex_minimize) over a Python objective:
     fn(points) with points an (n, nparams) array in the simplex's table order
     (fitted keys sorted, then fixed keys sorted) returns n values."""
@@ -542,14 +560,14 @@ def simplex_minimize(fn, fit_params, stp=0.1, maxit=100, ftol=1e-4, schedule=CS_
     arr = _fit_table(fit_params)
     rep = CsFitReport()
     rc = lib.cs_simplex_minimize(cfn, None, arr, len(fit_params), float(stp), int(maxit), float(ftol), int(schedule),
-                                 ctypes.byref(rep))
+                                 float(chi2_stop), ctypes.byref(rep))
     if rc != CS_OK:
         raise CrystalScatterError(rc, rep.info.decode() or "simplex failed")
     return {arr[i].key.decode(): arr[i].fitres for i in range(len(fit_params))}, _report(rep)
 
 
 def simplex_fit(base, data, fit_params, stp=0.1, maxit=100, ftol=1e-4, border=0, bstop=0, nofit=None,
-                mode=CS_MODE_FP64, schedule=CS_FIT_SEQUENTIAL):
+                mode=CS_MODE_FP64, schedule=CS_FIT_SEQUENTIAL, chi2_stop=0.0):
     """SasCalc_SimplexFit2D::doSimplexFit2D on the GPU (cs_simplex_fit).
 
     base: reference-key dict or CsParams; data: 2D target of the image's size;
@@ -566,8 +584,83 @@ def simplex_fit(base, data, fit_params, stp=0.1, maxit=100, ftol=1e-4, border=0,
     rep = CsFitReport()
     rc = lib.cs_simplex_fit(ctypes.byref(p), a.ctypes.data, int(w), int(h), nf.ctypes.data, arr, len(fit_params),
                             float(stp), int(maxit), float(ftol), int(border), int(bstop), int(mode), int(schedule),
-                            ctypes.byref(rep))
+                            float(chi2_stop), ctypes.byref(rep))
     if rc != CS_OK:
         raise CrystalScatterError(rc, rep.info.decode() or "simplex fit failed")
     res = {arr[i].key.decode(): arr[i].fitres for i in range(len(fit_params))}
     return res, _report(rep)
+
+
+class SurrogateMLP:
+    """The surrogate network of the library (cs_mlp_*): n_in -> hidden x3 ->
+    n_out with GELU, BF16 tensor-core GEMMs with FP32 accumulation, Adam on
+    the device. Inputs and outputs are CUDA float32 tensors (torch is used for
+    device memory only)."""
+
+    def __init__(self, n_in, hidden=512, n_out=4096, seed=0):
+        self._lib = load_library()
+        self._m = self._lib.cs_mlp_create(int(n_in), int(hidden), int(n_out), int(seed))
+        if not self._m:
+            raise CrystalScatterError(CS_ERR_CUDA, "cs_mlp_create failed (no GPU or unsupported sizes)")
+        self.n_in, self.hidden, self.n_out = n_in, hidden, n_out
+
+    def __del__(self):
+        self.cleanup()
+
+    def cleanup(self):
+        if getattr(self, "_m", None):
+            self._lib.cs_mlp_destroy(self._m)
+            self._m = None
+
+    def _check(self, rc):
+        if rc != CS_OK:
+            raise CrystalScatterError(rc, self._lib.cs_mlp_last_error(self._m).decode())
+
+    def forward(self, x, stream=0):
+        import torch
+        x = x.contiguous().float()
+        y = torch.empty((x.shape[0], self.n_out), dtype=torch.float32, device=x.device)
+        self._check(self._lib.cs_mlp_forward(self._m, x.data_ptr(), x.shape[0], y.data_ptr(), ctypes.c_void_p(stream)))
+        return y
+
+    def gradients(self, x, t, stream=0):
+        loss = ctypes.c_float()
+        x = x.contiguous().float()
+        t = t.contiguous().float()
+        self._check(self._lib.cs_mlp_gradients(self._m, x.data_ptr(), t.data_ptr(), x.shape[0], ctypes.byref(loss),
+                                               ctypes.c_void_p(stream)))
+        return loss.value
+
+    def train_step(self, x, t, lr, stream=0, want_loss=True):
+        loss = ctypes.c_float()
+        self._check(self._lib.cs_mlp_train_step(self._m, x.data_ptr(), t.data_ptr(), x.shape[0], float(lr),
+                                                ctypes.byref(loss) if want_loss else None, ctypes.c_void_p(stream)))
+        return loss.value if want_loss else None
+
+    def layer(self, l):
+        r, c = ctypes.c_int(), ctypes.c_int()
+        self._lib.cs_mlp_layer_dims(self._m, l, ctypes.byref(r), ctypes.byref(c))
+        w = np.empty((r.value, c.value), np.float32)
+        b = np.empty(r.value, np.float32)
+        gw = np.empty_like(w)
+        gb = np.empty_like(b)
+        self._check(self._lib.cs_mlp_get_layer(self._m, l, w.ctypes.data, b.ctypes.data, gw.ctypes.data,
+                                               gb.ctypes.data))
+        return {"w": w, "b": b, "gw": gw, "gb": gb}
+
+    def set_layer(self, l, w, b):
+        w = np.ascontiguousarray(w, np.float32)
+        b = np.ascontiguousarray(b, np.float32)
+        self._check(self._lib.cs_mlp_set_layer(self._m, l, w.ctypes.data, b.ctypes.data))
+
+
+def upsample_bilinear(x, factor, stream=0):
+    """(n, s, s) CUDA float32 -> (n, s*factor, s*factor), cs_upsample_bilinear"""
+    import torch
+    x = x.contiguous().float()
+    n, s = x.shape[0], x.shape[1]
+    out = torch.empty((n, s * factor, s * factor), dtype=torch.float32, device=x.device)
+    rc = load_library().cs_upsample_bilinear(x.data_ptr(), n, s, int(factor), out.data_ptr(), ctypes.c_void_p(stream))
+    if rc != CS_OK:
+        raise CrystalScatterError(rc, "upsample failed")
+    return out

@@ -18,12 +18,12 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libcrystalscatter.so")
 
 HOST_SOURCES = ["cs_prep.cpp", "cs_params.cpp", "cs_capi.cpp", "cs_batch.cpp", "cs_simplex.cpp"]
-CUDA_SOURCES = ["cs_kernels.cu", "cs_mixed.cu", "cs_noalloc.cu"]
+CUDA_SOURCES = ["cs_kernels.cu", "cs_mixed.cu", "cs_noalloc.cu", "cs_mlp.cu"]
 # No automatic multiply-add contraction in either unit: the FP64 drop-in keeps
 # the reference's separate multiply and add roundings, and the mixed kernels
 # share its FP64 functions (pixel geometry, power series, math library calls),
 # which must round identically there; FP32 code asks for fmaf where it wants one
-FMAD = {"cs_kernels.cu": "false", "cs_mixed.cu": "false", "cs_noalloc.cu": "false"}
+FMAD = {"cs_kernels.cu": "false", "cs_mixed.cu": "false", "cs_noalloc.cu": "false", "cs_mlp.cu": "true"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

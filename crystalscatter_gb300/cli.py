@@ -2,6 +2,7 @@
 
     python -m crystalscatter_gb300.cli --workload cyl_gauss_x --grid 64 --repeat 3
     python -m crystalscatter_gb300.cli --mcpval "cbparticle=sphere;radius=10;gridpoints=128" --out img.dat
+    python -m crystalscatter_gb300.cli --sweep 16 --mode mixed --repeat 2
 
 The parameter set is a named workload (crystalscatter_gb300.configs), optionally
 rescaled to another grid with the same q-range, then modified by a console
@@ -17,7 +18,7 @@ import time
 
 import numpy as np
 
-from . import CS_MODE_FP64, CS_MODE_MIXED, SasCalc_GENERIC_calculation
+from . import CS_MODE_FP64, CS_MODE_MIXED, SasCalc_GENERIC_calculation, SasCalcBatch
 from . import configs as C
 
 
@@ -37,7 +38,11 @@ def main(argv=None):
     ap.add_argument("--repeat", type=int, default=1)
     ap.add_argument("--ign-cbs", action="store_true")
     ap.add_argument("--out", default="")
+    ap.add_argument("--sweep", type=int, default=0,
+                    help="instead of one image: the first N parameter sets of the cylinder/BCT sweep as one batch")
     a = ap.parse_args(argv)
+    if a.sweep:
+        return sweep(a)
     params = C.bct_set(0) if a.workload == "bct0" else C.WORKLOADS[a.workload]
     if a.grid:
         params = C.scaled(params, a.grid)
@@ -63,6 +68,28 @@ def main(argv=None):
                       "nonfinite": int((~fin).sum()), "seconds": times,
                       "prep_ms": calc.higResTimerElapsedPrep, "calc_ms": calc.higResTimerElapsedCalc}))
     calc.cleanup()
+    return 0
+
+
+def sweep(a):
+    """the first a.sweep sets of the cylinder/BCT sweep in one batch
+    (persistent launch per dispatch key), a.repeat times"""
+    mode = CS_MODE_MIXED if a.mode == "mixed" else CS_MODE_FP64
+    b = SasCalcBatch()
+    t0 = time.perf_counter()
+    b.prepare(C.bct_sweep(a.sweep), bIgnoreCbs=True)
+    t_prep = time.perf_counter() - t0
+    times = []
+    for _ in range(max(1, a.repeat)):
+        t0 = time.perf_counter()
+        flat = b.run_host(mode)
+        times.append(time.perf_counter() - t0)
+    total, pixels, groups = b.info()
+    redo = b.redo_pixels()[0] if mode == CS_MODE_MIXED else 0
+    nonfinite = sum(int((~np.isfinite(img)).sum()) for img in b.split(flat))
+    print(json.dumps({"sweep_sets": a.sweep, "pixels": pixels, "key_groups": groups, "mode": a.mode,
+                      "prep_seconds": t_prep, "seconds": times, "redo_pixels": redo, "nonfinite": nonfinite}))
+    b.cleanup()
     return 0
 
 

@@ -75,6 +75,23 @@ __device__ __forceinline__ void convert_idx2q(const cs_prepared &P, int ihex, in
 // written with __dmul_rn/__dadd_rn, which are never fused into a
 // multiply-add, so they round as the reference's separate operations in every
 // translation unit, also in those compiled with contraction.
+// The reference's stop test fabs((s - old) / s) < 0.0001, decided without the
+// FP64 division wherever rounding cannot matter: with A = fl(0.0001 |s|), an
+// increment below A (1 - 2^-50) has an exact quotient below 0.0001 (1 - 2^-52),
+// whose rounding stays below 0.0001; one above A (1 + 2^-50) stays above. Only
+// inside that band, and for |s| outside [1e-290, 1e290] (zero, NaN, inf,
+// products that could be subnormal), is the quotient computed as the
+// reference computes it. The decision is the
+// reference's in every case.
+__device__ __forceinline__ bool series_converged(double s, double old) {
+    if (!(fabs(s) > 1e-290 && fabs(s) < 1e290)) return fabs((s - old) / s) < 0.0001;  // (no subnormal products)
+    const double d = fabs(__dadd_rn(s, -old));
+    const double a = __dmul_rn(0.0001, fabs(s));
+    if (d < __dmul_rn(a, 1.0 - 0x1p-50)) return true;
+    if (d > __dmul_rn(a, 1.0 + 0x1p-50)) return false;
+    return fabs((s - old) / s) < 0.0001;
+}
+
 __device__ __forceinline__ double series_q(const double *__restrict__ c, double q, int nmax) {
     double pqsum = 1.0;
     double oldpqsum = 0.0;
@@ -82,8 +99,7 @@ __device__ __forceinline__ double series_q(const double *__restrict__ c, double 
     for (int nser = 1; nser <= nmax; nser++) {
         qq = __dmul_rn(__dmul_rn(qq, q), q);
         pqsum = __dadd_rn(pqsum, __dmul_rn(c[nser], qq));
-        double delser = fabs((pqsum - oldpqsum) / pqsum);
-        if (delser < 0.0001) break;
+        if (series_converged(pqsum, oldpqsum)) break;
         oldpqsum = pqsum;
     }
     return pqsum;
@@ -100,8 +116,7 @@ __device__ __forceinline__ double series_zdir(const double *__restrict__ c, doub
     for (int nser = 1; nser <= 120; nser++) {
         qqnn = __dmul_rn(__dmul_rn(qqnn, s), s);
         pql = __dadd_rn(pql, __dmul_rn(c[nser], qqnn));
-        const double delser = fabs((pql - oldpqsum) / pql);
-        if (delser < 0.0001) break;
+        if (series_converged(pql, oldpqsum)) break;
         oldpqsum = pql;
     }
     return pql;
@@ -431,11 +446,17 @@ __device__ inline double cyl_double_series(const cs_prepared &P, double qxs, dou
                 binsum = __dadd_rn(binsum, __dmul_rn(__dmul_rn(P.carr11pm[mser][nser - mser], qxn[mser]), qyn[nser - mser]));
         }
         pql = __dadd_rn(pql, __dmul_rn(carr1[nser], binsum));
-        double delser = fabs((pql - oldpqsum) / pql);
-        if (delser < 0.0001) break;
+        if (series_converged(pql, oldpqsum)) break;
         oldpqsum = pql;
     }
     return pql;
+}
+
+// Length factor of the z-direction cylinder in the reference's closed form
+// (formpq/formfq_partCylinder ordis 6, Source/sc_lib_formpq_partCylinder.h:115-119).
+__device__ __forceinline__ double len_factor_ref(double arglq, double zl) {
+    return (1 / (2.0 * zl * (zl - 1))) * (1 / (arglq * arglq)) *
+           (1 - cos((zl - 1) * atan(2.0 * arglq)) / pow(1.0 + 4 * arglq * arglq, (zl - 1) / 2.0));
 }
 
 __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, double q) {
@@ -451,8 +472,7 @@ __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, d
                 pql = series_zdir(P.carrp[0], qxs, qys);
             } else {
                 const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-                pql = (1 / (2.0 * zl * (zl - 1))) * (1 / (arglq * arglq)) *
-                      (1 - cos((zl - 1) * atan(2.0 * arglq)) / pow(1.0 + 4 * arglq * arglq, (zl - 1) / 2.0));
+                pql = len_factor_ref(arglq, zl);
             }
         }
     }
@@ -508,8 +528,7 @@ __device__ inline double formfq_cylinder(const Ctx &C, double limql, double qxs,
                 pql = series_zdir(P.carrf[0], qxs, qys);
             } else {
                 const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-                pql = (1 / (2.0 * zl * (zl - 1))) * (1 / (arglq * arglq)) *
-                      (1 - cos((zl - 1) * atan(2.0 * arglq)) / pow(1.0 + 4 * arglq * arglq, (zl - 1) / 2.0));
+                pql = len_factor_ref(arglq, zl);
             }
         }
     }

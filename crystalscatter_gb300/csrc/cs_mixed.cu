@@ -40,7 +40,7 @@ __device__ __forceinline__ float powp1f(float x, float e) { return exp2f(e * log
 // closed forms / quadratures (a few FP32 roundings).
 #define EPS_SERIES 1.0e-14
 #define EPS_PQ 3.0e-7
-#define EPS_PEAK 6.0e-7
+#define EPS_PEAK 1.0e-7  // peak sums beyond their own estimate (Kahan, table rounding)
 
 // decision guard: true when v is within `band` relative of threshold t
 __device__ __forceinline__ bool near(double v, double t, double band) { return fabs(v - t) <= band * fabs(t); }
@@ -74,39 +74,83 @@ __device__ __forceinline__ void q_of_pixel(const cs_prepared &P, int ihex, int i
 }
 
 // ---------------------------------------------------------------- asymptotes
+// Every closed form below also returns `rel`, a first-order estimate of its
+// relative error from the FP32 roundings that matter: a sine or cosine of an
+// argument theta = c atan(.) carries ~|theta| 2.4e-7 absolute error (the
+// argument's rounding, c up to ~400), (1+x)^e = exp2(e log2(1+x)) carries
+// ~|e log2(1+x)| 1.25e-7 + 1.2e-7 relative, products ~3e-7; the sum of the
+// terms' absolute errors over the magnitude of the result accounts for
+// cancellation between the terms (near zeros of the form factors).
+#define TRIG_ERR(theta) (fabsf(theta) * 2.4e-7f + 6e-8f)
+
+// (1+x)^e and its relative error estimate
+__device__ __forceinline__ float powp1f_e(float x, float e, float &err) {
+    const float y = e * log1pf(x) * LOG2E_F;
+    err = fabsf(y) * 1.25e-7f + 1.2e-7f;
+    return exp2f(y);
+}
+
 // sphere P(q), q >= 0.4 limq4 (Source/sc_lib_formpq_partSphere.h:263-269)
-__device__ float sphere_pq_asym(float argq, float zr) {
+__device__ float sphere_pq_asym(float argq, float zr, float &rel) {
     const float t = atanf(2.0f * argq);
     const float x2 = 4.0f * argq * argq;
     const float pqr = (1.0f / (2.0f * zr * (zr - 1) * (zr - 2) * (zr - 3))) / (argq * argq * argq * argq);
-    const float pq1 = pqr * (1 + cosf((zr - 3) * t) / powp1f(x2, (zr - 3) / 2.0f));
-    const float pq2 = (pqr / ((zr - 4) * argq)) * sinf((zr - 4) * t) / powp1f(x2, (zr - 4) / 2.0f);
+    float e1, e2, e3;
+    const float th1 = (zr - 3) * t, th2 = (zr - 4) * t, th3 = (zr - 5) * t;
+    const float P1 = powp1f_e(x2, (zr - 3) / 2.0f, e1), P2 = powp1f_e(x2, (zr - 4) / 2.0f, e2),
+                P3 = powp1f_e(x2, zr - 5, e3);
+    const float C1 = cosf(th1), S2 = sinf(th2), C3 = cosf(th3);
+    const float pq1 = pqr * (1 + C1 / P1);
+    const float b2 = pqr / ((zr - 4) * argq);
+    const float pq2 = b2 * S2 / P2;
+    const float b3 = pqr / ((zr - 4) * (zr - 5) * argq * argq);
     // the reference divides by 2 outside the pow (reproduced)
-    const float pq3 = (pqr / ((zr - 4) * (zr - 5) * argq * argq)) * (1 - cosf((zr - 5) * t) / powp1f(x2, zr - 5) / 2.0f);
-    return 9.0f * (pq1 - 2.0f * pq2 + pq3);
+    const float pq3 = b3 * (1 - C3 / P3 / 2.0f);
+    const float v = 9.0f * (pq1 - 2.0f * pq2 + pq3);
+    const float E = fabsf(pqr) * ((TRIG_ERR(th1) + fabsf(C1) * e1) / P1 + 3e-7f * fabsf(1 + C1 / P1)) +
+                    2.0f * fabsf(b2) * ((TRIG_ERR(th2) + fabsf(S2) * e2) / P2 + 3e-7f * fabsf(S2 / P2)) +
+                    fabsf(b3) * ((TRIG_ERR(th3) + fabsf(C3) * e3) / (2.0f * P3) + 3e-7f * fabsf(1 - C3 / P3 / 2.0f));
+    rel = 9.0f * E / fabsf(v) + 3e-7f;
+    return v;
 }
 
 // sphere F(q), q >= 0.4 limq4f (Source/sc_lib_formfq_partSphere.h:443-448)
-__device__ float sphere_fq_asym(float argq, float zr) {
+__device__ float sphere_fq_asym(float argq, float zr, float &rel) {
     const float t = atanf(argq);
     const float x2 = argq * argq;
     const float pqr = 1.0f / (zr * (zr - 1)) / (argq * argq);
-    const float pq1 = pqr * cosf((zr - 1) * t) / powp1f(x2, (zr - 1) / 2.0f);
-    const float pq2 = (pqr / ((zr - 2) * argq)) * sinf((zr - 2) * t) / powp1f(x2, (zr - 2) / 2.0f);
+    float e1, e2;
+    const float th1 = (zr - 1) * t, th2 = (zr - 2) * t;
+    const float P1 = powp1f_e(x2, (zr - 1) / 2.0f, e1), P2 = powp1f_e(x2, (zr - 2) / 2.0f, e2);
+    const float C1 = cosf(th1), S2 = sinf(th2);
+    const float pq1 = pqr * C1 / P1;
+    const float b2 = pqr / ((zr - 2) * argq);
+    const float pq2 = b2 * S2 / P2;
     const float pq3 = 3 * (pq2 - pq1);
+    const float E = 3.0f * (fabsf(pqr) * (TRIG_ERR(th1) + fabsf(C1) * e1) / P1 + 3e-7f * fabsf(pq1) +
+                            fabsf(b2) * (TRIG_ERR(th2) + fabsf(S2) * e2) / P2 + 3e-7f * fabsf(pq2));
+    rel = 2.0f * E / fabsf(pq3) + 3e-7f;
     return pq3 * pq3;
 }
 
 // cylinder cross-section P(q), q >= 0.65 limq4 (Source/sc_lib_formpq_partCylinder.h:271-275)
-__device__ float cyl_pqr_asym(float argpq, float zr) {
+__device__ float cyl_pqr_asym(float argpq, float zr, float &rel) {
     const float t = atanf(2.0f * argpq);
     const float x2 = 4.0f * argpq * argpq;
     const float a3 = argpq * argpq * argpq;
     const float pqr1 = (1.0f / (zr * (zr - 1) * (zr - 2))) / a3;
-    const float pqr2 = pqr1 * sinf((zr - 2) * t) / powp1f(x2, (zr - 2) / 2.0f);
-    const float pqr3 = (1.0f / (zr * (zr - 1) * (zr - 2) * (zr - 3))) / (a3 * argpq) * cosf((zr - 3) * t) /
-                       powp1f(x2, (zr - 3) / 2.0f);
-    return (4.0f / (float)M_PI) * (pqr1 - pqr2 - (9.0f / 8.0f) * pqr3);
+    float e2, e3;
+    const float th2 = (zr - 2) * t, th3 = (zr - 3) * t;
+    const float P2 = powp1f_e(x2, (zr - 2) / 2.0f, e2), P3 = powp1f_e(x2, (zr - 3) / 2.0f, e3);
+    const float S2 = sinf(th2), C3 = cosf(th3);
+    const float pqr2 = pqr1 * S2 / P2;
+    const float b3 = (1.0f / (zr * (zr - 1) * (zr - 2) * (zr - 3))) / (a3 * argpq);
+    const float pqr3 = b3 * C3 / P3;
+    const float v = (4.0f / (float)M_PI) * (pqr1 - pqr2 - (9.0f / 8.0f) * pqr3);
+    const float E = 3e-7f * fabsf(pqr1) + fabsf(pqr1) * (TRIG_ERR(th2) + fabsf(S2) * e2) / P2 + 3e-7f * fabsf(pqr2) +
+                    1.125f * (fabsf(b3) * (TRIG_ERR(th3) + fabsf(C3) * e3) / P3 + 3e-7f * fabsf(pqr3));
+    rel = (4.0f / (float)M_PI) * E / fabsf(v) + 3e-7f;
+    return v;
 }
 
 // Length factor of the Schulz cylinder P(q) along its axis,
@@ -130,6 +174,23 @@ __device__ float cyl_len_factor(float a, float z) {
     }
     const float a1 = 1.0f / (2.0f * z * m);
     return (a1 / (a * a)) * (1.0f - cosf(m * atanf(2.0f * a)) / powp1f(4.0f * a * a, m / 2.0f));
+}
+
+// the same with a relative error estimate (see the asymptotes above)
+__device__ float cyl_len_factor_e(float a, float z, float &rel) {
+    const float m = z - 1.0f;
+    if (fabsf(m * a) < 0.35f) {
+        rel = 1e-6f;  // alternating series of quickly falling terms
+        return cyl_len_factor(a, z);
+    }
+    const float a1 = 1.0f / (2.0f * z * m);
+    float ep;
+    const float th = m * atanf(2.0f * a);
+    const float P = powp1f_e(4.0f * a * a, m / 2.0f, ep);
+    const float C = cosf(th);
+    const float br = 1.0f - C / P;
+    rel = ((TRIG_ERR(th) + fabsf(C) * ep) / P) / fabsf(br) + 3e-7f;
+    return (a1 / (a * a)) * br;
 }
 
 // ------------------------------------------------------ compensated addition
@@ -329,8 +390,12 @@ __device__ __forceinline__ int lower_bound_f(const float *__restrict__ a, int n,
     return lo;
 }
 
+// Error estimates of the sums: a term exp2f(x) carries the relative error of
+// its argument's FP32 rounding, ~|x| 2^-23 ln 2, plus exp2f's own; the sums'
+// relative errors are the term-weighted means of those (eps_rad, eps_int).
 __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, double qy, double qz, double q,
-                            double &radint, double &intens, bool &guard) {
+                            double &radint, double &intens, double &eps_rad, double &eps_int, bool &guard) {
+    const float c0 = 2.4e-7f, c1 = 8.3e-8f;
     double width = 1;
     if (P.debyescherrer) width = 4.0 / P.domainsize;
     if (P.para) width = (4.0 / P.domainsize) + cs64::sqr(P.reldis) * P.dist * cs64::sqr(q);
@@ -344,13 +409,19 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
         const float dmax = (float)(9.4 * widthiso);
         int i = lower_bound_f(T.iq, T.n_iso, qf - dmax);
         Kahan s;
+        float w = 0.0f;
         for (; i < T.n_iso; i++) {
             const float qh = __ldg(T.iq + i);
             const float d = (qf - qh) + ql;
             if (d < -dmax) break;
-            s.add(exp2f(-k * d * d) * __ldg(T.imf + i));
+            const float x = k * d * d;
+            const float t = exp2f(-x) * __ldg(T.imf + i);
+            s.add(t);
+            w = fmaf(fabsf(t), fmaf(c1, x, c0), w);
         }
-        radint = s.value() / (M_PI * widthiso / 2.0);
+        const double sum = s.value();
+        radint = sum / (M_PI * widthiso / 2.0);
+        eps_rad = sum != 0.0 ? (double)w / fabs(sum) : 0.0;
     }
     // anisotropic peaks
     {
@@ -358,9 +429,11 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
         const float dmax = (float)(9.4 * width);
         const float kphi = (float)(4 * q * q / (M_PI * cs64::sqr(P.phiwidth)) * 1.4426950408889634);
         const float invq = (float)(1.0 / q);
+        const float cphi = kphi * 1.7e-7f;
         const float fx = (float)qx * invq, fy = (float)qy * invq, fz = (float)qz * invq;
         int i = lower_bound_f(T.aq, T.n_aniso, qf - dmax);
         Kahan s;
+        float w = 0.0f;
         for (; i < T.n_aniso; i++) {
             const float qh = __ldg(T.aq + i);
             const float d = (qf - qh) + ql;
@@ -381,10 +454,15 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
             } else {
                 yphi = acosf(c);
             }
-            const float e = exp2f(fmaf(-k * d, d, -kphi * yphi * yphi));
-            s.add(e * v.w * __ldg(T.amf + i));
+            const float x = fmaf(k * d, d, kphi * yphi * yphi);
+            const float t = exp2f(-x) * v.w * __ldg(T.amf + i);
+            s.add(t);
+            // + the angle: the FP32 cosine's rounding (~6e-8) moves yphi^2 by ~1.2e-7
+            w = fmaf(fabsf(t), fmaf(c1, x, c0 + cphi), w);
         }
-        intens = s.value() / (M_PI * width / 2.0);
+        const double sum = s.value();
+        intens = sum / (M_PI * width / 2.0);
+        eps_int = sum != 0.0 ? (double)w / fabs(sum) : 0.0;
         if (!isfinite(intens)) guard = true;  // the reference stops at an infinite sum
     }
 }
@@ -408,8 +486,10 @@ __device__ double sphere_pq_mixed(const cs_prepared &P, double q, bool &guard, d
         return cs64::series_q(P.carrp[3], q, 100);
     }
     const double zr = zr_asym(P);
-    err = EPS_PQ;
-    return sphere_pq_asym((float)(q * P.radius / (zr + 1)), (float)zr);
+    float rel;
+    const float v = sphere_pq_asym((float)(q * P.radius / (zr + 1)), (float)zr, rel);
+    err = rel;
+    return v;
 }
 
 __device__ double sphere_fq_mixed(const cs_prepared &P, double q, bool &guard, double &err) {
@@ -420,8 +500,10 @@ __device__ double sphere_fq_mixed(const cs_prepared &P, double q, bool &guard, d
         return cs64::series_q(P.carrf[3], q, 100);
     }
     const double zr = (1 - cs64::sqr(P.sigma)) / cs64::sqr(P.sigma);
-    err = EPS_PQ;
-    return sphere_fq_asym((float)(q * P.radius / (zr + 1)), (float)zr);
+    float rel;
+    const float v = sphere_fq_asym((float)(q * P.radius / (zr + 1)), (float)zr, rel);
+    err = rel;
+    return v;
 }
 
 // formpq_partCylinder, ordis 0 and 6, cs 0 (mixed)
@@ -442,8 +524,15 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             pql = cs64::series_zdir(P.carrp[0], qxs, qys);
         } else {
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-            pql = cyl_len_factor((float)arglq, (float)zl);
-            el = EPS_PQ;
+            if (fabs((zl - 1) * arglq) < 1e-3) {
+                // the reference's closed form cancels to rounding noise here
+                // (see chi_integrand_f); evaluated as the drop-in does
+                pql = cs64::len_factor_ref(arglq, zl);
+            } else {
+                float rel;
+                pql = cyl_len_factor_e((float)arglq, (float)zl, rel);
+                el = rel;
+            }
         }
     } else if (P.ordis == 0) {
         const double thr = 0.4 * P.limq[1];
@@ -484,8 +573,9 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
         if (q < thr)
             pqr = cs64::series_q(P.carrp[3], q, 120);
         else {
-            pqr = cyl_pqr_asym((float)(q * P.radius / (zr + 1)), (float)zr);
-            er = EPS_PQ;
+            float rel;
+            pqr = cyl_pqr_asym((float)(q * P.radius / (zr + 1)), (float)zr, rel);
+            er = rel;
         }
     }
     err = el + er;
@@ -512,8 +602,15 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             pql = cs64::series_zdir(P.carrf[0], qxs, qys);
         } else {
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-            pql = cyl_len_factor((float)arglq, (float)zl);
-            el = EPS_PQ;
+            if (fabs((zl - 1) * arglq) < 1e-3) {
+                // the reference's closed form cancels to rounding noise here
+                // (see chi_integrand_f); evaluated as the drop-in does
+                pql = cs64::len_factor_ref(arglq, zl);
+            } else {
+                float rel;
+                pql = cyl_len_factor_e((float)arglq, (float)zl, rel);
+                el = rel;
+            }
         }
     } else if (P.ordis == 0) {
         const double thr = 0.2 * P.limqf[1];
@@ -556,11 +653,18 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
         const float t = atanf(a);
         const float a2 = a * a;
         const float s1 = (z - 0.5f) * t, s2 = (z - 1.5f) * t;
-        const float pqr1 = (float)P.gamma_ratio[0] * rsqrtf(a2 * a) * (sinf(s1) - cosf(s1)) / powp1f(a2, (z - 0.5f) / 2.0f);
-        const float pqr2 = (float)P.gamma_ratio[1] * rsqrtf(a2 * a2 * a) * (sinf(s2) + cosf(s2)) / powp1f(a2, (z - 1.5f) / 2.0f);
+        float e1, e2;
+        const float P1 = powp1f_e(a2, (z - 0.5f) / 2.0f, e1), P2 = powp1f_e(a2, (z - 1.5f) / 2.0f, e2);
+        const float b1 = (float)P.gamma_ratio[0] * rsqrtf(a2 * a), b2 = (float)P.gamma_ratio[1] * rsqrtf(a2 * a2 * a);
+        const float T1 = sinf(s1) - cosf(s1), T2 = sinf(s2) + cosf(s2);
+        const float pqr1 = b1 * T1 / P1;
+        const float pqr2 = b2 * T2 / P2;
         const float pqr3 = (2.0f / sqrtf((float)M_PI)) * (pqr1 + (9.0f / 16.0f) * pqr2);
         pqr = (double)pqr3 * (double)pqr3;
-        er = EPS_PQ;
+        // amplitude error (two trig terms each), doubled for the square
+        const float E = fabsf(b1) * (2.0f * TRIG_ERR(s1) + fabsf(T1) * e1) / P1 + 3e-7f * fabsf(pqr1) +
+                        0.5625f * (fabsf(b2) * (2.0f * TRIG_ERR(s2) + fabsf(T2) * e2) / P2 + 3e-7f * fabsf(pqr2));
+        er = 2.0f * (2.0f / sqrtf((float)M_PI)) * E / fabsf(pqr3) + 3e-7f;
     }
     err = el + er;
     return pql * pqr;
@@ -578,21 +682,24 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
 // is recomputed in FP64.
 __device__ __forceinline__ double lattice_combine(const cs_prepared &P, double q, double pq, double errp, double fq,
                                                   double errf, double pqi, double errpi, double radint, double intens,
-                                                  double tailv, bool &guard) {
+                                                  double eps_rad, double eps_int, double tailv, bool &guard) {
     const double v = P.latpar[1] * P.latpar[2];
     const double r2 = 8 * M_PI * M_PI * M_PI * radint / (4 * M_PI * v);
-    const double e2 = exp(-P.ucb * q * q);
+    // Debye-Waller factors in FP32: relative error <= |arg| 2^-23 + 2^-22
+    const float a2 = (float)(-P.ucb * q * q), a1 = (float)(-P.dwfactor * q * q);
+    const double e2 = expf(a2), e1 = expf(a1);
+    const double ee2 = fabsf(a2) * 1.2e-7f + 2.4e-7f, ee1 = fabsf(a1) * 1.2e-7f + 2.4e-7f;
     const double szqiso = 1 + (r2 - 1) * e2;
     const double r1 = 2 * M_PI * intens / v;
-    const double e1 = exp(-P.dwfactor * q * q);
     const double ratio = fq / pq;
     const double t = ratio * (r1 - 1) * e1;
     const double szq = 1 + t;
     const double res = P.base + P.izero * (szq * pq + P.iso * szqiso * pqi) + tailv;
     // first-order error bound
-    const double dt = fabs(t) * (errf + errp) + fabs(ratio * e1 * r1) * EPS_PEAK;
+    const double dt = fabs(t) * (errf + errp + ee1) + fabs(ratio * e1 * r1) * (eps_int + EPS_PEAK);
     const double d1 = fabs(pq) * dt + fabs(szq * pq) * errp;
-    const double d2 = fabs(P.iso) * (fabs(pqi) * fabs(r2 * e2) * EPS_PEAK + fabs(szqiso * pqi) * errpi);
+    const double d2 = fabs(P.iso) * (fabs(pqi) * (fabs(r2 * e2) * (eps_rad + EPS_PEAK) + fabs((r2 - 1) * e2) * ee2) +
+                                     fabs(szqiso * pqi) * errpi);
     const double bound = fabs(P.izero) * (d1 + d2);
     if (!(bound <= 5e-6 * fabs(res))) guard = true;
     return res;
@@ -611,9 +718,9 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
     if (KEY == CS_KEY_SPHERE_GAUSS_FCC_GAUSS) {
         const double pq = sphere_pq_mixed(P, q, guard, ep);
         const double fq = sphere_fq_mixed(P, q, guard, ef);
-        double radint, intens;
-        peak_sums_f(P, T, qx, qy, qz, q, radint, intens, guard);
-        return lattice_combine(P, q, pq, ep, fq, ef, pq, ep, radint, intens, tailv, guard);
+        double radint, intens, erad, eint;
+        peak_sums_f(P, T, qx, qy, qz, q, radint, intens, erad, eint, guard);
+        return lattice_combine(P, q, pq, ep, fq, ef, pq, ep, radint, intens, erad, eint, tailv, guard);
     }
     if (KEY == CS_KEY_CYL_NONE_GAUSS) {
         double pq;
@@ -654,10 +761,10 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
             fq = cyl_fq_mixed(C, q, qx, qy, q, guard, ef);
             break;
         }
-        double radint, intens;
-        peak_sums_f(P, T, qx, qy, qz, q, radint, intens, guard);
+        double radint, intens, erad, eint;
+        peak_sums_f(P, T, qx, qy, qz, q, radint, intens, erad, eint, guard);
         // the reference's BCT function multiplies szqiso by 1 instead of pq
-        return lattice_combine(P, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, tailv, guard);
+        return lattice_combine(P, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, guard);
     }
     guard = true;
     return 0.0;

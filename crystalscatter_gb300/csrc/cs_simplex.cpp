@@ -58,6 +58,7 @@ struct Fit {
     long images = 0;
     std::string err;
     int status = CS_OK;
+    double chi2_stop = 0;  // stop once the best vertex reaches it (0: off)
 };
 
 // fehlerquadratsumme's limit check (Source/sc_simplexfit2d.cpp:24-42): true
@@ -184,7 +185,7 @@ extern "C" {
 
 int cs_simplex_fit(const cs_params *base, const double *data, int width, int height, const int *nofit,
                    cs_fit_param *params, int nparams, double stp, int maxit, double ftol, int borderpix, int bstoppix,
-                   int mode, int schedule, cs_fit_report *report) {
+                   int mode, int schedule, double chi2_stop, cs_fit_report *report) {
     if (!base || !data || width <= 0 || height <= 0 || !params || nparams <= 0 || !report) return CS_ERR_PARAM;
     std::memset(report, 0, sizeof(*report));
     if (mode != CS_MODE_FP64 && mode != CS_MODE_MIXED) return CS_ERR_PARAM;
@@ -199,11 +200,12 @@ int cs_simplex_fit(const cs_params *base, const double *data, int width, int hei
     F.bstop = bstoppix;
     F.mode = mode;
     F.schedule = schedule;
+    F.chi2_stop = chi2_stop;
     return run_simplex(F, params, nparams, stp, maxit, ftol, report);
 }
 
 int cs_simplex_minimize(cs_objective_fn fn, void *ctx, cs_fit_param *params, int nparams, double stp, int maxit,
-                        double ftol, int schedule, cs_fit_report *report) {
+                        double ftol, int schedule, double chi2_stop, cs_fit_report *report) {
     if (!fn || !params || nparams <= 0 || !report) return CS_ERR_PARAM;
     std::memset(report, 0, sizeof(*report));
     if (schedule != CS_FIT_SEQUENTIAL && schedule != CS_FIT_BATCHED) return CS_ERR_PARAM;
@@ -211,6 +213,7 @@ int cs_simplex_minimize(cs_objective_fn fn, void *ctx, cs_fit_param *params, int
     F.fn = fn;
     F.fn_ctx = ctx;
     F.schedule = schedule;
+    F.chi2_stop = chi2_stop;
     return run_simplex(F, params, nparams, stp, maxit, ftol, report);
 }
 
@@ -357,6 +360,7 @@ int run_simplex(Fit &F, cs_fit_param *params, int nparams, double stp, int maxit
                 if (i != ihi) inhi = i;
             }
         }
+        if (F.chi2_stop > 0 && y[ilo] <= F.chi2_stop) break;  // (extension: target chi^2 reached)
         if (std::isnan(y[ihi]) || std::isnan(y[ilo]) || std::fabs(y[ihi]) + std::fabs(y[ilo]) == 0) {
             aborted = true;
             break;

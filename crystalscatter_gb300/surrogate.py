@@ -1,0 +1,207 @@
+"""Surrogate-seeded 2D fits: a small network, trained on patterns the
+simulator itself computes, proposes the simplex's start point; the exact
+calculation refines and judges every fit (the reference's fit,
+Source/sc_simplexfit2d.cpp, starts wherever the user puts it).
+
+Families (parameters uniform within +-30 % of the nominal values):
+  "2"   cylinders, Gaussian orientation, axis in the detector plane at
+        azimuth 30 deg (the benchmark's config 2) with its 8 free parameters
+        radius, sigma, length, sigma_L, orientation width, theta, phi, I0;
+  "2x"  the same at azimuth 0 (axis along x), whose orientation average runs
+        the full nested Romberg; theta and phi stay at 90 / 0, because any
+        other value selects the reference's general-orientation case, whose
+        orientation integral is zero (6 free parameters).
+
+Network: parameters (scaled to [-1, 1]) -> 512 -> 512 -> 512 -> 64 x 64
+log10 intensity (GELU, BF16 tensor-core GEMMs, FP32 accumulation; the
+library's cs_mlp kernels), bilinearly upsampled to the 256 x 256 fit grid.
+
+Training patterns are computed on a 128 x 128 detector with the fit image's
+q-range and averaged over 2 x 2 pixels; targets carry Poisson noise (a peak of
+`counts` counts) on the 256 x 256 fit grid.
+"""
+import math
+import time
+
+import numpy as np
+
+import crystalscatter_gb300 as cs
+from crystalscatter_gb300 import configs as C
+
+SPREAD = 0.30
+FLOOR = 1e-9  # intensity floor of the log10 targets (zero pixels of the degenerate family)
+FAMILIES = {
+    "2": (C.CYL_GAUSS, ["EditRadius", "EditSigma", "Length", "SigmaL", "EditDbeta", "theta", "phi", "I0"]),
+    "2x": (C.CYL_GAUSS_X, ["EditRadius", "EditSigma", "Length", "SigmaL", "EditDbeta", "I0"]),
+}
+# first key in the fit table: the reference's initialisation zeroes the first
+# parameter (sorted by key) of every initial vertex; EditAzi sorts first, is not
+# used by these families and its limits 0..360 are not checked
+PAD_KEY = {"key": "EditAzi", "min": 0.0, "max": 360.0, "start": 5.0, "used": True}
+
+
+class Family:
+    def __init__(self, name, fit_grid=128):
+        base, keys = FAMILIES[name]
+        self.name = name
+        self.keys = keys
+        self.nominal = {k: float(base.get(k, 1.0 if k == "I0" else 0.0)) for k in keys}
+        self.fit_base = C.scaled(base, fit_grid)  # 256 x 256 fit image, the detector's q-range
+        self.train_base = C.scaled(base, 64)      # 128 x 128 training patterns
+
+    def params(self, u, base):
+        p = dict(base)
+        for k, v in zip(self.keys, u):
+            p[k] = self.nominal[k] * (1.0 + SPREAD * float(v))
+        return p
+
+    def limits(self, k):
+        a, b = self.nominal[k] * (1 - SPREAD), self.nominal[k] * (1 + SPREAD)
+        return min(a, b), max(a, b)
+
+    def u_of(self, res):
+        return np.array([(res[k] / self.nominal[k] - 1.0) / SPREAD for k in self.keys])
+
+
+def bin2(img):
+    h, w = img.shape[-2:]
+    return img.reshape(img.shape[:-2] + (h // 2, 2, w // 2, 2)).mean(axis=(-1, -3))
+
+
+def simulate(fam, U, base, mode=cs.CS_MODE_MIXED, chunk=1024):
+    """images of the parameter vectors U (n x k) on `base`'s detector"""
+    out = []
+    b = cs.SasCalcBatch()
+    for s in range(0, len(U), chunk):
+        sets = [fam.params(u, base) for u in U[s:s + chunk]]
+        out.extend(b.calc(sets, mode=mode))
+    b.cleanup()
+    return np.stack(out)
+
+
+def training_set(fam, n, seed=0, mode=cs.CS_MODE_MIXED):
+    """(U, Y): n parameter vectors in [-1, 1]^k and 64 x 64 log10 targets"""
+    rng = np.random.default_rng(seed)
+    U = rng.uniform(-1, 1, (n, len(fam.keys)))
+    imgs = simulate(fam, U, fam.train_base, mode)
+    binned = bin2(np.where(np.isfinite(imgs), imgs, 0.0))  # the reference's non-finite pixels count as empty
+    Y = np.log10(np.maximum(binned, FLOOR)).reshape(n, -1).astype(np.float32)
+    return U.astype(np.float32), Y
+
+
+class Surrogate:
+    """the trained network with its input/output scaling"""
+
+    def __init__(self, fam, hidden=512, seed=0):
+        self.fam = fam
+        self.net = cs.SurrogateMLP(len(fam.keys), hidden, 64 * 64, seed=seed)
+        self.mean, self.std = 0.0, 1.0
+
+    def train(self, U, Y, epochs=30, batch=512, lr=1e-3, seed=0):
+        import torch
+        self.mean = float(Y.mean())
+        self.std = float(Y.std()) or 1.0
+        x = torch.from_numpy(U).cuda()
+        y = torch.from_numpy((Y - self.mean) / self.std).cuda()
+        n = len(U)
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        steps = epochs * max(1, n // batch)
+        losses = []
+        k = 0
+        t0 = time.perf_counter()
+        for ep in range(epochs):
+            perm = torch.randperm(n, generator=g).cuda()
+            for s in range(0, n - batch + 1, batch):
+                idx = perm[s:s + batch]
+                rate = lr * 0.5 * (1 + math.cos(math.pi * k / steps))
+                want = s + 2 * batch > n
+                loss = self.net.train_step(x[idx].contiguous(), y[idx].contiguous(), rate, want_loss=want)
+                if want:
+                    losses.append(loss)
+                k += 1
+        torch.cuda.synchronize()
+        return {"epochs": epochs, "steps": k, "seconds": time.perf_counter() - t0, "loss_per_epoch": losses}
+
+    def predict(self, U):
+        """64 x 64 log10 intensities of the rows of U (CUDA tensor)"""
+        return self.net.forward(U) * self.std + self.mean
+
+    def propose(self, target, rounds=3, candidates=4096, keep=16, seed=0):
+        """start vector u (in [-1, 1]^k) minimising the FQSVERGL distance of the
+        upsampled prediction to the target (256 x 256, pixels <= 0 ignored)"""
+        import torch
+        rng = np.random.default_rng(seed)
+        t = torch.from_numpy(np.log10(np.where(target > 0, target, 1.0))).float().cuda()
+        mask = torch.from_numpy(target > 0).cuda()
+        k = len(self.fam.keys)
+        centre, width = np.zeros(k), 1.0
+        best_u, best_c = None, np.inf
+        for r in range(rounds):
+            U = np.clip(centre + width * rng.uniform(-1, 1, (candidates, k)), -1, 1).astype(np.float32)
+            if best_u is not None:
+                U[0] = best_u
+            cost = []
+            for s in range(0, candidates, 512):
+                pred = self.predict(torch.from_numpy(U[s:s + 512]).cuda()).reshape(-1, 64, 64)
+                up = cs.upsample_bilinear(pred, target.shape[0] // 64)
+                d = torch.where(mask, up - t, torch.zeros_like(up))
+                cost.append((d * d).sum(dim=(1, 2)).cpu().numpy())
+            cost = np.concatenate(cost)
+            order = np.argsort(cost)
+            if cost[order[0]] < best_c:
+                best_c, best_u = float(cost[order[0]]), U[order[0]].copy()
+            centre = U[order[:keep]].mean(axis=0)
+            width *= 0.35
+        return best_u, best_c
+
+
+def noisy_target(fam, u, counts=1e4, seed=0):
+    """the 512 x 512 image of parameters u, averaged to 256 x 256, with Poisson
+    noise scaled to `counts` counts at the peak (zero-count pixels are 0)"""
+    img = simulate(fam, np.array([u]), C.scaled(FAMILIES[fam.name][0], 256), mode=cs.CS_MODE_FP64)[0]
+    img = bin2(np.where(np.isfinite(img), img, 0.0))
+    rng = np.random.default_rng(seed)
+    peak = float(np.max(img))
+    scale = counts / peak if peak > 0 else 1.0
+    return rng.poisson(np.maximum(img, 0) * scale) / scale
+
+
+def fit_table(fam, u_start):
+    table = [dict(PAD_KEY)]
+    for k, v in zip(fam.keys, u_start):
+        lo, hi = fam.limits(k)
+        table.append({"key": k, "min": lo, "max": hi, "start": fam.nominal[k] * (1 + SPREAD * float(v)), "used": True})
+    return table
+
+
+def compare_fits(fam, sur, n_targets=8, seed=0, maxit=300, ftol=1e-5, stp=0.1):
+    """Plain fits (FP64, sequential, random start) against surrogate-seeded
+    fits (batched, mixed precision, stopping at the plain fit's chi^2)."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    for i in range(n_targets):
+        u_true = rng.uniform(-0.8, 0.8, len(fam.keys))
+        target = noisy_target(fam, u_true, seed=seed + i)
+        u_rand = rng.uniform(-1, 1, len(fam.keys))
+        t0 = time.perf_counter()
+        res_p, rep_p = cs.simplex_fit(fam.fit_base, target, fit_table(fam, u_rand), stp=stp, maxit=maxit, ftol=ftol,
+                                      mode=cs.CS_MODE_FP64, schedule=cs.CS_FIT_SEQUENTIAL)
+        t_plain = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        u_s, _ = sur.propose(target, seed=seed + i)
+        t_prop = time.perf_counter() - t0
+        res_s, rep_s = cs.simplex_fit(fam.fit_base, target, fit_table(fam, u_s), stp=stp, maxit=maxit, ftol=ftol,
+                                      mode=cs.CS_MODE_MIXED, schedule=cs.CS_FIT_BATCHED,
+                                      chi2_stop=rep_p["chi2"] * (1 + 1e-3))
+        t_seeded = time.perf_counter() - t0
+        rows.append({"target": i, "chi2_plain": rep_p["chi2"], "chi2_seeded": rep_s["chi2"],
+                     "reached": bool(rep_s["chi2"] <= rep_p["chi2"] * (1 + 1e-3)),
+                     "t_plain_s": t_plain, "t_seeded_s": t_seeded + t_prop, "t_propose_s": t_prop,
+                     "images_plain": rep_p["images"], "images_seeded": rep_s["images"],
+                     "iters_plain": rep_p["repetitions"], "iters_seeded": rep_s["repetitions"],
+                     "u_err_plain": float(np.abs(fam.u_of(res_p) - u_true).max()),
+                     "u_err_seeded": float(np.abs(fam.u_of(res_s) - u_true).max()),
+                     "u_err_start": float(np.abs(u_s - u_true).max())})
+    sp = [r["t_plain_s"] / r["t_seeded_s"] for r in rows]
+    return {"family": fam.name, "targets": n_targets, "median_speedup": float(np.median(sp)),
+            "reached_fraction": float(np.mean([r["reached"] for r in rows])), "rows": rows}

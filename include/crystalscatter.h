@@ -259,7 +259,9 @@ int cs_batch_fit_chi2(cs_batch *b, int mode, double *chi2, long *cnt, long *nanc
    independent vertices and, per iteration, the reference's next candidate
    vertices speculatively as one batch (same decisions and result, fewer
    host round trips, more images). mode CS_MODE_MIXED judges vertices by the
-   mixed-precision images. */
+   mixed-precision images. chi2_stop > 0 (no counterpart in the reference; 0
+   keeps the reference's behaviour) also ends the fit once the best vertex's
+   chi^2 is at or below it. */
 #define CS_FIT_SEQUENTIAL 0
 #define CS_FIT_BATCHED 1
 typedef struct cs_fit_param {
@@ -280,7 +282,7 @@ typedef struct cs_fit_report {
 } cs_fit_report;
 int cs_simplex_fit(const cs_params *base, const double *data, int width, int height, const int *nofit,
                    cs_fit_param *params, int nparams, double stp, int maxit, double ftol, int borderpix, int bstoppix,
-                   int mode, int schedule, cs_fit_report *report);
+                   int mode, int schedule, double chi2_stop, cs_fit_report *report);
 /* The same simplex over a caller's objective instead of the image chi^2
    (no GPU involved): fn receives npoints parameter vectors of nparams values
    each (the table order of the simplex: fitted keys sorted, then fixed keys
@@ -288,7 +290,36 @@ int cs_simplex_fit(const cs_params *base, const double *data, int width, int hei
    without a call. CS_FIT_SEQUENTIAL passes one point per call. */
 typedef void (*cs_objective_fn)(const double *points, int npoints, int nparams, double *values, void *ctx);
 int cs_simplex_minimize(cs_objective_fn fn, void *ctx, cs_fit_param *params, int nparams, double stp, int maxit,
-                        double ftol, int schedule, cs_fit_report *report);
+                        double ftol, int schedule, double chi2_stop, cs_fit_report *report);
+
+/* ---- Surrogate network (no counterpart in the reference) -------------------
+   A multilayer perceptron n_in -> hidden -> hidden -> hidden -> n_out (GELU
+   after the hidden layers) that maps parameter vectors to log intensities on a
+   coarse detector grid; it proposes start points for the simplex fit. BF16
+   weights and activations into tensor-core GEMMs with FP32 accumulation; FP32
+   master weights updated by Adam on the device. hidden and n_out must be
+   multiples of 128, n_in <= 256. All data pointers are device pointers
+   (FP32, row-major, n rows); stream NULL = the network's own stream, which is
+   ordered with the legacy default stream (work queued there before the call
+   is seen, work queued there after it waits). */
+typedef struct cs_mlp cs_mlp;
+cs_mlp *cs_mlp_create(int n_in, int hidden, int n_out, unsigned long long seed);
+void cs_mlp_destroy(cs_mlp *m);
+const char *cs_mlp_last_error(cs_mlp *m);
+int cs_mlp_forward(cs_mlp *m, const float *d_x, int n, float *d_y, void *stream);
+/* gradients of the mean squared error over the n x n_out outputs (kept in the
+   network, read with cs_mlp_get_layer); loss (host) may be NULL */
+int cs_mlp_gradients(cs_mlp *m, const float *d_x, const float *d_t, int n, float *loss, void *stream);
+/* gradients, then one Adam step (beta 0.9 / 0.999, eps 1e-8) with rate lr */
+int cs_mlp_train_step(cs_mlp *m, const float *d_x, const float *d_t, int n, float lr, float *loss, void *stream);
+/* layer l = 0..3: rows x cols of its weight matrix (cols of layer 0 padded to
+   a multiple of 32); FP32 weights, bias and last gradients to/from host */
+int cs_mlp_layer_dims(cs_mlp *m, int l, int *rows, int *cols);
+int cs_mlp_get_layer(cs_mlp *m, int l, float *w, float *b, float *gw, float *gb);
+int cs_mlp_set_layer(cs_mlp *m, int l, const float *w, const float *b);
+/* bilinear upsampling of n square s x s FP32 images by an integer factor
+   (pixel-centre aligned, clamped at the border), device pointers */
+int cs_upsample_bilinear(const float *d_in, int n, int s, int factor, float *d_out, void *stream);
 
 /* Host-buffer forms: run the prepared batch (persistent schedule, a redo
    overflow handled internally) and copy all images into out; cs_calc_batch

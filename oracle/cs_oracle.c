@@ -52,9 +52,11 @@
    library; pixels with a large spread cannot be reproduced to 1e-10 by any
    other libm and are reported separately. Mode 0 disables the probe. */
 static int g_probe_mode = 0;
+static int g_probe_mask = 0x1FF; /* functions the probe moves (bit k = function k) */
 void oracle_set_probe(int mode) { g_probe_mode = mode; }
+void oracle_set_probe_mask(int mask) { g_probe_mask = mask; }
 static double probe_(double r, int fn) {
-    if (!g_probe_mode || !isfinite(r)) return r;
+    if (!g_probe_mode || !((g_probe_mask >> fn) & 1) || !isfinite(r)) return r;
     return nextafter(r, ((g_probe_mode >> fn) & 1) ? INFINITY : -INFINITY);
 }
 #define sin(x) probe_(sin(x), 0)
