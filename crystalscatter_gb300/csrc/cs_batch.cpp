@@ -169,13 +169,13 @@ long region_pixels(const cs_prepared &P) {
 
 size_t image_doubles(const cs_prepared &P) { return (size_t)(P.xmax - P.xmin) * (size_t)(P.ymax - P.ymin); }
 
-// Redo entries per group when the caller asked for none: a quarter of the
-// group's pixels, at least 2^20, at most the group's pixels.
+// Redo entries per group when the caller asked for none: one per pixel of the
+// largest group (8 B per pixel, as much as the image), so the list cannot
+// overflow.
 long auto_redo_cap(const cs_batch *b) {
     long most = 0;
     for (const auto &g : b->groups) most = std::max(most, g.tiles * (long)CS_BATCH_TILE);
-    long cap = std::max(most / 4, 1L << 20);
-    return std::min(cap, std::max(most, 1L));
+    return std::max(most, 1L);
 }
 
 int ensure_redo(cs_batch *b) {
@@ -346,6 +346,7 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
     std::vector<std::string> errs(nsets);
     std::atomic<int> next(0);
     auto worker = [&]() {
+        cs::set_prep_threads(nt > 1 ? 1 : 0);  // sets in parallel, each set serial
         for (;;) {
             const int k = next.fetch_add(1);
             if (k >= nsets) break;

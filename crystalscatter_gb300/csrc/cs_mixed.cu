@@ -76,17 +76,17 @@ __device__ __forceinline__ void q_of_pixel(const cs_prepared &P, int ihex, int i
 // ---------------------------------------------------------------- asymptotes
 // Every closed form below also returns `rel`, a first-order estimate of its
 // relative error from the FP32 roundings that matter: a sine or cosine of an
-// argument theta = c atan(.) carries ~|theta| 2.4e-7 absolute error (the
+// argument theta = c atan(.) carries ~|theta| 1.2e-7 absolute error (the
 // argument's rounding, c up to ~400), (1+x)^e = exp2(e log2(1+x)) carries
-// ~|e log2(1+x)| 1.25e-7 + 1.2e-7 relative, products ~3e-7; the sum of the
+// ~|e log2(1+x)| 8e-8 + 1.2e-7 relative, products ~3e-7; the sum of the
 // terms' absolute errors over the magnitude of the result accounts for
 // cancellation between the terms (near zeros of the form factors).
-#define TRIG_ERR(theta) (fabsf(theta) * 2.4e-7f + 6e-8f)
+#define TRIG_ERR(theta) (fabsf(theta) * 1.2e-7f + 6e-8f)
 
 // (1+x)^e and its relative error estimate
 __device__ __forceinline__ float powp1f_e(float x, float e, float &err) {
     const float y = e * log1pf(x) * LOG2E_F;
-    err = fabsf(y) * 1.25e-7f + 1.2e-7f;
+    err = fabsf(y) * 8e-8f + 1.2e-7f;
     return exp2f(y);
 }
 

@@ -19,7 +19,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "cs_prep.h"
@@ -35,6 +40,114 @@ constexpr double kEps9 = 0.000000001; // eps9, Source/sc_math.h:45
 constexpr double kEps3 = 0.001;       // eps3, Source/sc_math.h:39
 
 inline double sqr(double x) { return x * x; }
+
+// Threads for the per-n loops of coefficients(): the O(n^2) sums over
+// long-double factorials (software-emulated quad precision on aarch64) are
+// independent for different n once the recurrences are done. A thread that
+// prepares many sets at once (a batch worker) keeps them serial.
+thread_local int t_prep_threads = 0;  // 0: min(8, hardware threads)
+
+}  // namespace
+
+void set_prep_threads(int n) { t_prep_threads = n; }
+
+namespace {
+
+int prep_threads() {
+    if (t_prep_threads > 0) return t_prep_threads;
+    const unsigned hw = std::thread::hardware_concurrency();
+    return (int)std::max(1u, std::min(8u, hw));
+}
+
+// Persistent workers for parallel_n (created on first use). Tasks n are taken
+// from an atomic counter; the calling thread works too. One loop at a time: a
+// caller that finds the pool busy (another thread preparing) runs serially.
+class PrepPool {
+public:
+    static PrepPool &get() {
+        // never destroyed: its detached workers wait on its condition
+        // variable until the process ends
+        static PrepPool *pool = new PrepPool;
+        return *pool;
+    }
+    bool try_run(int lo, int hi, int threads, const std::function<void(int)> &f) {
+        std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
+        if (!busy.owns_lock()) return false;
+        ensure(threads - 1);
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            job_ = &f;
+            hi_ = hi;
+            next_.store(lo);
+            active_ = (int)workers_.size();
+            gen_++;
+        }
+        cv_.notify_all();
+        work();
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&] { return active_ == 0; });
+        job_ = nullptr;
+        return true;
+    }
+
+private:
+    std::vector<std::thread> workers_;
+    std::mutex run_mu_, mu_;
+    std::condition_variable cv_, done_cv_;
+    const std::function<void(int)> *job_ = nullptr;
+    std::atomic<int> next_{0};
+    int hi_ = 0, active_ = 0;
+    unsigned long gen_ = 0;
+
+    void work() {
+        for (;;) {
+            const int n = next_.fetch_add(1);
+            if (n > hi_) break;
+            (*job_)(n);
+        }
+    }
+    void ensure(int n) {
+        while ((int)workers_.size() < n) {
+            // the worker starts from the generation current now, before the
+            // caller publishes the next job (a worker that read gen_ only
+            // once running could miss that job and wait forever)
+            unsigned long start;
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                start = gen_;
+            }
+            workers_.emplace_back([this, start] {
+                unsigned long seen = start;
+                for (;;) {
+                    {
+                        std::unique_lock<std::mutex> lk(mu_);
+                        cv_.wait(lk, [&] { return gen_ != seen; });
+                        seen = gen_;
+                    }
+                    work();
+                    {
+                        std::lock_guard<std::mutex> lk(mu_);
+                        active_--;
+                    }
+                    done_cv_.notify_one();
+                }
+            });
+            workers_.back().detach();
+        }
+    }
+};
+
+// f(n) for n in [lo, hi] on the pool; every value is computed by the same
+// operations as in a serial loop, only the order of independent n differs
+template <class F>
+void parallel_n(int lo, int hi, const F &f) {
+    const int T = prep_threads();
+    if (T > 1 && hi - lo >= 32) {
+        const std::function<void(int)> fn = [&f](int n) { f(n); };
+        if (PrepPool::get().try_run(lo, hi, T, fn)) return;
+    }
+    for (int n = lo; n <= hi; n++) f(n);
+}
 
 // log2 of a positive double, good to ~1e-15 absolute: the exponent from frexp
 // (exact), the mantissa in [0.5, 1) through log2.
@@ -511,6 +624,10 @@ bool Prep::coefficients() {
                     lgpw11[e] = pw11[e] > 0 ? lg2(pw11[e]) : 0.0;  // unused where the product is 0
                     lgpw13[e] = pw13[e] > 0 ? lg2(pw13[e]) : 0.0;
                 }
+                // recurrences (serial), then the rows of every n (parallel),
+                // then the searches over n (serial)
+                long double xln[kNmax + 1];
+                double xrn[kNmax + 1];
                 for (int n = 1; n <= nmax; n++) {
                     z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
                     z12vl[n] = z12vl[n - 1] * ((zl + 1) - 2 + 2 * n) * ((zl + 1) - 1 + 2 * n);
@@ -521,6 +638,12 @@ bool Prep::coefficients() {
                     gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
                     xln_n = -xln_n * xl2z;
                     xrn_n = -xrn_n * xr2z;
+                    xln[n] = xln_n;
+                    xrn[n] = xrn_n;
+                }
+                parallel_n(1, nmax, [&](int n) {
+                    const long double xln_n = xln[n];
+                    const double xrn_n = xrn[n];
                     for (int m = 0; m <= n; m++) {
                         double sump = 0.0;
                         double lim = lim0;  // negligible_lg2(sump)
@@ -559,6 +682,8 @@ bool Prep::coefficients() {
                     for (int m = 0; m <= n; m++)
                         sump = sump + z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
                     carr4f[n] = xrn_n * sump;
+                });
+                for (int n = 1; n <= nmax; n++) {
                     if (search1) {
                         if (carr1p[n] < 1e-50) {
                             n1 = n;
@@ -624,6 +749,9 @@ bool Prep::coefficients() {
                 double xrn_n = 1.0;
                 long double xln_n = 1.0;
                 const int orc = P.orcase;
+                // recurrences (serial), rows of every n (parallel), searches (serial)
+                long double xln[kNmax + 1];
+                double xrn[kNmax + 1];
                 for (int n = 1; n <= nmax; n++) {
                     z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
                     if (orc == CS_ORC_XAXIS)
@@ -635,34 +763,36 @@ bool Prep::coefficients() {
                     gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
                     xln_n = -xln_n * xl2z;
                     xrn_n = -xrn_n * xr2z;
+                    xln[n] = xln_n;
+                    xrn[n] = xrn_n;
+                }
+                const double intl_v = intl_const;  // every qrombdeltac moment of these blocks
+                parallel_n(1, nmax, [&](int n) {
+                    const long double xln_n = xln[n];
+                    const double xrn_n = xrn[n];
                     double sump;
                     if (orc == CS_ORC_XAXIS) {
-                        for (int m = 0; m <= n; m++) {
-                            intl = intl_const;
-                            P.carr11pm[n][m] = std::pow(4.0, m) * intl / (fk2v[m] * fkv[n - m] * fkv[n - m] * P.norm);
-                        }
+                        for (int m = 0; m <= n; m++)
+                            P.carr11pm[n][m] = std::pow(4.0, m) * intl_v / (fk2v[m] * fkv[n - m] * fkv[n - m] * P.norm);
                         carr1p[n] = std::pow(4.0, n) * z12vl[n] * xln_n / ((2.0 * n + 1) * (n + 1));
                         sump = 0.0;
                         for (int m = 0; m <= n; m++)
                             sump = sump + z12vl[m] * z12vl[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
                         carr1f[n] = fk2v[n] * xln_n * sump / (std::pow(4.0, n));
                     } else if (orc == CS_ORC_YAXIS) {
-                        for (int m = 0; m <= n; m++) {
-                            intl = intl_const;
-                            P.carr11pm[n][m] = intl / (std::pow(4.0, m) * fk2v[n - m] * fkv[m] * fkv[m] * P.norm);
-                        }
+                        for (int m = 0; m <= n; m++)
+                            P.carr11pm[n][m] = intl_v / (std::pow(4.0, m) * fk2v[n - m] * fkv[m] * fkv[m] * P.norm);
                         carr1p[n] = std::pow(4.0, 2 * n) * z12vl[n] * xln_n / ((2.0 * n + 1) * (n + 1));
                         sump = 0.0;
                         for (int m = 0; m <= n; m++)
                             sump += z12vl[m] * z12vl[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
                         carr1f[n] = fk2v[n] * xln_n * sump;
                     } else {
-                        intl = intl_const;
-                        carr1p[n] = std::pow(4.0, n) * z12vl[n] * xln_n * intl / ((2.0 * n + 1) * (n + 1) * fkv[n] * fkv[n] * P.norm);
+                        carr1p[n] = std::pow(4.0, n) * z12vl[n] * xln_n * intl_v / ((2.0 * n + 1) * (n + 1) * fkv[n] * fkv[n] * P.norm);
                         sump = 0.0;
                         for (int m = 0; m <= n; m++)
                             sump += z12vl[m] * z12vl[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
-                        carr1f[n] = fk2v[n] * xln_n * sump * intl / (std::pow(4.0, n) * fkv[n] * fkv[n] * P.norm);
+                        carr1f[n] = fk2v[n] * xln_n * sump * intl_v / (std::pow(4.0, n) * fkv[n] * fkv[n] * P.norm);
                     }
                     carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
                                 ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n]);
@@ -670,6 +800,9 @@ bool Prep::coefficients() {
                     for (int m = 0; m <= n; m++)
                         sump = sump + z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
                     carr4f[n] = xrn_n * sump;
+                });
+                intl = intl_v;
+                for (int n = 1; n <= nmax; n++) {
                     if (search1) {
                         if (carr1p[n] < 1e-50) {
                             n1 = n;
@@ -738,19 +871,25 @@ bool Prep::coeff_sphere(double z, double xr2z, double xrm2z, double p, int &n4, 
     double *carr4f = P.carrf[3], *carr5f = P.carrf[4], *carr6f = P.carrf[5];
     if (P.cs == 0) {
         long double xrn_n = 1.0;
-        long double z12v[kNmax + 1];
+        long double z12v[kNmax + 1], xrn[kNmax + 1];
         z12v[0] = 1.0;
+        // recurrences (serial), values of every n (parallel), searches (serial)
         for (int n = 1; n <= nmax; n++) {
             z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
             fkv[n] = fkv[n - 1] * n;
             gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
             xrn_n = -xrn_n * xr2z;
-            carr4p[n] = 9 * std::sqrt(M_PI) * std::pow(4.0, n) * z12v[n] * xrn_n /
+            xrn[n] = xrn_n;
+        }
+        parallel_n(1, nmax, [&](int n) {
+            carr4p[n] = 9 * std::sqrt(M_PI) * std::pow(4.0, n) * z12v[n] * xrn[n] /
                         (2.0 * (n + 3) * (n + 2) * (n + 3 / 2.0) * gam3[n] * fkv[n]);
             double binsum = 0.0;
             for (int m = 0; m <= n; m++)
                 binsum += z12v[m] * z12v[n - m] / ((m + 3 / 2.0) * gam3[m] * (n - m + 3 / 2.0) * gam3[n - m] * fkv[m] * fkv[n - m]);
-            carr4f[n] = 9 * M_PI * xrn_n * binsum / 16.0;
+            carr4f[n] = 9 * M_PI * xrn[n] * binsum / 16.0;
+        });
+        for (int n = 1; n <= nmax; n++) {
             if (std::fabs(carr4p[n]) < kMin) {
                 if (n < n4) n4 = n;
             }

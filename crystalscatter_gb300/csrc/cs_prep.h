@@ -20,6 +20,11 @@ std::string check_all_parameters(const cs_params &in, int shp, int ign_cbs);
 int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_switch, int ign_cbs, int check,
             cs_prepared *out, std::string &err);
 
+// Threads the calling thread uses for the per-n loops of the coefficient
+// preparation (0: up to 8 hardware threads; 1: serial, e.g. inside a thread
+// that prepares one of many sets).
+void set_prep_threads(int n);
+
 // The reference's own Gamma function (Source/sc_calc_generic_gpu.cu:613-673),
 // evaluated on the host where pixel kernels need pixel-independent ratios.
 double ref_gamma(double z);

@@ -222,8 +222,8 @@ int cs_batch_replay(cs_batch *b, void *stream);
 int cs_batch_graph_nodes(cs_batch *b, size_t *n);
 /* Mixed persistent form: guarded pixels of the last run (waits for stream).
    CS_ERR_SIZE when the redo list overflowed (some pixels then keep their
-   FP32 value): raise the capacity (entries per key group, 0 = automatic:
-   a quarter of the group's pixels, at least 2^20) and run again. */
+   FP32 value): raise the capacity (entries per key group, 0 = automatic: one
+   per pixel of the largest group, which cannot overflow) and run again. */
 int cs_batch_redo_pixels(cs_batch *b, void *stream, long *n, long *capacity);
 int cs_batch_set_redo_capacity(cs_batch *b, long entries_per_group);
 double cs_batch_timer_ms(cs_batch *b); /* host preparation time of the last cs_batch_prepare */
