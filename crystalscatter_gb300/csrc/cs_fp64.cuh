@@ -23,6 +23,7 @@
 
 #include "cs_prepared.h"
 #include "cs_tables.h"
+#include "cs_series_stop.h"
 
 namespace cs64 {
 
@@ -75,22 +76,9 @@ __device__ __forceinline__ void convert_idx2q(const cs_prepared &P, int ihex, in
 // written with __dmul_rn/__dadd_rn, which are never fused into a
 // multiply-add, so they round as the reference's separate operations in every
 // translation unit, also in those compiled with contraction.
-// The reference's stop test fabs((s - old) / s) < 0.0001, decided without the
-// FP64 division wherever rounding cannot matter: with A = fl(0.0001 |s|), an
-// increment below A (1 - 2^-50) has an exact quotient below 0.0001 (1 - 2^-52),
-// whose rounding stays below 0.0001; one above A (1 + 2^-50) stays above. Only
-// inside that band, and for |s| outside [1e-290, 1e290] (zero, NaN, inf,
-// products that could be subnormal), is the quotient computed as the
-// reference computes it. The decision is the
-// reference's in every case.
-__device__ __forceinline__ bool series_converged(double s, double old) {
-    if (!(fabs(s) > 1e-290 && fabs(s) < 1e290)) return fabs((s - old) / s) < 0.0001;  // (no subnormal products)
-    const double d = fabs(__dadd_rn(s, -old));
-    const double a = __dmul_rn(0.0001, fabs(s));
-    if (d < __dmul_rn(a, 1.0 - 0x1p-50)) return true;
-    if (d > __dmul_rn(a, 1.0 + 0x1p-50)) return false;
-    return fabs((s - old) / s) < 0.0001;
-}
+// The reference's stop test fabs((s - old) / s) < 0.0001 with its decision in
+// every case, almost always without the FP64 division (cs_series_stop.h).
+using cs_series::series_converged;
 
 __device__ __forceinline__ double series_q(const double *__restrict__ c, double q, int nmax) {
     double pqsum = 1.0;

@@ -32,8 +32,11 @@ def test_surrogate_start_beats_random_start():
     for i in range(4):
         u_true = rng.uniform(-0.7, 0.7, len(fam.keys))
         target = S.noisy_target(fam, u_true, seed=i)
-        u_s, _ = sur.propose(target, candidates=2048, seed=i)
+        u_s, _, short = sur.propose(target, candidates=2048, seed=i, shortlist=4)
+        assert np.array_equal(short[0], u_s) and len(short) <= 4
+        u_p, c_p = S.exact_pick(fam, target, short)
         c_s = exact_chi2(fam, target, u_s)
+        assert c_p <= c_s * (1 + 1e-4)  # mixed-precision pick vs the FP64 chi^2 of the first candidate
         c_r = np.median([exact_chi2(fam, target, rng.uniform(-1, 1, len(fam.keys))) for _ in range(5)])
         wins += c_s < 0.5 * c_r
     assert wins >= 3
