@@ -392,11 +392,11 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
     if (b->chi_b != b->hprep[0].romb_chi_b) {
         for (int k = 1; k < nsets; k++)
             if (b->hprep[k].romb_chi_b != b->hprep[0].romb_chi_b) return fail(b, CS_ERR_PARAM, "chi limits differ between sets");
-        std::vector<cs_chi_node> host(CS_NODE_COUNT);
+        std::vector<cs_chi_node> host(CS_CHI_TABLE_LEN);
         cs::build_chi_table(b->hprep[0].romb_chi_b, host.data());
-        if (!b->d_chi_own && (e = cudaMalloc(&b->d_chi_own, sizeof(cs_chi_node) * CS_NODE_COUNT)) != cudaSuccess)
+        if (!b->d_chi_own && (e = cudaMalloc(&b->d_chi_own, sizeof(cs_chi_node) * CS_CHI_TABLE_LEN)) != cudaSuccess)
             return cuda_fail(b, e, "cudaMalloc(chi table)");
-        if ((e = cudaMemcpy(b->d_chi_own, host.data(), sizeof(cs_chi_node) * CS_NODE_COUNT, cudaMemcpyHostToDevice)) != cudaSuccess)
+        if ((e = cudaMemcpy(b->d_chi_own, host.data(), sizeof(cs_chi_node) * CS_CHI_TABLE_LEN, cudaMemcpyHostToDevice)) != cudaSuccess)
             return cuda_fail(b, e, "upload chi table");
         b->chi_b = b->hprep[0].romb_chi_b;
     }

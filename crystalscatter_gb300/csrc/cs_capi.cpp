@@ -103,11 +103,11 @@ int ensure_chi(cs_handle *h, double chi_b, const cs_chi_node **out) {
     std::lock_guard<std::mutex> lock(g_chi_mutex);
     if (h->device < 0 || h->device >= 64) return fail(h, CS_ERR_CUDA, "device index out of range");
     if (!g_dchi[h->device]) {
-        cs_chi_node *host = new cs_chi_node[CS_NODE_COUNT];
+        cs_chi_node *host = new cs_chi_node[CS_CHI_TABLE_LEN];
         cs::build_chi_table(chi_b, host);
         cs_chi_node *dev = nullptr;
-        cudaError_t e = cudaMalloc(&dev, sizeof(cs_chi_node) * CS_NODE_COUNT);
-        if (e == cudaSuccess) e = cudaMemcpy(dev, host, sizeof(cs_chi_node) * CS_NODE_COUNT, cudaMemcpyHostToDevice);
+        cudaError_t e = cudaMalloc(&dev, sizeof(cs_chi_node) * CS_CHI_TABLE_LEN);
+        if (e == cudaSuccess) e = cudaMemcpy(dev, host, sizeof(cs_chi_node) * CS_CHI_TABLE_LEN, cudaMemcpyHostToDevice);
         delete[] host;
         if (e != cudaSuccess) return cuda_fail(h, e, "chi node table");
         g_dchi[h->device] = dev;

@@ -36,7 +36,7 @@ int launch_fit(const DevSet &D, const cs_prepared &P, const double *d_data, doub
 
 // Host-side node tables (built with the host libm, node by node in the
 // reference's order); see cs_tables.h.
-void build_chi_table(double chi_b, cs_chi_node *tab);
+void build_chi_table(double chi_b, cs_chi_node *tab);  // tab: CS_CHI_TABLE_LEN slots
 void build_delta_table(double delta_b, double dbeta, cs_delta_node *tab);
 
 }  // namespace cs

@@ -209,6 +209,7 @@ struct Kahan {
 struct ChiArgsF {
     float qx, qy, lz;  // lz = l/(z+1)
     float z;
+    float b;           // upper chi limit
     float p11, p12, p13, p21, p22, p23;
     int i1;
 };
@@ -269,31 +270,66 @@ __device__ __forceinline__ bool romb_stop(const double win[5], double &pq, doubl
     return false;
 }
 
-__device__ double qromb_chi_f(const Ctx &C, const ChiArgsF &A, float cd, float sd, bool &guard) {
-    const double b = C.P->romb_chi_b;
-    double win[5];
-    double cur;
+// The same extrapolation and test in FP32 for the inner (chi) integrals, whose
+// estimates are FP32-accurate in any case. The differences y_i - y_4 carry the
+// estimates' rounding (~6e-8 |y|), which moves dss by ~1e-9 |y|: about 1e-5 of
+// the threshold 1e-4 |pq|, far inside the decision band. A result below
+// 1e-30 (the reference stops below 1e-300, which FP32 cannot hold) is decided
+// in FP64 by the redo, and so is a non-finite one.
+__device__ __forceinline__ bool romb_stop_f(const float y[5], float &pq, bool &guard) {
+    const float W0 = 1.0f / 722925.0f, W1 = -4.0f / 8505.0f, W2 = 64.0f / 2025.0f, W3 = -4096.0f / 8505.0f;
+    const float U0 = 1.0f / 722925.0f, U1 = -1.0f / 8505.0f, U2 = 4.0f / 2025.0f, U3 = -64.0f / 8505.0f;
+    const float d0 = y[0] - y[4], d1 = y[1] - y[4], d2 = y[2] - y[4], d3 = y[3] - y[4];
+    pq = y[4] + fmaf(W0, d0, fmaf(W1, d1, fmaf(W2, d2, W3 * d3)));
+    const float dss = fmaf(U0, d0, fmaf(U1, d1, fmaf(U2, d2, U3 * d3)));
+    const float lhs = fabsf(dss), rhs = 1.0e-4f * fabsf(pq);
+    if (!(fabsf(pq) >= 1e-30f) || !(fabsf(pq) < INFINITY)) {
+        guard = true;
+        return true;
+    }
+    if (fabsf(lhs - rhs) <= 3e-3f * rhs) guard = true;
+    return lhs < rhs;
+}
+
+struct KahanF {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ float value() const { return s - c; }
+};
+
+// qrombchid over chi in [0, b] in FP32: nodes from the FP32 copy of the node
+// table, compensated trapezoid sums, extrapolation and stop test in FP32.
+__device__ float qromb_chi_f(const Ctx &C, const ChiArgsF &A, float cd, float sd, bool &guard) {
+    const float b = A.b;
+    const cs_chi_node_f *__restrict__ nf = reinterpret_cast<const cs_chi_node_f *>(C.chi + CS_NODE_COUNT);
+    float win[5];
+    float cur;
     int cnt;
-    double pq = 0.0;
+    float pq = 0.0f;
     {
-        const cs_chi_node n0 = C.chi[0], n1 = C.chi[1];
-        const float pa = chi_integrand_f(A, (float)n0.c, (float)n0.s, cd, sd, guard);
-        const float pb = chi_integrand_f(A, (float)n1.c, (float)n1.s, cd, sd, guard);
-        cur = 0.5 * b * ((double)pa + (double)pb);
+        const cs_chi_node_f n0 = nf[0], n1 = nf[1];
+        const float pa = chi_integrand_f(A, n0.c, n0.s, cd, sd, guard);
+        const float pb = chi_integrand_f(A, n1.c, n1.s, cd, sd, guard);
+        cur = 0.5f * b * (pa + pb);
         cnt = 1;
     }
-    double rcnt = 1.0;
+    float rcnt = 1.0f;
     win[4] = cur;
     for (int j = 2; j <= 20; j++) {
-        Kahan sum;
+        KahanF sum;
         if (j <= CS_NODE_LEVELS) {
-            const cs_chi_node *nd = C.chi + CS_NODE_OFFSET(j);
+            const cs_chi_node_f *nd = nf + CS_NODE_OFFSET(j);
             for (int k = 0; k < cnt; k++) {
-                const cs_chi_node n = nd[k];
-                sum.add(chi_integrand_f(A, (float)n.c, (float)n.s, cd, sd, guard));
+                const cs_chi_node_f n = nd[k];
+                sum.add(chi_integrand_f(A, n.c, n.s, cd, sd, guard));
             }
         } else {
-            const double del = b / cnt;
+            const double del = (double)b / cnt;
             double x = 0.5 * del;
             for (int k = 0; k < cnt; k++) {
                 float s, c;
@@ -302,15 +338,15 @@ __device__ double qromb_chi_f(const Ctx &C, const ChiArgsF &A, float cd, float s
                 x += del;
             }
         }
-        cur = 0.5 * (cur + b * sum.value() * rcnt);  // rcnt = 1/cnt exactly (cnt is a power of 2)
+        cur = 0.5f * (cur + b * sum.value() * rcnt);  // rcnt = 1/cnt exactly (cnt is a power of 2)
         cnt *= 2;
-        rcnt *= 0.5;
+        rcnt *= 0.5f;
         win[0] = win[1];
         win[1] = win[2];
         win[2] = win[3];
         win[3] = win[4];
         win[4] = cur;
-        if (j >= 5 && romb_stop(win, pq, 1.0e-300, guard)) break;
+        if (j >= 5 && romb_stop_f(win, pq, guard)) break;
     }
     return pq;
 }
@@ -558,6 +594,7 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             A.p22 = (float)P.romb_p[4];
             A.p23 = (float)P.romb_p[5];
             A.i1 = P.orcase;
+            A.b = (float)P.romb_chi_b;
             pql = qromb_delta_f(C, A, guard) / P.norm;
             el = EPS_PQ;
         }
@@ -636,6 +673,7 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             A.p22 = (float)P.romb_p[4];
             A.p23 = (float)P.romb_p[5];
             A.i1 = P.orcase;
+            A.b = (float)P.romb_chi_b;
             pql = qromb_delta_f(C, A, guard) / P.norm;
             el = EPS_PQ;
         }

@@ -1873,7 +1873,8 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
 
 // ---------------------------------------------------------------------------
 // Orientation node tables (see cs_tables.h): node x of level j in the
-// reference's order, x = a + del/2 then x += del, with a = 0.
+// reference's order, x = a + del/2 then x += del, with a = 0. The chi table
+// (CS_CHI_TABLE_LEN slots) also holds the FP32 copies after the FP64 nodes.
 // ---------------------------------------------------------------------------
 void build_chi_table(double chi_b, cs_chi_node *tab) {
     const double a = 0.0, b = chi_b;
@@ -1892,6 +1893,11 @@ void build_chi_table(double chi_b, cs_chi_node *tab) {
             nd[k].s = std::sin(x);
             x += del;
         }
+    }
+    cs_chi_node_f *f = reinterpret_cast<cs_chi_node_f *>(tab + CS_NODE_COUNT);
+    for (int k = 0; k < CS_NODE_COUNT; k++) {
+        f[k].c = (float)tab[k].c;
+        f[k].s = (float)tab[k].s;
     }
 }
 

@@ -25,6 +25,14 @@ typedef struct cs_chi_node {
     double c, s; /* cos(x), sin(x) */
 } cs_chi_node;
 
+/* FP32 copies of the chi nodes for the mixed-precision kernels: they follow the
+ * CS_NODE_COUNT FP64 nodes in the same allocation (two per cs_chi_node slot),
+ * so a chi table holds CS_CHI_TABLE_LEN cs_chi_node slots in all. */
+typedef struct cs_chi_node_f {
+    float c, s;
+} cs_chi_node_f;
+#define CS_CHI_TABLE_LEN (CS_NODE_COUNT + (CS_NODE_COUNT + 1) / 2)
+
 typedef struct cs_delta_node {
     double w;    /* sin(x)*exp(-x*x/(dbeta*dbeta)) */
     double c, s; /* cos(x), sin(x) */
