@@ -219,7 +219,7 @@ int ensure_mixed(cs_handle *h) {
                 (e = cudaMalloc(&h->d_amf, sizeof(float) * n)) != cudaSuccess ||
                 (e = cudaMalloc(&h->d_iq, sizeof(float) * n)) != cudaSuccess ||
                 (e = cudaMalloc(&h->d_imf, sizeof(float) * n)) != cudaSuccess ||
-                (e = cudaMalloc(&h->d_av, sizeof(float4) * n)) != cudaSuccess)
+                (e = cudaMalloc(&h->d_av, sizeof(float4) * 2 * n)) != cudaSuccess)
                 return cuda_fail(h, e, "cudaMalloc(peak tables)");
             h->peak_cap = n;
         }

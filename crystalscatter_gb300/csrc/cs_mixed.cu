@@ -75,30 +75,69 @@ __device__ __forceinline__ void q_of_pixel(const cs_prepared &P, int ihex, int i
 
 // ---------------------------------------------------------------- asymptotes
 // Every closed form below also returns `rel`, a first-order estimate of its
-// relative error from the FP32 roundings that matter: a sine or cosine of an
-// argument theta = c atan(.) carries ~|theta| 1.2e-7 absolute error (the
-// argument's rounding, c up to ~400), (1+x)^e = exp2(e log2(1+x)) carries
-// ~|e log2(1+x)| 8e-8 + 1.2e-7 relative, products ~3e-7; the sum of the
-// terms' absolute errors over the magnitude of the result accounts for
-// cancellation between the terms (near zeros of the form factors).
+// relative error; the sum of the terms' absolute errors over the magnitude of
+// the result accounts for cancellation between the terms (near zeros of the
+// form factors). Its sines and cosines take arguments theta = c atan(x) with
+// c up to ~400, and its powers (1+x^2)^e = exp2(e log2(1+x^2)) exponents of up
+// to a few hundred. Two forms of those arguments (ClosedArgs):
+//  * FP32: theta = c atanf(x) is off by ~|theta| 1.2e-7 (absolute: 1.8e-5 at
+//    theta = 150), the power by ~|e log2(1+x^2)| 8e-8 + 1.2e-7 (relative);
+//  * FP64: atan and log1p in FP64, theta reduced to [-pi, pi] before its FP32
+//    rounding (error |r| 6e-8 + the FP32 sine's 1.2e-7), the exponent split
+//    into an integer and a fraction in [-1/2, 1/2] (error 1.8e-7).
+// A closed form is evaluated in FP32 first and again with the FP64 arguments
+// when its estimate exceeds acc_switch<LAT>(); that costs one FP64 atan and
+// log1p. Lattice pixels amplify the form factors' errors where the structure
+// factor cancels (see lattice_combine) and switch early; the others only
+// need the estimate below the 5e-6 guard.
 #define TRIG_ERR(theta) (fabsf(theta) * 1.2e-7f + 6e-8f)
+template <bool LAT> __device__ __forceinline__ float acc_switch() { return LAT ? 4e-7f : 2e-6f; }
 
-// (1+x)^e and its relative error estimate
-__device__ __forceinline__ float powp1f_e(float x, float e, float &err) {
-    const float y = e * log1pf(x) * LOG2E_F;
-    err = fabsf(y) * 8e-8f + 1.2e-7f;
-    return exp2f(y);
-}
+template <bool ACC> struct ClosedArgs;
+
+template <> struct ClosedArgs<false> {
+    float t, l2;  // atan(x), log2(1 + x2)
+    __device__ __forceinline__ ClosedArgs(double x, double x2)
+        : t(atanf((float)x)), l2(log1pf((float)x2) * LOG2E_F) {}
+    __device__ __forceinline__ float angle(double c, float &err) const {
+        const float th = (float)c * t;
+        err = TRIG_ERR(th);
+        return th;
+    }
+    __device__ __forceinline__ float power(double e, float &err) const {
+        const float y = (float)e * l2;
+        err = fabsf(y) * 8e-8f + 1.2e-7f;
+        return exp2f(y);
+    }
+};
+
+template <> struct ClosedArgs<true> {
+    double t, l2;
+    __device__ __forceinline__ ClosedArgs(double x, double x2) : t(atan(x)), l2(log1p(x2) * 1.4426950408889634) {}
+    __device__ __forceinline__ float angle(double c, float &err) const {
+        const double th = c * t;
+        const double k = rint(th * (0.5 / M_PI));
+        const float r = (float)(th - k * (2.0 * M_PI));
+        err = fabsf(r) * 6e-8f + 1.2e-7f;
+        return r;
+    }
+    __device__ __forceinline__ float power(double e, float &err) const {
+        const double y = e * l2;
+        const double n = fmin(fmax(rint(y), -300.0), 300.0);
+        err = 1.8e-7f;
+        return ldexpf(exp2f((float)(y - n)), (int)n);
+    }
+};
 
 // sphere P(q), q >= 0.4 limq4 (Source/sc_lib_formpq_partSphere.h:263-269)
-__device__ float sphere_pq_asym(float argq, float zr, float &rel) {
-    const float t = atanf(2.0f * argq);
-    const float x2 = 4.0f * argq * argq;
+template <bool ACC>
+__device__ float sphere_pq_asym(double argq_d, double zr_d, float &rel) {
+    const ClosedArgs<ACC> A(2.0 * argq_d, 4.0 * argq_d * argq_d);
+    const float argq = (float)argq_d, zr = (float)zr_d;
     const float pqr = (1.0f / (2.0f * zr * (zr - 1) * (zr - 2) * (zr - 3))) / (argq * argq * argq * argq);
-    float e1, e2, e3;
-    const float th1 = (zr - 3) * t, th2 = (zr - 4) * t, th3 = (zr - 5) * t;
-    const float P1 = powp1f_e(x2, (zr - 3) / 2.0f, e1), P2 = powp1f_e(x2, (zr - 4) / 2.0f, e2),
-                P3 = powp1f_e(x2, zr - 5, e3);
+    float e1, e2, e3, g1, g2, g3;
+    const float th1 = A.angle(zr_d - 3, g1), th2 = A.angle(zr_d - 4, g2), th3 = A.angle(zr_d - 5, g3);
+    const float P1 = A.power((zr_d - 3) / 2.0, e1), P2 = A.power((zr_d - 4) / 2.0, e2), P3 = A.power(zr_d - 5, e3);
     const float C1 = cosf(th1), S2 = sinf(th2), C3 = cosf(th3);
     const float pq1 = pqr * (1 + C1 / P1);
     const float b2 = pqr / ((zr - 4) * argq);
@@ -107,89 +146,142 @@ __device__ float sphere_pq_asym(float argq, float zr, float &rel) {
     // the reference divides by 2 outside the pow (reproduced)
     const float pq3 = b3 * (1 - C3 / P3 / 2.0f);
     const float v = 9.0f * (pq1 - 2.0f * pq2 + pq3);
-    const float E = fabsf(pqr) * ((TRIG_ERR(th1) + fabsf(C1) * e1) / P1 + 3e-7f * fabsf(1 + C1 / P1)) +
-                    2.0f * fabsf(b2) * ((TRIG_ERR(th2) + fabsf(S2) * e2) / P2 + 3e-7f * fabsf(S2 / P2)) +
-                    fabsf(b3) * ((TRIG_ERR(th3) + fabsf(C3) * e3) / (2.0f * P3) + 3e-7f * fabsf(1 - C3 / P3 / 2.0f));
+    const float E = fabsf(pqr) * ((g1 + fabsf(C1) * e1) / P1 + 3e-7f * fabsf(1 + C1 / P1)) +
+                    2.0f * fabsf(b2) * ((g2 + fabsf(S2) * e2) / P2 + 3e-7f * fabsf(S2 / P2)) +
+                    fabsf(b3) * ((g3 + fabsf(C3) * e3) / (2.0f * P3) + 3e-7f * fabsf(1 - C3 / P3 / 2.0f));
     rel = 9.0f * E / fabsf(v) + 3e-7f;
     return v;
 }
 
 // sphere F(q), q >= 0.4 limq4f (Source/sc_lib_formfq_partSphere.h:443-448)
-__device__ float sphere_fq_asym(float argq, float zr, float &rel) {
-    const float t = atanf(argq);
-    const float x2 = argq * argq;
+template <bool ACC>
+__device__ float sphere_fq_asym(double argq_d, double zr_d, float &rel) {
+    const ClosedArgs<ACC> A(argq_d, argq_d * argq_d);
+    const float argq = (float)argq_d, zr = (float)zr_d;
     const float pqr = 1.0f / (zr * (zr - 1)) / (argq * argq);
-    float e1, e2;
-    const float th1 = (zr - 1) * t, th2 = (zr - 2) * t;
-    const float P1 = powp1f_e(x2, (zr - 1) / 2.0f, e1), P2 = powp1f_e(x2, (zr - 2) / 2.0f, e2);
+    float e1, e2, g1, g2;
+    const float th1 = A.angle(zr_d - 1, g1), th2 = A.angle(zr_d - 2, g2);
+    const float P1 = A.power((zr_d - 1) / 2.0, e1), P2 = A.power((zr_d - 2) / 2.0, e2);
     const float C1 = cosf(th1), S2 = sinf(th2);
     const float pq1 = pqr * C1 / P1;
     const float b2 = pqr / ((zr - 2) * argq);
     const float pq2 = b2 * S2 / P2;
     const float pq3 = 3 * (pq2 - pq1);
-    const float E = 3.0f * (fabsf(pqr) * (TRIG_ERR(th1) + fabsf(C1) * e1) / P1 + 3e-7f * fabsf(pq1) +
-                            fabsf(b2) * (TRIG_ERR(th2) + fabsf(S2) * e2) / P2 + 3e-7f * fabsf(pq2));
+    const float E = 3.0f * (fabsf(pqr) * (g1 + fabsf(C1) * e1) / P1 + 3e-7f * fabsf(pq1) +
+                            fabsf(b2) * (g2 + fabsf(S2) * e2) / P2 + 3e-7f * fabsf(pq2));
     rel = 2.0f * E / fabsf(pq3) + 3e-7f;
     return pq3 * pq3;
 }
 
 // cylinder cross-section P(q), q >= 0.65 limq4 (Source/sc_lib_formpq_partCylinder.h:271-275)
-__device__ float cyl_pqr_asym(float argpq, float zr, float &rel) {
-    const float t = atanf(2.0f * argpq);
-    const float x2 = 4.0f * argpq * argpq;
+template <bool ACC>
+__device__ float cyl_pqr_asym(double argpq_d, double zr_d, float &rel) {
+    const ClosedArgs<ACC> A(2.0 * argpq_d, 4.0 * argpq_d * argpq_d);
+    const float argpq = (float)argpq_d, zr = (float)zr_d;
     const float a3 = argpq * argpq * argpq;
     const float pqr1 = (1.0f / (zr * (zr - 1) * (zr - 2))) / a3;
-    float e2, e3;
-    const float th2 = (zr - 2) * t, th3 = (zr - 3) * t;
-    const float P2 = powp1f_e(x2, (zr - 2) / 2.0f, e2), P3 = powp1f_e(x2, (zr - 3) / 2.0f, e3);
+    float e2, e3, g2, g3;
+    const float th2 = A.angle(zr_d - 2, g2), th3 = A.angle(zr_d - 3, g3);
+    const float P2 = A.power((zr_d - 2) / 2.0, e2), P3 = A.power((zr_d - 3) / 2.0, e3);
     const float S2 = sinf(th2), C3 = cosf(th3);
     const float pqr2 = pqr1 * S2 / P2;
     const float b3 = (1.0f / (zr * (zr - 1) * (zr - 2) * (zr - 3))) / (a3 * argpq);
     const float pqr3 = b3 * C3 / P3;
     const float v = (4.0f / (float)M_PI) * (pqr1 - pqr2 - (9.0f / 8.0f) * pqr3);
-    const float E = 3e-7f * fabsf(pqr1) + fabsf(pqr1) * (TRIG_ERR(th2) + fabsf(S2) * e2) / P2 + 3e-7f * fabsf(pqr2) +
-                    1.125f * (fabsf(b3) * (TRIG_ERR(th3) + fabsf(C3) * e3) / P3 + 3e-7f * fabsf(pqr3));
+    const float E = 3e-7f * fabsf(pqr1) + fabsf(pqr1) * (g2 + fabsf(S2) * e2) / P2 + 3e-7f * fabsf(pqr2) +
+                    1.125f * (fabsf(b3) * (g3 + fabsf(C3) * e3) / P3 + 3e-7f * fabsf(pqr3));
     rel = (4.0f / (float)M_PI) * E / fabsf(v) + 3e-7f;
     return v;
+}
+
+// The same in FP64 for lattice pixels (there the FP32 form's ~1e-6 is
+// amplified where the structure factor cancels): one atan, one log1p, two
+// exps, a sine and a cosine. Its own error is that of a few FP64 roundings per
+// term, relative to the sum.
+__device__ double cyl_pqr_asym_d(double argpq, double zr, float &rel) {
+    const double t = atan(2.0 * argpq), L = log1p(4.0 * argpq * argpq);
+    const double a3 = argpq * argpq * argpq;
+    const double pqr1 = (1.0 / (zr * (zr - 1) * (zr - 2))) / a3;
+    const double pqr2 = pqr1 * sin((zr - 2) * t) / exp((zr - 2) / 2.0 * L);
+    const double b3 = (1.0 / (zr * (zr - 1) * (zr - 2) * (zr - 3))) / (a3 * argpq);
+    const double pqr3 = b3 * cos((zr - 3) * t) / exp((zr - 3) / 2.0 * L);
+    const double v = (4.0 / M_PI) * (pqr1 - pqr2 - (9.0 / 8.0) * pqr3);
+    rel = (float)((fabs(pqr1) + fabs(pqr2) + fabs(pqr3)) * 1e-13 / fabs(v) + 1e-15);
+    return v;
+}
+
+// cylinder cross-section F(q), q >= limq4f (Source/sc_lib_formfq_partCylinder.h)
+// amplitude squared; gamma ratios from the preparation
+template <bool ACC>
+__device__ float cyl_fqr_asym(double a_d, double z_d, double g0, double g1, float &rel) {
+    const ClosedArgs<ACC> A(a_d, a_d * a_d);
+    const float a = (float)a_d;
+    const float a2 = a * a;
+    float e1, e2, h1, h2;
+    const float s1 = A.angle(z_d - 0.5, h1), s2 = A.angle(z_d - 1.5, h2);
+    const float P1 = A.power((z_d - 0.5) / 2.0, e1), P2 = A.power((z_d - 1.5) / 2.0, e2);
+    const float b1 = (float)g0 * rsqrtf(a2 * a), b2 = (float)g1 * rsqrtf(a2 * a2 * a);
+    const float T1 = sinf(s1) - cosf(s1), T2 = sinf(s2) + cosf(s2);
+    const float pqr1 = b1 * T1 / P1;
+    const float pqr2 = b2 * T2 / P2;
+    const float pqr3 = (2.0f / sqrtf((float)M_PI)) * (pqr1 + (9.0f / 16.0f) * pqr2);
+    // amplitude error (two trig terms each), doubled for the square
+    const float E = fabsf(b1) * (2.0f * h1 + fabsf(T1) * e1) / P1 + 3e-7f * fabsf(pqr1) +
+                    0.5625f * (fabsf(b2) * (2.0f * h2 + fabsf(T2) * e2) / P2 + 3e-7f * fabsf(pqr2));
+    rel = 2.0f * (2.0f / sqrtf((float)M_PI)) * E / fabsf(pqr3) + 3e-7f;
+    return pqr3;
 }
 
 // Length factor of the Schulz cylinder P(q) along its axis,
 //   (1/(2z(z-1) a^2)) (1 - cos((z-1) atan 2a) / (1+4a^2)^((z-1)/2)),
 // which tends to 1 for a -> 0 with cancellation in the bracket. With m = z-1
 // the bracket is 1 - Re (1+2ia)^(-m) = -sum_{j>=1} C(m+2j-1, 2j) (-4a^2)^j, so
-// for small m*a the function is the series 1 - (m+3)(m+2)/3 a^2 + ... obtained
-// from the term ratio below; otherwise the closed form is used.
+// the function is the series 1 + sum_{j>=1} T_j with
+//   T_j / T_(j-1) = -4a^2 (m+2j)(m+2j+1)/((2j+1)(2j+2)),
+// whose ratios lie between the first one, 4a^2 (m+2)(m+3)/12, and their limit
+// 4a^2. Where both are below 0.12, ten terms leave a remainder below 1e-9 and
+// S = sum T_j (|S| < 0.14, largest terms first) then 1 + S round to < 1.2e-7;
+// elsewhere the closed form is used.
+__device__ __forceinline__ bool len_series_ok(float a, float m) {
+    const float x = 4.0f * a * a;
+    return x < 0.12f && x * (m + 2.0f) * (m + 3.0f) < 1.44f;
+}
+
+__device__ __forceinline__ float len_series(float a, float m) {
+    const float x = -4.0f * a * a;
+    float term = 1.0f, sum = 0.0f;
+#pragma unroll
+    for (int j = 1; j <= 10; j++) {
+        term *= x * (m + 2 * j) * (m + 2 * j + 1) * (1.0f / ((2 * j + 1) * (2 * j + 2)));
+        sum += term;
+    }
+    return 1.0f + sum;
+}
+
 __device__ float cyl_len_factor(float a, float z) {
     const float m = z - 1.0f;
-    if (fabsf(m * a) < 0.35f) {
-        // P = sum_j T_j with T_0 = 1, T_j/T_(j-1) = -4a^2 (m+2j)(m+2j+1)/((2j+1)(2j+2))
-        const float x = -4.0f * a * a;
-        float term = 1.0f, sum = 1.0f;
-#pragma unroll
-        for (int j = 1; j <= 9; j++) {
-            term *= x * (m + 2 * j) * (m + 2 * j + 1) * (1.0f / ((2 * j + 1) * (2 * j + 2)));
-            sum += term;
-        }
-        return sum;
-    }
+    if (len_series_ok(a, m)) return len_series(a, m);
     const float a1 = 1.0f / (2.0f * z * m);
     return (a1 / (a * a)) * (1.0f - cosf(m * atanf(2.0f * a)) / powp1f(4.0f * a * a, m / 2.0f));
 }
 
 // the same with a relative error estimate (see the asymptotes above)
-__device__ float cyl_len_factor_e(float a, float z, float &rel) {
+template <bool ACC>
+__device__ float cyl_len_factor_e(double a_d, double z_d, float &rel) {
+    const float a = (float)a_d, z = (float)z_d;
     const float m = z - 1.0f;
-    if (fabsf(m * a) < 0.35f) {
-        rel = 1e-6f;  // alternating series of quickly falling terms
-        return cyl_len_factor(a, z);
+    if (len_series_ok(a, m)) {
+        rel = 1.5e-7f;
+        return len_series(a, m);
     }
+    const ClosedArgs<ACC> A(2.0 * a_d, 4.0 * a_d * a_d);
     const float a1 = 1.0f / (2.0f * z * m);
-    float ep;
-    const float th = m * atanf(2.0f * a);
-    const float P = powp1f_e(4.0f * a * a, m / 2.0f, ep);
+    float ep, g;
+    const float th = A.angle(z_d - 1.0, g);
+    const float P = A.power((z_d - 1.0) / 2.0, ep);
     const float C = cosf(th);
     const float br = 1.0f - C / P;
-    rel = ((TRIG_ERR(th) + fabsf(C) * ep) / P) / fabsf(br) + 3e-7f;
+    rel = ((g + fabsf(C) * ep) / P) / fabsf(br) + 3e-7f;
     return (a1 / (a * a)) * br;
 }
 
@@ -214,11 +306,12 @@ struct ChiArgsF {
     int i1;
 };
 
-// Where |m*a| < 1e-3 (m = z-1) the reference's closed form of the length
-// factor, 1 - cos(m atan 2a)/(1+4a^2)^(m/2) in FP64, cancels to below ~1e-8
-// relative accuracy: its value there is rounding noise that the FP64 drop-in
-// reproduces and this FP32 series form does not. Such a node flags the pixel
-// for the FP64 redo.
+// Where m*a is small (m = z-1) the reference's closed form of the length
+// factor, 1 - cos(m atan 2a)/(1+4a^2)^(m/2) in FP64, cancels: its bracket is
+// ~2 (m a)^2 while its rounding is a few 1e-16, a relative noise of up to
+// ~5e-16/(m a)^2 that the FP64 drop-in reproduces and this FP32 series form does
+// not. Below |m a| = 1e-4 (noise above ~5e-8) a node flags the pixel for the
+// FP64 redo; above it the two agree to FP32 accuracy.
 __device__ __forceinline__ float chi_integrand_f(const ChiArgsF &A, float cx, float sx, float cd, float sd,
                                                  bool &guard) {
     const float eps = 1e-10f;
@@ -236,7 +329,7 @@ __device__ __forceinline__ float chi_integrand_f(const ChiArgsF &A, float cx, fl
     default: return 0.0f;
     }
     const float a = s * A.lz;
-    if (fabsf((A.z - 1.0f) * a) < 1e-3f) guard = true;
+    if (fabsf((A.z - 1.0f) * a) < 1e-4f) guard = true;
     return cyl_len_factor(a, A.z);
 }
 
@@ -426,12 +519,47 @@ __device__ __forceinline__ int lower_bound_f(const float *__restrict__ a, int n,
     return lo;
 }
 
-// Error estimates of the sums: a term exp2f(x) carries the relative error of
-// its argument's FP32 rounding, ~|x| 2^-23 ln 2, plus exp2f's own; the sums'
-// relative errors are the term-weighted means of those (eps_rad, eps_int).
+// Float-pair helpers of the peak sums (this unit is compiled without
+// contraction, so the error terms below are exact where stated).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// k d^2 as a float pair (xh + xl) from k = kh + kl and d = dh + dl
+__device__ __forceinline__ void scaled_square(float kh, float kl, float dh, float dl, float &xh, float &xl) {
+    const float p = dh * dh;
+    const float pe = fmaf(dh, dh, -p) + 2.0f * dh * dl;
+    xh = kh * p;
+    xl = fmaf(kh, p, -xh) + fmaf(kh, pe, kl * p);
+}
+
+// exp2(-(xh + xl)): exp2f of the high part, first-order factor for the low one
+__device__ __forceinline__ float exp2_pair(float xh, float xl) { return exp2f(-xh) * fmaf(-xl, 0.6931472f, 1.0f); }
+
+// yphi = acos(1 - s) = 2 asin(sqrt(s/2)) and yphi^2 = 2 s (1 + r(s)) with
+// r(s) = sum_{n>=2} 2^n s^(n-1) / (n^2 C(2n, n)) (the series of asin^2); through
+// n = 17 the remainder is below 1e-12 for s < 1/2 (yphi < 60 degrees)
+__device__ __forceinline__ float asin2_rest(float s) {
+    const float c[16] = {1.666666667e-01f, 4.444444444e-02f, 1.428571429e-02f, 5.079365079e-03f,
+                         1.924001924e-03f, 7.611436183e-04f, 3.108003108e-04f, 1.300079731e-04f,
+                         5.542445171e-05f, 2.399326914e-05f, 1.051878828e-05f, 4.660632346e-06f,
+                         2.083721869e-06f, 9.388723824e-07f, 4.258997702e-07f, 1.943499843e-07f};
+    float r = c[15];
+#pragma unroll
+    for (int n = 14; n >= 0; n--) r = fmaf(r, s, c[n]);
+    return r * s;
+}
+
+// Error estimates of the sums: a term carries exp2f's error and the rounding
+// of its factors (c0), and the error of its angular argument (ephi); the
+// radial argument k (q - q_hkl)^2 is a float pair, exact to ~1e-12 of its
+// size. The sums' relative errors are the term-weighted means (eps_rad,
+// eps_int).
 __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, double qy, double qz, double q,
                             double &radint, double &intens, double &eps_rad, double &eps_int, bool &guard) {
-    const float c0 = 2.4e-7f, c1 = 8.3e-8f;
+    const float c0 = 3e-7f;
     double width = 1;
     if (P.debyescherrer) width = 4.0 / P.domainsize;
     if (P.para) width = (4.0 / P.domainsize) + cs64::sqr(P.reldis) * P.dist * cs64::sqr(q);
@@ -441,19 +569,23 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
     const float ql = (float)(q - (double)qf);
     // isotropic peaks: exp(-4 x2/pi) / (pi widthiso/2), x2 = (q-qhkl)^2/widthiso^2
     {
-        const float k = (float)(4.0 / M_PI / (widthiso * widthiso) * 1.4426950408889634);
+        const double kd = 4.0 / M_PI / (widthiso * widthiso) * 1.4426950408889634;
+        const float kh = (float)kd, kl = (float)(kd - (double)kh);
         const float dmax = (float)(9.4 * widthiso);
         int i = lower_bound_f(T.iq, T.n_iso, qf - dmax);
         Kahan s;
         float w = 0.0f;
         for (; i < T.n_iso; i++) {
             const float qh = __ldg(T.iq + i);
-            const float d = (qf - qh) + ql;
-            if (d < -dmax) break;
-            const float x = k * d * d;
-            const float t = exp2f(-x) * __ldg(T.imf + i);
+            float dh, de;
+            two_sum(qf, -qh, dh, de);
+            const float dl = de + ql;
+            if (dh + dl < -dmax) break;
+            float xh, xl;
+            scaled_square(kh, kl, dh, dl, xh, xl);
+            const float t = exp2_pair(xh, xl) * __ldg(T.imf + i);
             s.add(t);
-            w = fmaf(fabsf(t), fmaf(c1, x, c0), w);
+            w = fmaf(fabsf(t), c0, w);
         }
         const double sum = s.value();
         radint = sum / (M_PI * widthiso / 2.0);
@@ -461,40 +593,90 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
     }
     // anisotropic peaks
     {
-        const float k = (float)(4.0 / M_PI / (width * width) * 1.4426950408889634);
+        const double kd = 4.0 / M_PI / (width * width) * 1.4426950408889634;
+        const float kh = (float)kd, kl = (float)(kd - (double)kh);
         const float dmax = (float)(9.4 * width);
-        const float kphi = (float)(4 * q * q / (M_PI * cs64::sqr(P.phiwidth)) * 1.4426950408889634);
-        const float invq = (float)(1.0 / q);
-        const float cphi = kphi * 1.7e-7f;
-        const float fx = (float)qx * invq, fy = (float)qy * invq, fz = (float)qz * invq;
+        const double kphid = 4 * q * q / (M_PI * cs64::sqr(P.phiwidth)) * 1.4426950408889634;
+        const float kph = (float)kphid, kpl = (float)(kphid - (double)kph);
+        // unit q as a float pair; eps = 1 - |q|/q of the reference's cosine
+        // (its q carries CS_EPS9)
+        const double rn = 1.0 / (q - CS_EPS9);
+        const double uxd = qx * rn, uyd = qy * rn, uzd = qz * rn;
+        const float fx = (float)uxd, fy = (float)uyd, fz = (float)uzd;
+        const float lx = (float)(uxd - fx), ly = (float)(uyd - fy), lz = (float)(uzd - fz);
+        const float epsq = (float)(CS_EPS9 / q);
         int i = lower_bound_f(T.aq, T.n_aniso, qf - dmax);
         Kahan s;
         float w = 0.0f;
         for (; i < T.n_aniso; i++) {
             const float qh = __ldg(T.aq + i);
-            const float d = (qf - qh) + ql;
-            if (d < -dmax) break;
-            const float4 v = __ldg(T.av + i);  // unit q_hkl (x,y,z) and g3/peaknorm1
+            float dh, de;
+            two_sum(qf, -qh, dh, de);
+            const float dl = de + ql;
+            if (dh + dl < -dmax) break;
+            const float4 v = __ldg(T.av + 2 * i);       // unit q_hkl (x, y, z), mult * g3/peaknorm1
+            const float4 vl = __ldg(T.av + 2 * i + 1);  // low parts, 1 - |h|/q_hkl
             const float c = fmaf(fx, v.x, fmaf(fy, v.y, fz * v.z));
             // myacos: the reference maps c < -1 to 0 and c > 1 to pi. For q
             // (anti)parallel to q_hkl the FP64 rounding of the reference's
             // cosine decides between those and acos(c) ~ 0, a jump of the
             // Gaussian; there the cosine is taken as the reference computes it.
-            float yphi;
+            // Up to 90 degrees the angle comes from 1 - c_ref = eh + (1 - eh)
+            // |u - h|^2/2 (eh: the reference's norms), free of acos's
+            // cancellation near 1; below 1 - c_ref = 0.05 (18 degrees) yphi^2
+            // itself comes from the series of 4 asin^2(sqrt(s/2)) with |u - h|^2
+            // as a float pair. Beyond 90 degrees acos(c) is used, off by
+            // ~2e-7/sin(yphi).
+            float xph, xpl = 0.0f, ephi;  // angular argument kphi yphi^2 (pair) and its error
             if (fabsf(c) > 1.0f - 1e-5f) {
                 const int ii = __ldg(T.aidx + i);
                 const double cd = (qx * (double)P.latpar3[ii][2] + qy * (double)P.latpar3[ii][3] +
                                    qz * (double)P.latpar3[ii][4]) /
                                   (q * (double)P.latpar3[ii][5]);
-                yphi = (float)((cd < -1) ? 0.0 : ((cd > 1) ? M_PI : acos(cd)));
+                const float yphi = (float)((cd < -1) ? 0.0 : ((cd > 1) ? M_PI : acos(cd)));
+                xph = kph * yphi * yphi;
+                ephi = 2e-7f * xph;
+            } else if (c > 0.0f) {
+                // u - h as float pairs (the high differences are not always
+                // exact: components near zero may differ in sign)
+                float dxh, dxe, dyh, dye, dzh, dze;
+                two_sum(fx, -v.x, dxh, dxe);
+                two_sum(fy, -v.y, dyh, dye);
+                two_sum(fz, -v.z, dzh, dze);
+                const float dxl = dxe + (lx - vl.x), dyl = dye + (ly - vl.y), dzl = dze + (lz - vl.z);
+                const float px = dxh * dxh, py = dyh * dyh, pz = dzh * dzh;
+                const float pe = fmaf(dxh, dxh, -px) + fmaf(dyh, dyh, -py) + fmaf(dzh, dzh, -pz) +
+                                 2.0f * fmaf(dxh, dxl, fmaf(dyh, dyl, dzh * dzl));
+                float s1, e1, ddh, e2;
+                two_sum(px, py, s1, e1);
+                two_sum(s1, pz, ddh, e2);
+                const float ddl = e1 + e2 + pe;
+                const float eh = epsq + vl.w;
+                const float shh = 0.5f * ddh;  // exact
+                const float shl = fmaf(0.5f, ddl, eh * (1.0f - shh));
+                const float sh = shh + shl;
+                if (sh < 0.5f) {
+                    // kphi yphi^2 = 2 kphi s (1 + r): 2 kphi s as a pair, r small
+                    const float ah = (2.0f * kph) * shh;
+                    const float al = fmaf(2.0f * kph, shh, -ah) + 2.0f * fmaf(kph, shl, kpl * shh);
+                    two_sum(ah, fmaf(ah, asin2_rest(sh), al), xph, xpl);
+                    ephi = 1e-8f * xph;
+                } else {
+                    const float yphi = 2.0f * asinf(sqrtf(0.5f * sh));
+                    xph = kph * yphi * yphi;
+                    ephi = 6e-7f * xph;
+                }
             } else {
-                yphi = acosf(c);
+                const float yphi = acosf(c);
+                xph = kph * yphi * yphi;
+                ephi = 2.1e-7f * kph * yphi / sqrtf(fmaxf(1.0f - c * c, 1e-10f));
             }
-            const float x = fmaf(k * d, d, kphi * yphi * yphi);
-            const float t = exp2f(-x) * v.w * __ldg(T.amf + i);
+            float xh, xl, sx, ex;
+            scaled_square(kh, kl, dh, dl, xh, xl);
+            two_sum(xh, xph, sx, ex);
+            const float t = exp2_pair(sx, ex + xl + xpl) * v.w;
             s.add(t);
-            // + the angle: the FP32 cosine's rounding (~6e-8) moves yphi^2 by ~1.2e-7
-            w = fmaf(fabsf(t), fmaf(c1, x, c0 + cphi), w);
+            w = fmaf(fabsf(t), c0 + ephi, w);
         }
         const double sum = s.value();
         intens = sum / (M_PI * width / 2.0);
@@ -510,6 +692,7 @@ __device__ __forceinline__ double zr_asym(const cs_prepared &P) {
     return zr;
 }
 
+template <bool LAT>
 __device__ double sphere_pq_mixed(const cs_prepared &P, double q, bool &guard, double &err) {
     if (P.cs != 0) {
         guard = true;
@@ -523,11 +706,14 @@ __device__ double sphere_pq_mixed(const cs_prepared &P, double q, bool &guard, d
     }
     const double zr = zr_asym(P);
     float rel;
-    const float v = sphere_pq_asym((float)(q * P.radius / (zr + 1)), (float)zr, rel);
+    const double argq = q * P.radius / (zr + 1);
+    float v = sphere_pq_asym<false>(argq, zr, rel);
+    if (!(rel <= acc_switch<LAT>())) v = sphere_pq_asym<true>(argq, zr, rel);
     err = rel;
     return v;
 }
 
+template <bool LAT>
 __device__ double sphere_fq_mixed(const cs_prepared &P, double q, bool &guard, double &err) {
     const double thr = 0.4 * P.limqf[4];
     if (near(q, thr, 1e-12)) guard = true;
@@ -537,12 +723,15 @@ __device__ double sphere_fq_mixed(const cs_prepared &P, double q, bool &guard, d
     }
     const double zr = (1 - cs64::sqr(P.sigma)) / cs64::sqr(P.sigma);
     float rel;
-    const float v = sphere_fq_asym((float)(q * P.radius / (zr + 1)), (float)zr, rel);
+    const double argq = q * P.radius / (zr + 1);
+    float v = sphere_fq_asym<false>(argq, zr, rel);
+    if (!(rel <= acc_switch<LAT>())) v = sphere_fq_asym<true>(argq, zr, rel);
     err = rel;
     return v;
 }
 
 // formpq_partCylinder, ordis 0 and 6, cs 0 (mixed)
+template <bool LAT>
 __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, bool &guard, double &err) {
     const cs_prepared &P = *C.P;
     if (P.cs != 0) {
@@ -560,13 +749,16 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             pql = cs64::series_zdir(P.carrp[0], qxs, qys);
         } else {
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-            if (fabs((zl - 1) * arglq) < 1e-3) {
-                // the reference's closed form cancels to rounding noise here
-                // (see chi_integrand_f); evaluated as the drop-in does
+            if (LAT || fabs((zl - 1) * arglq) < 1e-3) {
+                // the reference's closed form cancels to rounding noise for
+                // small |m a| (see chi_integrand_f), and lattice pixels need the
+                // length factor beyond FP32 accuracy where the structure factor
+                // cancels: evaluated as the drop-in does (same value)
                 pql = cs64::len_factor_ref(arglq, zl);
             } else {
                 float rel;
-                pql = cyl_len_factor_e((float)arglq, (float)zl, rel);
+                pql = cyl_len_factor_e<false>(arglq, zl, rel);
+                if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
                 el = rel;
             }
         }
@@ -611,7 +803,14 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             pqr = cs64::series_q(P.carrp[3], q, 120);
         else {
             float rel;
-            pqr = cyl_pqr_asym((float)(q * P.radius / (zr + 1)), (float)zr, rel);
+            const double argpq = q * P.radius / (zr + 1);
+            if (LAT) {
+                pqr = cyl_pqr_asym_d(argpq, zr, rel);
+            } else {
+                pqr = cyl_pqr_asym<false>(argpq, zr, rel);
+                // (a zero length factor makes the product zero: no need to refine)
+                if (!(rel <= acc_switch<LAT>()) && pql != 0.0) pqr = cyl_pqr_asym<true>(argpq, zr, rel);
+            }
             er = rel;
         }
     }
@@ -621,6 +820,7 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
 
 
 // formfq_partCylinder, ordis 0 and 6, cs 0 (mixed)
+template <bool LAT>
 __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qys, double q, bool &guard,
                              double &err) {
     const cs_prepared &P = *C.P;
@@ -639,13 +839,16 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             pql = cs64::series_zdir(P.carrf[0], qxs, qys);
         } else {
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-            if (fabs((zl - 1) * arglq) < 1e-3) {
-                // the reference's closed form cancels to rounding noise here
-                // (see chi_integrand_f); evaluated as the drop-in does
+            if (LAT || fabs((zl - 1) * arglq) < 1e-3) {
+                // the reference's closed form cancels to rounding noise for
+                // small |m a| (see chi_integrand_f), and lattice pixels need the
+                // length factor beyond FP32 accuracy where the structure factor
+                // cancels: evaluated as the drop-in does (same value)
                 pql = cs64::len_factor_ref(arglq, zl);
             } else {
                 float rel;
-                pql = cyl_len_factor_e((float)arglq, (float)zl, rel);
+                pql = cyl_len_factor_e<false>(arglq, zl, rel);
+                if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
                 el = rel;
             }
         }
@@ -686,23 +889,12 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
     if (q < thr) {
         pqr = cs64::series_q(P.carrf[3], q, 120);
     } else {
-        const float a = (float)(q * P.radius / (zr + 1));
-        const float z = (float)zr;
-        const float t = atanf(a);
-        const float a2 = a * a;
-        const float s1 = (z - 0.5f) * t, s2 = (z - 1.5f) * t;
-        float e1, e2;
-        const float P1 = powp1f_e(a2, (z - 0.5f) / 2.0f, e1), P2 = powp1f_e(a2, (z - 1.5f) / 2.0f, e2);
-        const float b1 = (float)P.gamma_ratio[0] * rsqrtf(a2 * a), b2 = (float)P.gamma_ratio[1] * rsqrtf(a2 * a2 * a);
-        const float T1 = sinf(s1) - cosf(s1), T2 = sinf(s2) + cosf(s2);
-        const float pqr1 = b1 * T1 / P1;
-        const float pqr2 = b2 * T2 / P2;
-        const float pqr3 = (2.0f / sqrtf((float)M_PI)) * (pqr1 + (9.0f / 16.0f) * pqr2);
-        pqr = (double)pqr3 * (double)pqr3;
-        // amplitude error (two trig terms each), doubled for the square
-        const float E = fabsf(b1) * (2.0f * TRIG_ERR(s1) + fabsf(T1) * e1) / P1 + 3e-7f * fabsf(pqr1) +
-                        0.5625f * (fabsf(b2) * (2.0f * TRIG_ERR(s2) + fabsf(T2) * e2) / P2 + 3e-7f * fabsf(pqr2));
-        er = 2.0f * (2.0f / sqrtf((float)M_PI)) * E / fabsf(pqr3) + 3e-7f;
+        const double a = q * P.radius / (zr + 1);
+        float rel;
+        float amp = cyl_fqr_asym<false>(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
+        if (!(rel <= acc_switch<LAT>())) amp = cyl_fqr_asym<true>(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
+        pqr = (double)amp * (double)amp;
+        er = rel;
     }
     err = el + er;
     return pql * pqr;
@@ -723,10 +915,11 @@ __device__ __forceinline__ double lattice_combine(const cs_prepared &P, double q
                                                   double eps_rad, double eps_int, double tailv, bool &guard) {
     const double v = P.latpar[1] * P.latpar[2];
     const double r2 = 8 * M_PI * M_PI * M_PI * radint / (4 * M_PI * v);
-    // Debye-Waller factors in FP32: relative error <= |arg| 2^-23 + 2^-22
-    const float a2 = (float)(-P.ucb * q * q), a1 = (float)(-P.dwfactor * q * q);
-    const double e2 = expf(a2), e1 = expf(a1);
-    const double ee2 = fabsf(a2) * 1.2e-7f + 2.4e-7f, ee1 = fabsf(a1) * 1.2e-7f + 2.4e-7f;
+    // Debye-Waller factors in FP64 (two exps per pixel): in FP32 the rounding
+    // of the argument alone moves them by |arg| 6e-8, which dominated the
+    // error estimate of pixels where szq cancels
+    const double e2 = exp(-P.ucb * q * q), e1 = exp(-P.dwfactor * q * q);
+    const double ee2 = 4e-16, ee1 = 4e-16;
     const double szqiso = 1 + (r2 - 1) * e2;
     const double r1 = 2 * M_PI * intens / v;
     const double ratio = fq / pq;
@@ -750,12 +943,13 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
     const double tailv = P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
     double ep = 0, ef = 0;  // relative error estimates of pq and fq
     if (KEY == CS_KEY_SPHERE_NONE_ISO) {
-        const double pq = sphere_pq_mixed(P, q, guard, ep);
+        const double pq = sphere_pq_mixed<false>(P, q, guard, ep);
+        if (!(ep <= 5e-6)) guard = true;
         return P.base + P.izero * (pq + P.iso * pq) + tailv;
     }
     if (KEY == CS_KEY_SPHERE_GAUSS_FCC_GAUSS) {
-        const double pq = sphere_pq_mixed(P, q, guard, ep);
-        const double fq = sphere_fq_mixed(P, q, guard, ef);
+        const double pq = sphere_pq_mixed<true>(P, q, guard, ep);
+        const double fq = sphere_fq_mixed<true>(P, q, guard, ef);
         double radint, intens, erad, eint;
         peak_sums_f(P, T, qx, qy, qz, q, radint, intens, erad, eint, guard);
         return lattice_combine(P, q, pq, ep, fq, ef, pq, ep, radint, intens, erad, eint, tailv, guard);
@@ -763,40 +957,42 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
     if (KEY == CS_KEY_CYL_NONE_GAUSS) {
         double pq;
         if (P.orcase == CS_ORC_GENERAL)
-            pq = cyl_pq_mixed(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q, guard, ep);
+            pq = cyl_pq_mixed<false>(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q, guard, ep);
         else
-            pq = cyl_pq_mixed(C, qx, qy, q, guard, ep);
+            pq = cyl_pq_mixed<false>(C, qx, qy, q, guard, ep);
+        if (!(ep <= 5e-6)) guard = true;
         return P.base + P.izero * (pq + P.iso) + tailv;
     }
     if (KEY == CS_KEY_CYL_NONE_ZDIR) {
         double pq;
         switch (P.orcase) {
-        case CS_ORC_GENERAL: pq = cyl_pq_mixed(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard, ep); break;
-        case CS_ORC_XAXIS: pq = cyl_pq_mixed(C, qx, 0, q, guard, ep); break;
-        case CS_ORC_YAXIS: pq = cyl_pq_mixed(C, 0, qy, q, guard, ep); break;
-        default: pq = cyl_pq_mixed(C, qx, qy, q, guard, ep); break;
+        case CS_ORC_GENERAL: pq = cyl_pq_mixed<false>(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard, ep); break;
+        case CS_ORC_XAXIS: pq = cyl_pq_mixed<false>(C, qx, 0, q, guard, ep); break;
+        case CS_ORC_YAXIS: pq = cyl_pq_mixed<false>(C, 0, qy, q, guard, ep); break;
+        default: pq = cyl_pq_mixed<false>(C, qx, qy, q, guard, ep); break;
         }
+        if (!(ep <= 5e-6)) guard = true;
         return P.base + P.izero * (pq + P.iso) + tailv;
     }
     if (KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR) {
         double pq = 0, fq = 0;
         switch (P.orcase) {
         case CS_ORC_GENERAL:
-            pq = cyl_pq_mixed(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard, ep);
-            fq = cyl_fq_mixed(C, sqrt(P.cosphi * qx * qx + P.sinphi * qy * qy + CS_EPS9), qx * P.cosphi * P.sintheta,
+            pq = cyl_pq_mixed<true>(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard, ep);
+            fq = cyl_fq_mixed<true>(C, sqrt(P.cosphi * qx * qx + P.sinphi * qy * qy + CS_EPS9), qx * P.cosphi * P.sintheta,
                               qy * P.sinphi * P.sintheta, q, guard, ef);
             break;
         case CS_ORC_XAXIS:
-            pq = cyl_pq_mixed(C, qx, 0, q, guard, ep);
-            fq = cyl_fq_mixed(C, fabs(qx), qx, 0, q, guard, ef);
+            pq = cyl_pq_mixed<true>(C, qx, 0, q, guard, ep);
+            fq = cyl_fq_mixed<true>(C, fabs(qx), qx, 0, q, guard, ef);
             break;
         case CS_ORC_YAXIS:
-            pq = cyl_pq_mixed(C, 0, qy, q, guard, ep);
-            fq = cyl_fq_mixed(C, fabs(qy), 0, qy, q, guard, ef);
+            pq = cyl_pq_mixed<true>(C, 0, qy, q, guard, ep);
+            fq = cyl_fq_mixed<true>(C, fabs(qy), 0, qy, q, guard, ef);
             break;
         default:
-            pq = cyl_pq_mixed(C, qx, qy, q, guard, ep);
-            fq = cyl_fq_mixed(C, q, qx, qy, q, guard, ef);
+            pq = cyl_pq_mixed<true>(C, qx, qy, q, guard, ep);
+            fq = cyl_fq_mixed<true>(C, q, qx, qy, q, guard, ef);
             break;
         }
         double radint, intens, erad, eint;
@@ -872,7 +1068,7 @@ namespace cs {
 // Compact, sorted reflection tables from the prepared block (see PeakTab).
 void build_peak_tables(const cs_prepared &P, HostPeaks &H) {
     H.aq.clear(); H.amf.clear(); H.av.clear(); H.iq.clear(); H.imf.clear(); H.aidx.clear();
-    struct A { float q; float4 v; float mf; int idx; };
+    struct A { float q; float4 v, vl; float mf; int idx; };
     std::vector<A> an;
     for (int ii = 1; ii <= P.peakmax2 && ii < CS_LATPARLEN; ii++) {
         const float qh = P.latpar3[ii][5];
@@ -881,8 +1077,15 @@ void build_peak_tables(const cs_prepared &P, HostPeaks &H) {
         const double q = qh;
         A a;
         a.q = qh;
-        a.v = make_float4((float)(P.latpar3[ii][2] / q), (float)(P.latpar3[ii][3] / q), (float)(P.latpar3[ii][4] / q),
-                          (float)((double)P.latpar3[ii][10] / (double)P.latpar3[ii][11]));
+        // unit vector of q_hkl as a float pair, and 1 - |h|/q_hkl (the stored
+        // components and magnitude are rounded separately)
+        const double hx = P.latpar3[ii][2], hy = P.latpar3[ii][3], hz = P.latpar3[ii][4];
+        const double hn = std::sqrt(hx * hx + hy * hy + hz * hz);
+        const double ux = hx / hn, uy = hy / hn, uz = hz / hn;
+        a.v = make_float4((float)ux, (float)uy, (float)uz,
+                          (float)((double)P.latpar3[ii][10] / (double)P.latpar3[ii][11] * (double)mf));
+        a.vl = make_float4((float)(ux - (double)(float)ux), (float)(uy - (double)(float)uy), (float)(uz - (double)(float)uz),
+                           (float)(1.0 - hn / q));
         a.mf = (float)mf;
         a.idx = ii;
         an.push_back(a);
@@ -891,6 +1094,7 @@ void build_peak_tables(const cs_prepared &P, HostPeaks &H) {
     for (auto &a : an) {
         H.aq.push_back(a.q);
         H.av.push_back(a.v);
+        H.av.push_back(a.vl);
         H.amf.push_back(a.mf);
         H.aidx.push_back(a.idx);
     }

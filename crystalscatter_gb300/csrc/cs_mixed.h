@@ -16,8 +16,9 @@ namespace csm {
 struct PeakTab {
     int n_aniso = 0;
     const float *aq = nullptr;   // q_hkl
-    const float4 *av = nullptr;  // unit q_hkl vector (x, y, z), g3/peaknorm1
-    const float *amf = nullptr;  // multiplicity * structure factor
+    const float4 *av = nullptr;  // per reflection two entries: unit q_hkl (x, y, z), mult * g3/peaknorm1;
+                                 // low parts of the unit vector, 1 - |h|/q_hkl
+    const float *amf = nullptr;  // multiplicity * structure factor (also folded into av[2i].w)
     const int *aidx = nullptr;   // row of the reflection in latpar2/latpar3
     int n_iso = 0;
     const float *iq = nullptr;

@@ -95,14 +95,18 @@ class Surrogate:
     def __init__(self, fam, hidden=512, seed=0):
         self.fam = fam
         self.net = cs.SurrogateMLP(len(fam.keys), hidden, 64 * 64, seed=seed)
-        self.mean, self.std = 0.0, 1.0
+        self.mean, self.std = 0.0, 1.0  # per-pixel tensors after training
 
     def train(self, U, Y, epochs=30, batch=512, lr=1e-3, seed=0):
         import torch
-        self.mean = float(Y.mean())
-        self.std = float(Y.std()) or 1.0
+        # per-pixel standardisation: the network learns each q's deviation from
+        # its mean over the family (floor: 5 % of the overall spread)
+        mean = Y.mean(axis=0)
+        std = np.maximum(Y.std(axis=0), 0.05 * float(Y.std()) + 1e-6)
+        self.mean = torch.from_numpy(mean.astype(np.float32)).cuda()
+        self.std = torch.from_numpy(std.astype(np.float32)).cuda()
         x = torch.from_numpy(U).cuda()
-        y = torch.from_numpy((Y - self.mean) / self.std).cuda()
+        y = torch.from_numpy(((Y - mean) / std).astype(np.float32)).cuda()
         n = len(U)
         g = torch.Generator(device="cpu").manual_seed(seed)
         steps = epochs * max(1, n // batch)
