@@ -47,8 +47,8 @@ def parse():
     ap.add_argument("--sweep-sets", type=int, default=4096, help="parameter sets of the batched sweep (0 = skip)")
     ap.add_argument("--sweep-steps", type=int, default=2)
     ap.add_argument("--surrogate", default="", help="surrogate-seeded fits of this family ('2', '2x'); off by default")
-    ap.add_argument("--surrogate-train", type=int, default=20000)
-    ap.add_argument("--surrogate-epochs", type=int, default=30)
+    ap.add_argument("--surrogate-train", type=int, default=32768)
+    ap.add_argument("--surrogate-epochs", type=int, default=200)
     ap.add_argument("--surrogate-targets", type=int, default=8)
     return ap.parse_args()
 

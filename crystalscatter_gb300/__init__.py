@@ -591,6 +591,17 @@ def simplex_fit(base, data, fit_params, stp=0.1, maxit=100, ftol=1e-4, border=0,
     return res, _report(rep)
 
 
+def _torch_stream(stream):
+    """The stream handle for the cs_mlp calls: the caller's, else torch's
+    current stream, so that the network's kernels are ordered after the torch
+    operations that produced their inputs (0 = the legacy default stream, for
+    which the library uses the network's own stream, synchronous with it)."""
+    if stream is not None:
+        return int(stream)
+    import torch
+    return int(torch.cuda.current_stream().cuda_stream)
+
+
 class SurrogateMLP:
     """The surrogate network of the library (cs_mlp_*): n_in -> hidden x3 ->
     n_out with GELU, BF16 tensor-core GEMMs with FP32 accumulation, Adam on
@@ -616,14 +627,16 @@ class SurrogateMLP:
         if rc != CS_OK:
             raise CrystalScatterError(rc, self._lib.cs_mlp_last_error(self._m).decode())
 
-    def forward(self, x, stream=0):
+    def forward(self, x, stream=None):
         import torch
+        stream = _torch_stream(stream)
         x = x.contiguous().float()
         y = torch.empty((x.shape[0], self.n_out), dtype=torch.float32, device=x.device)
         self._check(self._lib.cs_mlp_forward(self._m, x.data_ptr(), x.shape[0], y.data_ptr(), ctypes.c_void_p(stream)))
         return y
 
-    def gradients(self, x, t, stream=0):
+    def gradients(self, x, t, stream=None):
+        stream = _torch_stream(stream)
         loss = ctypes.c_float()
         x = x.contiguous().float()
         t = t.contiguous().float()
@@ -631,7 +644,8 @@ class SurrogateMLP:
                                                ctypes.c_void_p(stream)))
         return loss.value
 
-    def train_step(self, x, t, lr, stream=0, want_loss=True):
+    def train_step(self, x, t, lr, stream=None, want_loss=True):
+        stream = _torch_stream(stream)
         loss = ctypes.c_float()
         self._check(self._lib.cs_mlp_train_step(self._m, x.data_ptr(), t.data_ptr(), x.shape[0], float(lr),
                                                 ctypes.byref(loss) if want_loss else None, ctypes.c_void_p(stream)))
@@ -654,9 +668,10 @@ class SurrogateMLP:
         self._check(self._lib.cs_mlp_set_layer(self._m, l, w.ctypes.data, b.ctypes.data))
 
 
-def upsample_bilinear(x, factor, stream=0):
+def upsample_bilinear(x, factor, stream=None):
     """(n, s, s) CUDA float32 -> (n, s*factor, s*factor), cs_upsample_bilinear"""
     import torch
+    stream = _torch_stream(stream)
     x = x.contiguous().float()
     n, s = x.shape[0], x.shape[1]
     out = torch.empty((n, s * factor, s * factor), dtype=torch.float32, device=x.device)

@@ -217,10 +217,11 @@ int enqueue(cs_batch *b, double *d_out, cudaStream_t s, int mode, int schedule) 
         }
         for (size_t gi = 0; gi < b->groups.size(); gi++) {
             const cs::BatchGroup &g = b->groups[gi];
-            const int per_sm = mode == CS_MODE_MIXED ? cs::batch_blocks_per_sm_mixed(g.key) : cs::batch_blocks_per_sm_fp64(g.key);
+            const bool mixed = mode == CS_MODE_MIXED && cs::mixed_key(g.key);
+            const int per_sm = mixed ? cs::batch_blocks_per_sm_mixed(g.key) : cs::batch_blocks_per_sm_fp64(g.key);
             long grid = (long)b->sm_count * std::max(per_sm, 1);
             grid = std::min(grid, std::max(g.tiles, 1L));
-            int rc = mode == CS_MODE_MIXED
+            int rc = mixed
                          ? cs::launch_batch_mixed(b->dsets, g, (int)gi, b->d_counters + gi, b->d_chi, d_out, b->redo,
                                                   (int)grid, s)
                          : cs::launch_batch_fp64(b->dsets, g, b->d_counters + gi, b->d_chi, d_out, (int)grid, s);
@@ -238,7 +239,7 @@ int enqueue(cs_batch *b, double *d_out, cudaStream_t s, int mode, int schedule) 
             D.d_delta = S.delta;
             double *out = d_out + S.out_offset;
             int rc;
-            if (mode == CS_MODE_MIXED) {
+            if (mode == CS_MODE_MIXED && cs::mixed_key(P.key) && !P.twin) {
                 if (S.npix > b->plain_scratch_cap) {
                     cudaFree(b->plain_scratch.d_list);
                     b->plain_scratch.d_list = nullptr;
@@ -412,7 +413,8 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
         b->offset[k] = off;
         off += (image_doubles(b->hprep[k]) + 31) & ~(size_t)31;
         pix += region_pixels(b->hprep[k]);
-        if (b->hprep[k].twin) b->any_twin = true;
+        // twinned lattices of a key with a mixed kernel (the generic key runs FP64)
+        if (b->hprep[k].twin && cs::mixed_key(b->hprep[k].key)) b->any_twin = true;
         if (b->hprep[k].expand && b->hprep[k].calc_quadrants != CS_RADQ4 && b->hprep[k].calc_quadrants != CS_RAD1D)
             b->expand_sets.push_back(k);
     }

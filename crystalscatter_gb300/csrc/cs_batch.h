@@ -29,6 +29,13 @@ namespace cs {
     M(CS_KEY_CYL_NONE_ZDIR)          \
     M(CS_KEY_CYL_GAUSS_BCT_ZDIR)
 
+// the keys with an FP64 kernel: the above plus the cube and the generic pixel
+// function (which have no mixed-precision kernel; mixed requests run FP64)
+#define CS_FOR_EACH_KEY_FP64(M) \
+    CS_FOR_EACH_KEY(M)          \
+    M(CS_KEY_CUBE_NONE_ISO)     \
+    M(CS_KEY_GENERIC)
+
 // One set as the batch kernels see it (array in device memory).
 struct BatchSetDev {
     const cs_prepared *prep;     // the set's prepared block

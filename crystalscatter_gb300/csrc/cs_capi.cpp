@@ -254,6 +254,11 @@ int run_image(cs_handle *h, double *d_out, cudaStream_t s, int mode) {
     int rc;
     if (mode == CS_MODE_FP64) {
         rc = cs::launch_image(D, *h->hprep, d_out, s);
+    } else if (mode == CS_MODE_MIXED && (!cs::mixed_key(h->hprep->key) || h->hprep->twin)) {
+        // no mixed-precision kernel for this combination: the FP64 kernel
+        // serves the request (no pixel needs a redo)
+        if (h->mscratch.d_count) cudaMemsetAsync(h->mscratch.d_count, 0, sizeof(int), s);
+        rc = cs::launch_image(D, *h->hprep, d_out, s);
     } else if (mode == CS_MODE_MIXED) {
         if ((rc = ensure_mixed(h))) return rc;
         csm::PeakTab T;

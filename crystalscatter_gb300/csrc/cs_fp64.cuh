@@ -705,6 +705,206 @@ __device__ inline double calc_cyl_bct_zdir(const Ctx &C, double qx, double qy, d
     return P.base + P.izero * (szq * pq + P.iso * szqiso * pqiso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
 }
 
+// formpq_partCube, homogeneous isotropic cube (ordis 7, cs 0; the only cube
+// case the preparation supports), Source/sc_lib_formpq_partCube.h:21-62
+__device__ inline double formpq_cube(const cs_prepared &P, double q) {
+    if (q < 1.2 * P.limq[4]) return series_q(P.carrp[3], q, 120);
+    return P.por / (q * q * q * q);
+}
+
+// calc_partCube_lattNone_ordisIsotropic, Source/sc_gpu_pCub_lNon_oIso.h:16-77
+__device__ inline double calc_cube_none_iso(const Ctx &C, double qx, double qy, double qz) {
+    const cs_prepared &P = *C.P;
+    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
+    const double pq = (P.cs == 0) ? formpq_cube(P, q) : 1.0;
+    return P.base + P.izero * (pq + P.iso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+}
+
+// calc_GENERIC, Source/sc_gpu_generic.h:27-881, for the particles the
+// preparation supports (spheres, cylinders with z-direction or Gaussian
+// orientation, homogeneous isotropic cubes), any supported lattice and the
+// peak shapes 1-7 (the reference's shape 7 falls to its `default: return 0`).
+__device__ inline double calc_generic(const Ctx &C, double qx, double qy, double qz) {
+    const cs_prepared &P = *C.P;
+    double pq = 0, fq = 0, intensity, radintensity;
+    const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;  // :33
+    double pqiso = 1;
+    double szqiso = 1, szq = 1;
+    if (P.particle == 0) {  // spheres, :44-58
+        pq = formpq_sphere(P, q);
+        if (P.lattice) fq = formfq_sphere(P, q);
+        pqiso = pq;
+    } else if (P.particle == 1) {  // cylinders, :64-165
+        if (P.ordis == 6) {
+            switch (P.orcase) {
+            case CS_ORC_GENERAL:
+                pq = formpq_cylinder(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q);
+                if (P.lattice)
+                    fq = formfq_cylinder(C, sqrt(P.cosphi * qx * qx + P.sinphi * qy * qy + CS_EPS9),
+                                         qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q);
+                break;
+            case CS_ORC_XAXIS:
+                pq = formpq_cylinder(C, qx, 0, q);
+                if (P.lattice) fq = formfq_cylinder(C, fabs(qx), qx, 0, q);
+                break;
+            case CS_ORC_YAXIS:
+                pq = formpq_cylinder(C, 0, qy, q);
+                if (P.lattice) fq = formfq_cylinder(C, fabs(qy), 0, qy, q);
+                break;
+            case CS_ORC_ZAXIS:
+                pq = formpq_cylinder(C, qx, qy, q);
+                if (P.lattice) fq = formfq_cylinder(C, q, qx, qy, q);
+                break;
+            }
+        } else if (P.ordis == 0) {
+            switch (P.orcase) {
+            case CS_ORC_GENERAL:
+                pq = formpq_cylinder(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q);
+                if (P.lattice)
+                    fq = formfq_cylinder(C, q, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q);
+                break;
+            case CS_ORC_XAXIS:
+                pq = formpq_cylinder(C, qx, qy, q);
+                if (P.lattice) fq = formfq_cylinder(C, sqrt(qx * qx + (1 - P.order) * qy * qy), qx, qy, q);
+                break;
+            case CS_ORC_YAXIS:
+                pq = formpq_cylinder(C, qx, qy, q);
+                if (P.lattice) fq = formfq_cylinder(C, sqrt((1.0 - P.order) * qx * qx + qy * qy), qx, qy, q);
+                break;
+            case CS_ORC_ZAXIS:
+                pq = formpq_cylinder(C, qx, qy, q);
+                if (P.lattice) fq = formfq_cylinder(C, q, qx, qy, q);
+                break;
+            }
+        }
+    } else if (P.particle == 4) {  // cubes, :291-320
+        pq = formpq_cube(P, q);
+        fq = pq;
+    }
+
+    double width = 1;  // :511-524
+    if (P.debyescherrer) width = 4.0 / P.domainsize;
+    if (P.para) width = (4.0 / P.domainsize) + sqr(P.reldis) * P.dist * sqr(q);
+    width *= P.width_zuf;
+    const double widthiso = 1.0 / P.uca;
+    radintensity = 0.0;
+    intensity = 0.0;
+    if (P.lattice) {  // :537-846
+        const double sphno_cubevol = P.latpar[1] * P.latpar[2];
+        for (int ii = 1; ii <= P.peakmax1; ii++) {
+            const int mhkl = P.latpar1[ii][4];
+            const int fhkl = P.latpar1[ii][5];
+            const double qhkl = P.latpar3[ii][5];
+            const double x2 = sqr(q - qhkl) / sqr(widthiso);
+            const double sq = exp(-4 * x2 / M_PI) / (M_PI * widthiso / 2.0);
+            const double savintens = radintensity;
+            radintensity += sq * mhkl * fhkl;
+            if (isinf(radintensity) || isnan(radintensity)) {
+                radintensity = savintens;
+                break;
+            }
+        }
+        for (int ii = 1; ii <= P.peakmax2; ii++) {
+            const double qhkl = P.latpar3[ii][5];
+            if (qhkl <= 0 || isnan(qhkl)) continue;
+            const int mhkl = P.latpar2[ii][4];
+            const int fhkl = P.latpar2[ii][5];
+            const double qxhkl = P.latpar3[ii][2], qyhkl = P.latpar3[ii][3], qzhkl = P.latpar3[ii][4];
+            const double qxhklt = P.latpar3[ii][7], qyhklt = P.latpar3[ii][8], qzhklt = P.latpar3[ii][9];
+            const double g3 = P.latpar3[ii][10];
+            const double peaknorm1 = P.latpar3[ii][11];
+            double sq = 1.0, psiord = 1.0;
+            const double yphi = myacos((qx * qxhkl + qy * qyhkl + qz * qzhkl) / (q * qhkl));
+            const double x2 = (q - qhkl) * (q - qhkl) / (width * width);
+            double yphit = 0;
+            if (P.twin) yphit = myacos((qx * qxhklt + qy * qyhklt + qz * qzhklt) / (q * qhkl));
+            switch (P.shp) {
+            case 1: {  // Lorentzian, :692-704
+                sq = sqrt(P.pk_c1) / (M_PI * width * (1.0 + P.pk_c1 * x2));
+                const double x2phi = 4 * q * q / sqr(P.phiwidth);
+                psiord = g3 / (peaknorm1 * (1 + x2phi * yphi * yphi));
+                if (P.twin) {
+                    const double phiord = g3 / (peaknorm1 * (1 + x2phi * yphit * yphit));
+                    psiord = P.ceff * psiord + (1 - P.ceff) * phiord;
+                }
+                break;
+            }
+            case 2: {  // Gaussian, :706-727
+                sq = exp(-4 * x2 / M_PI) / (M_PI * width / 2.0);
+                const double x2phi = 4 * q * q / (M_PI * sqr(P.phiwidth));
+                psiord = g3 * exp(-x2phi * yphi * yphi) / peaknorm1;
+                if (P.twin) {
+                    const double phiord = g3 * exp(-x2phi * yphit * yphit) / peaknorm1;
+                    psiord = P.ceff * psiord + (1 - P.ceff) * phiord;
+                }
+                break;
+            }
+            case 3: {  // modified Lorentzian 1, :739-752
+                sq = 2 * sqrt(P.pk_c2) / (M_PI * width * (1 + P.pk_c1 * x2) * (1 + P.pk_c1 * x2));
+                const double x2phi = 4 * q * q / sqr(P.phiwidth);
+                psiord = g3 / (peaknorm1 * (1 + x2phi * yphi * yphi) * (1 + x2phi * yphi * yphi));
+                if (P.twin) {
+                    const double phiord = g3 / (peaknorm1 * (1 + x2phi * yphit * yphit) * (1 + x2phi * yphit * yphit));
+                    psiord = P.ceff * psiord + (1 - P.ceff) * phiord;
+                }
+                break;
+            }
+            case 4: {  // modified Lorentzian 2, :754-767
+                sq = sqrt(P.pk_c3) / (2 * width * exp(3 * log(1 + P.pk_c1 * x2) / 2.0));
+                const double x2phi = 4 * q * q / sqr(P.phiwidth);
+                psiord = g3 / (peaknorm1 * exp(3 * log(1 + x2phi * yphi * yphi) / 2.0));
+                if (P.twin) {
+                    const double phiord = g3 / (peaknorm1 * exp(3 * log(1 + x2phi * yphit * yphit) / 2.0));
+                    psiord = P.ceff * psiord + (1 - P.ceff) * phiord;
+                }
+                break;
+            }
+            case 5: {  // pseudo-Voigt, :769-785
+                const double peaknorm2 = P.latpar3[ii][12];
+                const double eta = P.pk_eta;
+                sq = eta * sqrt(P.pk_c1) / (M_PI * width * (1 + P.pk_c1 * x2)) +
+                     (1 - eta) * sqrt(1.0) * exp(-1.0 * x2) / (sqrt(M_PI) * width);
+                const double x2psi = 4 * q * q / (M_PI * sqr(P.phiwidth));
+                const double x2phi = 4 * q * q / sqr(P.phiwidth);
+                psiord = g3 * (eta * (1 / (1 + x2phi * yphi * yphi)) + (1 - eta) * exp(-x2psi * yphi * yphi)) /
+                         (eta * peaknorm1 + (1 - eta) * peaknorm2);
+                if (P.twin) {
+                    const double phiord =
+                        g3 * (eta * (1 / (1 + x2phi * yphit * yphit)) + (1 - eta) * exp(-x2psi * yphit * yphit)) /
+                        (eta * peaknorm1 + (1 - eta) * peaknorm2);
+                    psiord = P.ceff * psiord + (1 - P.ceff) * phiord;
+                }
+                break;
+            }
+            case 6: {  // Pearson VII, :787-800
+                const double beta = P.pk_beta;
+                sq = P.pk_gbeta * P.pk_c4 * 2 /
+                     (P.pk_gbeta_h * M_PI * width * exp(beta * log(1 + 4 * P.pk_c4 * x2)));
+                const double x2phi = 4 * q * q / sqr(P.phiwidth);
+                psiord = g3 / (peaknorm1 * exp(beta * log(1 + x2phi * yphi * yphi)));
+                if (P.twin) {
+                    const double phiord = g3 / (peaknorm1 * exp(beta * log(1 + x2phi * yphit * yphit)));
+                    psiord = P.ceff * psiord + (1 - P.ceff) * phiord;
+                }
+                break;
+            }
+            default:
+                return 0.0;  // :833-834
+            }
+            const double savintens = intensity;
+            intensity += sq * mhkl * fhkl * psiord;
+            if (isinf(intensity) || isnan(intensity)) {
+                intensity = savintens;
+                break;
+            }
+        }
+        szqiso = (1 + (1) * (8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol) - 1) *
+                          exp(-P.ucb * q * q));
+        szq = (1 + (fq / pq) * (2 * M_PI * intensity / (sphno_cubevol)-1) * exp(-P.dwfactor * q * q));
+    }
+    return P.base + P.izero * (szq * pq + P.iso * szqiso * pqiso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+}
+
 template <int KEY>
 __device__ __forceinline__ double calc_pixel(const Ctx &C, double qx, double qy, double qz) {
     if (KEY == CS_KEY_SPHERE_NONE_ISO) return calc_sphere_none_iso(C, qx, qy, qz);
@@ -712,6 +912,8 @@ __device__ __forceinline__ double calc_pixel(const Ctx &C, double qx, double qy,
     if (KEY == CS_KEY_CYL_NONE_GAUSS) return calc_cyl_none_gauss(C, qx, qy, qz);
     if (KEY == CS_KEY_CYL_NONE_ZDIR) return calc_cyl_none_zdir(C, qx, qy, qz);
     if (KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR) return calc_cyl_bct_zdir(C, qx, qy, qz);
+    if (KEY == CS_KEY_CUBE_NONE_ISO) return calc_cube_none_iso(C, qx, qy, qz);
+    if (KEY == CS_KEY_GENERIC) return calc_generic(C, qx, qy, qz);
     return 0.0;
 }
 

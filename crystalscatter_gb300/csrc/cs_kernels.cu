@@ -349,8 +349,22 @@ static int grid_for(long n, int block) {
 }
 
 bool key_supported(const cs_prepared &P) {
-    if (P.ign_switch) return false;
     switch (P.key) {
+    case CS_KEY_SPHERE_NONE_ISO:
+    case CS_KEY_SPHERE_GAUSS_FCC_GAUSS:
+    case CS_KEY_CYL_NONE_GAUSS:
+    case CS_KEY_CYL_NONE_ZDIR:
+    case CS_KEY_CYL_GAUSS_BCT_ZDIR:
+    case CS_KEY_CUBE_NONE_ISO:
+    case CS_KEY_GENERIC:
+        return true;
+    default:
+        return false;
+    }
+}
+
+bool mixed_key(int key) {
+    switch (key) {
     case CS_KEY_SPHERE_NONE_ISO:
     case CS_KEY_SPHERE_GAUSS_FCC_GAUSS:
     case CS_KEY_CYL_NONE_GAUSS:
@@ -379,6 +393,8 @@ int launch_image(const DevSet &D, const cs_prepared &P, double *d_out, cudaStrea
     case CS_KEY_CYL_NONE_GAUSS: launch_image_key<CS_KEY_CYL_NONE_GAUSS>(D, P, d_out, s); break;
     case CS_KEY_CYL_NONE_ZDIR: launch_image_key<CS_KEY_CYL_NONE_ZDIR>(D, P, d_out, s); break;
     case CS_KEY_CYL_GAUSS_BCT_ZDIR: launch_image_key<CS_KEY_CYL_GAUSS_BCT_ZDIR>(D, P, d_out, s); break;
+    case CS_KEY_CUBE_NONE_ISO: launch_image_key<CS_KEY_CUBE_NONE_ISO>(D, P, d_out, s); break;
+    case CS_KEY_GENERIC: launch_image_key<CS_KEY_GENERIC>(D, P, d_out, s); break;
     default: return CS_ERR_UNSUPPORTED;
     }
     if (P.expand && P.calc_quadrants != CS_RADQ4 && P.calc_quadrants != CS_RAD1D) launch_mirror(P, d_out, s);
@@ -406,6 +422,8 @@ int launch_redo(const DevSet &D, const cs_prepared &P, double *d_out, const Mixe
     case CS_KEY_CYL_NONE_GAUSS: launch_redo_key<CS_KEY_CYL_NONE_GAUSS>(D, P, d_out, S, s); break;
     case CS_KEY_CYL_NONE_ZDIR: launch_redo_key<CS_KEY_CYL_NONE_ZDIR>(D, P, d_out, S, s); break;
     case CS_KEY_CYL_GAUSS_BCT_ZDIR: launch_redo_key<CS_KEY_CYL_GAUSS_BCT_ZDIR>(D, P, d_out, S, s); break;
+    case CS_KEY_CUBE_NONE_ISO: launch_redo_key<CS_KEY_CUBE_NONE_ISO>(D, P, d_out, S, s); break;
+    case CS_KEY_GENERIC: launch_redo_key<CS_KEY_GENERIC>(D, P, d_out, S, s); break;
     default: return CS_ERR_UNSUPPORTED;
     }
     return CS_OK;
@@ -427,6 +445,8 @@ int launch_fit(const DevSet &D, const cs_prepared &P, const double *d_data, doub
     case CS_KEY_CYL_NONE_GAUSS: launch_fit_key<CS_KEY_CYL_NONE_GAUSS>(D, P, d_data, d_fqs, nbuf, s); break;
     case CS_KEY_CYL_NONE_ZDIR: launch_fit_key<CS_KEY_CYL_NONE_ZDIR>(D, P, d_data, d_fqs, nbuf, s); break;
     case CS_KEY_CYL_GAUSS_BCT_ZDIR: launch_fit_key<CS_KEY_CYL_GAUSS_BCT_ZDIR>(D, P, d_data, d_fqs, nbuf, s); break;
+    case CS_KEY_CUBE_NONE_ISO: launch_fit_key<CS_KEY_CUBE_NONE_ISO>(D, P, d_data, d_fqs, nbuf, s); break;
+    case CS_KEY_GENERIC: launch_fit_key<CS_KEY_GENERIC>(D, P, d_data, d_fqs, nbuf, s); break;
     default: return CS_ERR_UNSUPPORTED;
     }
     const int nb = R.nblocks;
@@ -447,7 +467,7 @@ int launch_batch_fp64(const BatchSetDev *d_sets, const BatchGroup &g, unsigned l
         cs64::k_batch_fp64<K><<<grid, CS_BATCH_TILE, 0, s>>>(d_sets, g.set_begin, g.set_end, g.tiles, d_counter, \
                                                              d_chi, d_out);                                     \
         break;
-        CS_FOR_EACH_KEY(CS_CASE)
+        CS_FOR_EACH_KEY_FP64(CS_CASE)
 #undef CS_CASE
     default: return CS_ERR_UNSUPPORTED;
     }
@@ -460,7 +480,7 @@ int launch_batch_redo(const BatchSetDev *d_sets, int key, const cs_chi_node *d_c
     switch (key) {
 #define CS_CASE(K)                                                                                  \
     case K: cs64::k_batch_redo<K><<<grid, 128, 0, s>>>(d_sets, d_chi, d_out, d_count, d_list, cap); break;
-        CS_FOR_EACH_KEY(CS_CASE)
+        CS_FOR_EACH_KEY_FP64(CS_CASE)
 #undef CS_CASE
     default: return CS_ERR_UNSUPPORTED;
     }
@@ -472,7 +492,7 @@ int batch_blocks_per_sm_fp64(int key) {
     switch (key) {
 #define CS_CASE(K) \
     case K: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cs64::k_batch_fp64<K>, CS_BATCH_TILE, 0); break;
-        CS_FOR_EACH_KEY(CS_CASE)
+        CS_FOR_EACH_KEY_FP64(CS_CASE)
 #undef CS_CASE
     default: return 0;
     }

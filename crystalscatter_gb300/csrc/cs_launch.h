@@ -27,6 +27,10 @@ struct FitReduce {
 };
 
 bool key_supported(const cs_prepared &P);
+// keys with a mixed-precision kernel; the others (and twinned lattices) run
+// their FP64 kernel when mixed precision is requested (exact, so within any
+// mixed tolerance)
+bool mixed_key(int key);
 // True when the prepared set evaluates the cylinder orientation integral.
 bool needs_delta_table(const cs_prepared &P);
 

@@ -1862,8 +1862,41 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
         P.ymax = P.iimax;
     }
 
-    // dispatch key, Source/sc_calc_generic_gpu.cu:113
+    // peak-shape constants, :585-590 (c0 = 1 is written as a literal), and
+    // setPeakPar (eta = peakpar/100, beta = peakpar)
+    P.pk_c1 = 4;
+    P.pk_c2 = 4 * (std::sqrt(2.0) - 1);
+    P.pk_c3 = 4 * (std::exp(2 * std::log(2.0) / 3.0) - 1);
+    P.pk_beta = in.peakpar;
+    P.pk_c4 = (P.pk_beta == 0) ? 1 : std::exp(std::log(2.) / P.pk_beta) - 1;
+    P.pk_eta = in.peakpar / 100.;
+    P.pk_gbeta = P.pk_gbeta_h = 0;
+    if (shp == 6) {
+        P.pk_gbeta = ref_gamma(P.pk_beta);
+        P.pk_gbeta_h = ref_gamma(P.pk_beta - 0.5);
+    }
+
+    // dispatch key, Source/sc_calc_generic_gpu.cu:113: the specialised pixel
+    // functions, else calc_GENERIC (also for every combination when the new
+    // switch is ignored)
     P.key = (P.particle << 24) | (P.ltype == 12 ? 0 : (shp << 16)) | (P.ltype << 8) | P.ordis;
+    const bool special = !P.ign_switch &&
+                         (P.key == CS_KEY_SPHERE_NONE_ISO || P.key == CS_KEY_SPHERE_GAUSS_FCC_GAUSS ||
+                          P.key == CS_KEY_CYL_NONE_GAUSS || P.key == CS_KEY_CYL_NONE_ZDIR ||
+                          P.key == CS_KEY_CYL_GAUSS_BCT_ZDIR || P.key == CS_KEY_CUBE_NONE_ISO);
+    if (!special) {
+        // the generic pixel function covers the particles prepared above:
+        // spheres, cylinders (z-direction, Gaussian orientation) and
+        // homogeneous isotropic cubes
+        const bool ok = P.particle == 0 || (P.particle == 1 && (P.ordis == 6 || P.ordis == 0)) ||
+                        (P.particle == 4 && P.ordis == 7 && P.cs == 0);
+        if (!ok) {
+            err = "generic pixel function: particle " + std::to_string(P.particle) + " with ordis " +
+                  std::to_string(P.ordis) + " is not implemented";
+            return CS_ERR_UNSUPPORTED;
+        }
+        P.key = CS_KEY_GENERIC;
+    }
     for (int i = 0; i < 4; i++) {
         P.nofit_x0[i] = P.nofit_x1[i] = P.nofit_y0[i] = P.nofit_y1[i] = -1;
     }

@@ -41,6 +41,9 @@
 #define CS_KEY_CYL_NONE_ZDIR 0x01000C06
 #define CS_KEY_CYL_GAUSS_BCT_ZDIR 0x01020806
 #define CS_KEY_CUBE_NONE_ISO 0x04000C07
+/* every other combination, and every combination with bIgnoreNewSwitch: the
+   reference's calc_GENERIC (Source/sc_gpu_generic.h:27-881) */
+#define CS_KEY_GENERIC 0x7F000000
 
 typedef struct cs_prepared {
     /* dispatch */
@@ -96,6 +99,11 @@ typedef struct cs_prepared {
     /* 2D-fit masks (checkFitRanges, Source/sc_calc_generic_gpu.cu:293-347) */
     int nofit_x0[4], nofit_x1[4], nofit_y0[4], nofit_y1[4];
     int fit_width, fit_height, fit_bstop, fit_border;
+
+    /* peak-shape constants of the generic lattice sums (prepareCalculation,
+       Source/sc_calc_generic_cpu.cpp:585-590, and setPeakPar: eta = peakpar/100,
+       beta = peakpar); gamma(beta) and gamma(beta - 1/2) for Pearson VII */
+    double pk_c1, pk_c2, pk_c3, pk_c4, pk_eta, pk_beta, pk_gbeta, pk_gbeta_h;
 } cs_prepared;
 
 #endif /* CS_PREPARED_H */

@@ -25,6 +25,7 @@ class CsPrepared(ctypes.Structure):
            ("latpar1", (_I * 6) * 2500), ("latpar2", (_I * 6) * 2500), ("latpar3", (ctypes.c_float * 17) * 2500)]
         + [("nofit_x0", _I * 4), ("nofit_x1", _I * 4), ("nofit_y0", _I * 4), ("nofit_y1", _I * 4)]
         + [(n, _I) for n in "fit_width fit_height fit_bstop fit_border".split()]
+        + [(n, _D) for n in "pk_c1 pk_c2 pk_c3 pk_c4 pk_eta pk_beta pk_gbeta pk_gbeta_h".split()]
     )
 
 

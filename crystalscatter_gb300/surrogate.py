@@ -29,6 +29,10 @@ import crystalscatter_gb300 as cs
 from crystalscatter_gb300 import configs as C
 
 SPREAD = 0.30
+# start vectors stay inside +-START_BOX: the reference's initial simplex moves
+# every parameter up by a fraction of its step, so a start at a fit limit
+# puts every vertex outside the limits (chi^2 1e20) and the fit cannot move
+START_BOX = 0.8
 FLOOR = 1e-9  # intensity floor of the log10 targets (zero pixels of the degenerate family)
 FAMILIES = {
     "2": (C.CYL_GAUSS, ["EditRadius", "EditSigma", "Length", "SigmaL", "EditDbeta", "theta", "phi", "I0"]),
@@ -97,12 +101,17 @@ class Surrogate:
         self.net = cs.SurrogateMLP(len(fam.keys), hidden, 64 * 64, seed=seed)
         self.mean, self.std = 0.0, 1.0  # per-pixel tensors after training
 
-    def train(self, U, Y, epochs=30, batch=512, lr=1e-3, seed=0):
+    def train(self, U, Y, epochs=200, batch=512, lr=1e-3, seed=0, pixel_norm=False):
         import torch
         # per-pixel standardisation: the network learns each q's deviation from
-        # its mean over the family (floor: 5 % of the overall spread)
-        mean = Y.mean(axis=0)
-        std = np.maximum(Y.std(axis=0), 0.05 * float(Y.std()) + 1e-6)
+        # its mean over the family (floor: 5 % of the overall spread); or one
+        # mean and spread for all pixels
+        if pixel_norm:
+            mean = Y.mean(axis=0)
+            std = np.maximum(Y.std(axis=0), 0.05 * float(Y.std()) + 1e-6)
+        else:
+            mean = np.full(Y.shape[1], Y.mean(), dtype=np.float64)
+            std = np.full(Y.shape[1], float(Y.std()) or 1.0)
         self.mean = torch.from_numpy(mean.astype(np.float32)).cuda()
         self.std = torch.from_numpy(std.astype(np.float32)).cuda()
         x = torch.from_numpy(U).cuda()
@@ -219,7 +228,7 @@ def seeded_fit(fam, target, u0, chi2_stop, maxit, ftol, stp, schedule, restarts=
             best_res, best = res, dict(rep)
         if best["chi2"] <= chi2_stop or reps >= maxit:
             break
-        u = np.clip(fam.u_of(best_res), -1.0, 1.0)
+        u = np.clip(fam.u_of(best_res), -START_BOX, START_BOX)
     best.update({"images": images, "repetitions": reps, "restarts": r})
     return best_res, best
 
@@ -247,8 +256,8 @@ def compare_fits(fam, sur, n_targets=8, seed=0, maxit=300, ftol=1e-5, stp=0.1, s
         if shortlist > 1:
             u_s, chi2_start = exact_pick(fam, target, short)
         t_prop = time.perf_counter() - t0
-        res_s, rep_s = seeded_fit(fam, target, u_s, rep_p["chi2"] * (1 + 1e-3), maxit, ftol, stp_seeded,
-                                  schedule_seeded, restarts)
+        res_s, rep_s = seeded_fit(fam, target, np.clip(u_s, -START_BOX, START_BOX), rep_p["chi2"] * (1 + 1e-3),
+                                  maxit, ftol, stp_seeded, schedule_seeded, restarts)
         t_seeded = time.perf_counter() - t0  # proposal + fit
         rows.append({"target": i, "chi2_plain": rep_p["chi2"], "chi2_seeded": rep_s["chi2"], "chi2_start": chi2_start,
                      "restarts": rep_s["restarts"],

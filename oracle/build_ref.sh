@@ -22,3 +22,15 @@ g++ $CXXFLAGS -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o" &
 wait
 g++ -shared -o "$OUT/libscref.so" "$OUT/sc_calc_generic_cpu.o" "$OUT/sc_calc_generic_gpu.o" "$OUT/ref_driver.o" -lpthread
 echo "built $OUT/libscref.so"
+# probe build: the same sources without builtins (every math call stays a
+# call), linked with one-ulp wrappers of the math library (ref_probe.c)
+PFLAGS="$CXXFLAGS -fno-builtin"
+g++ $PFLAGS -c -x c++ "$REF/Source/sc_calc_generic_cpu.cpp" -o "$OUT/probe_cpu.o" &
+g++ $PFLAGS -c -x c++ "$REF/Source/sc_calc_generic_gpu.cu" -o "$OUT/probe_gpu.o" &
+g++ $PFLAGS -c "$HERE/ref_driver.cpp" -o "$OUT/probe_driver.o" &
+gcc -O2 -fPIC -c "$HERE/ref_probe.c" -o "$OUT/ref_probe.o" &
+wait
+WRAP="-Wl,--wrap=sin,--wrap=cos,--wrap=atan,--wrap=atan2,--wrap=pow,--wrap=exp,--wrap=log,--wrap=acos"
+g++ -shared $WRAP -o "$OUT/libscref_probe.so" "$OUT/probe_cpu.o" "$OUT/probe_gpu.o" "$OUT/probe_driver.o" \
+    "$OUT/ref_probe.o" -lpthread -lm
+echo "built $OUT/libscref_probe.so"

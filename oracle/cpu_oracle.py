@@ -102,6 +102,11 @@ def prepare(params, ign_cbs=0):
     return P
 
 
+def supported(P):
+    """True when the oracle restates the pixel function of prepared block P."""
+    return bool(load().oracle_supported(ctypes.byref(P)))
+
+
 def image(params, ign_cbs=0, nthreads=None, rows=None):
     """The oracle image for a parameter dict (all rows, or ihex rows [r0,r1))."""
     P = prepare(params, ign_cbs)

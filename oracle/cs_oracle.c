@@ -778,6 +778,18 @@ double oracle_pixel_q(const cs_prepared *P, double qx, double qy, double qz) {
         const double szq = (1 + (fq / pq) * (2 * M_PI * intensity / (sphno_cubevol)-1) * exp(-P->dwfactor * q * q));
         return P->base + P->izero * (szq * pq + P->iso * szqiso * pqiso) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
     }
+    case CS_KEY_CUBE_NONE_ISO: {
+        /* calc_partCube_lattNone_ordisIsotropic, Source/sc_gpu_pCub_lNon_oIso.h:16-77, with
+           formpq_partCube's homogeneous isotropic branch, Source/sc_lib_formpq_partCube.h:21-62 */
+        double pq = 1.0;
+        if (P->cs == 0) {
+            if (q < 1.2 * P->limq[4])
+                pq = series_q(P->carrp[3], q, 120);
+            else
+                pq = P->por / (q * q * q * q);
+        }
+        return P->base + P->izero * (pq + P->iso) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
+    }
     default:
         return NAN;
     }
@@ -790,7 +802,8 @@ int oracle_supported(const cs_prepared *P) {
     case CS_KEY_SPHERE_GAUSS_FCC_GAUSS:
     case CS_KEY_CYL_NONE_GAUSS:
     case CS_KEY_CYL_NONE_ZDIR:
-    case CS_KEY_CYL_GAUSS_BCT_ZDIR: return 1;
+    case CS_KEY_CYL_GAUSS_BCT_ZDIR:
+    case CS_KEY_CUBE_NONE_ISO: return 1;
     default: return 0;
     }
 }

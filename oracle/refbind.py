@@ -13,19 +13,30 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_ref", "libscref.so")
+PROBE = os.path.join(HERE, "_ref", "libscref_probe.so")
 
 _lib = None
+_probe = None
 
 
 def available():
     return os.path.exists(LIB)
 
 
-def load():
-    global _lib
-    if _lib is not None:
-        return _lib
-    lib = ctypes.CDLL(LIB)
+def load(probe=False):
+    """The reference library; probe=True: its one-ulp probe build."""
+    global _lib, _probe
+    if probe:
+        if _probe is None:
+            _probe = _bind(ctypes.CDLL(PROBE))
+            _probe.ref_set_probe.argtypes = [ctypes.c_int]
+        return _probe
+    if _lib is None:
+        _lib = _bind(ctypes.CDLL(LIB))
+    return _lib
+
+
+def _bind(lib):
     V = ctypes.c_void_p
     lib.ref_create.restype = V
     lib.ref_destroy.argtypes = [V]
@@ -50,15 +61,14 @@ def load():
     lib.ref_fit.restype = ctypes.c_double
     lib.ref_fit_fqs.argtypes = [V, ctypes.c_void_p, ctypes.c_long]
     lib.ref_fit_fqs.restype = ctypes.c_long
-    _lib = lib
     return lib
 
 
 class RefCalc:
     """One reference calculation: parameters by reference key, then run()."""
 
-    def __init__(self, params=None):
-        self.lib = load()
+    def __init__(self, params=None, probe=False):
+        self.lib = load(probe)
         self.h = self.lib.ref_create()
         if params:
             self.set(params)
@@ -125,3 +135,35 @@ class RefCalc:
         fqs = np.zeros(w * h, dtype=np.float64)
         self.lib.ref_fit_fqs(self.h, fqs.ctypes.data, w * h)
         return chi2, cnt.value, nan.value, fqs.reshape(h, w)
+
+
+PROBE_MODES = (0x1FF, 0x100, 0x155, 0x0AA)
+
+
+def condition(params, ign_new_switch=0, ign_cbs=0, nthreads=8, modes=PROBE_MODES):
+    """Per-pixel sensitivity of the reference's own result to one-ulp changes
+    of its math library: max over probe modes of |I_mode - I| / max(|I|, tau),
+    I the unperturbed image of the probe build; non-finite disagreements are
+    inf."""
+    lib = load(probe=True)
+    imgs = []
+    for m in (-1,) + tuple(modes):
+        lib.ref_set_probe(int(m))
+        r = RefCalc(params, probe=True)
+        rc, err = r.run(nthreads=nthreads, ign_new_switch=ign_new_switch, ign_cbs=ign_cbs)
+        assert rc == 0, err
+        imgs.append(r.image())
+        r.close()
+    lib.ref_set_probe(-1)
+    base = imgs[0]
+    fin = np.isfinite(base)
+    tau = 1e-30 * (np.max(np.abs(base[fin])) if fin.any() else 1.0)
+    cond = np.zeros(base.shape)
+    for out in imgs[1:]:
+        with np.errstate(invalid="ignore", over="ignore"):
+            d = np.abs(out - base) / np.maximum(np.abs(base), tau)
+        same_nf = (~np.isfinite(base)) & ((np.isnan(base) & np.isnan(out)) | (base == out))
+        d[same_nf] = 0.0
+        d[~np.isfinite(d)] = np.inf
+        cond = np.maximum(cond, d)
+    return cond

@@ -10,7 +10,9 @@ the chi^2 sums. Usage (needs the reference sources and the built oracle/_ref):
 
 Each case also stores "cond", the per-pixel sensitivity of the reference's
 result to one-ulp differences of the math library (oracle.cpu_oracle.condition,
-measured with the reference-pinned oracle): pixels where the reference's own
+measured with the reference-pinned oracle, or, for the generic pixel function
+that the oracle does not restate, oracle.refbind.condition on the reference's
+own probe build): pixels where the reference's own
 result moves by more than 1e-12 under such perturbations cannot be reproduced
 to 1e-10 by another math library and are compared against that envelope.
 
@@ -66,7 +68,27 @@ def image_cases():
         b = C.bct_set(k)
         cases[f"cyl_bct_set{k}_g24"] = C.scaled(b, 24)
     cases["cyl_bct_zaxis_g24"] = dict(C.scaled(C.bct_set(0), 24), theta=0.0, phi=0.0)
+    # cube (its own pixel function) and the generic pixel function: other
+    # lattices and peak shapes, cubes and cylinders on lattices, and the
+    # specialised combinations with the new switch ignored
+    sph = C.scaled(C.SPHERE_FCC, 24)
+    cases["cube_g32"] = dict(C.scaled(C.SPHERE, 32), ComboBoxParticle=4)
+    cases["cube_fcc_g24"] = dict(sph, ComboBoxParticle=4, Ordis=7)
+    cases["sphere_bcc_g24"] = dict(sph, LType=4)
+    cases["sphere_sc_g24"] = dict(sph, LType=7)
+    cases["sphere_fcc_lorentz_g24"] = dict(sph, ComboBoxPeak=0)
+    cases["sphere_fcc_modlor1_g24"] = dict(sph, ComboBoxPeak=2)
+    cases["sphere_fcc_modlor2_g24"] = dict(sph, ComboBoxPeak=3)
+    cases["sphere_fcc_voigt_g24"] = dict(sph, ComboBoxPeak=4, EditPeakPar=40.0)
+    cases["sphere_fcc_pearson_g24"] = dict(sph, ComboBoxPeak=5, EditPeakPar=1.5)
+    cases["sphere_fcc_twin_g24"] = dict(sph, LType=4, CheckBoxTwinned=1, EditCeff=0.7)
+    cases["sphere_fcc_ignswitch_g24"] = dict(sph)
+    cases["cyl_zdir_fcc_g24"] = dict(C.scaled(C.bct_set(2), 24), LType=5)
+    cases["cyl_gauss_x_ignswitch_g16"] = C.scaled(C.CYL_GAUSS_X, 16)
     return cases
+
+
+IGN_NEW_SWITCH = {"sphere_fcc_ignswitch_g24", "cyl_gauss_x_ignswitch_g16"}
 
 
 def ign_cbs_for(p):
@@ -94,12 +116,26 @@ def main():
     for name, p in image_cases().items():
         r = refbind.RefCalc(p)
         ign = ign_cbs_for(p)
-        rc, err = r.run(nthreads=8, ign_cbs=ign)
+        ins = 1 if name in IGN_NEW_SWITCH else 0
+        rc, err = r.run(nthreads=8, ign_new_switch=ins, ign_cbs=ign)
+        if rc != 0 and "INVALID CBParticle" in err and not ign:
+            # the console's combination check rejects it: run as the benchmark
+            # runs such combinations, with bIgnoreCbs
+            r.close()
+            ign = 1
+            r = refbind.RefCalc(p)
+            rc, err = r.run(nthreads=8, ign_new_switch=ins, ign_cbs=ign)
         assert rc == 0, (name, err)
         img = r.image()
         # per-pixel conditioning of the reference computation: spread of the
-        # (reference-pinned) oracle under one-ulp math-library perturbations
-        cond = cpu_oracle.condition(p, ign_cbs=ign, nthreads=8)
+        # (reference-pinned) oracle under one-ulp math-library perturbations;
+        # for the generic pixel function, which the oracle does not restate,
+        # the spread of the reference's own probe build (oracle/ref_probe.c)
+        P0 = cpu_oracle.prepare(p, ign)
+        if ins == 0 and cpu_oracle.supported(P0):
+            cond = cpu_oracle.condition(p, ign_cbs=ign, nthreads=8)
+        else:
+            cond = refbind.condition(p, ign_new_switch=ins, ign_cbs=ign, nthreads=8)
         rec = {"image": img, "dims": np.array(r.dims()), "cond": cond.astype(np.float32)}
         for a in ARRAYS:
             rec[a] = r.array(a)
@@ -111,7 +147,7 @@ def main():
             rec["latpar2"] = r.latpar(2)[: pm2 + 1]
             rec["latpar3"] = r.latpar(3)[: pm2 + 1]
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **rec)
-        out[name] = {"params": p, "ign_cbs": ign, "shape": list(img.shape),
+        out[name] = {"params": p, "ign_cbs": ign, "ign_new_switch": ins, "shape": list(img.shape),
                      "nonfinite": int((~np.isfinite(img)).sum()), "zeros": int((img == 0).sum()),
                      "ill_conditioned": int((cond > 1e-12).sum())}
         print(name, img.shape, "nonfinite", out[name]["nonfinite"], "zeros", out[name]["zeros"],

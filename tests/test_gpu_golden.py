@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 def run_case(case, mode=cs.CS_MODE_FP64):
     c = cs.SasCalc_GENERIC_calculation()
     c.setParams(case["params"])
-    c.doCalculation(0, False, bool(case["ign_cbs"]), mode=mode)
+    c.doCalculation(0, bool(case.get("ign_new_switch", 0)), bool(case["ign_cbs"]), mode=mode)
     img = c.data()
     dims = [c.minX(), c.maxX(), c.minY(), c.maxY()]
     c.cleanup()

@@ -16,10 +16,10 @@ TOL = 1e-5
 pytestmark = pytest.mark.gpu
 
 
-def run(params, ign_cbs, mode):
+def run(params, ign_cbs, mode, ign_new_switch=0):
     c = cs.SasCalc_GENERIC_calculation()
     c.setParams(params)
-    c.doCalculation(0, False, bool(ign_cbs), mode=mode)
+    c.doCalculation(0, bool(ign_new_switch), bool(ign_cbs), mode=mode)
     img = c.data()
     redo = c.mixed_redo_pixels() if mode == cs.CS_MODE_MIXED else 0
     c.cleanup()
@@ -30,7 +30,7 @@ def run(params, ign_cbs, mode):
 def test_mixed_matches_reference(name):
     case = CASES[name]
     g = golden(name)
-    img, redo = run(case["params"], case["ign_cbs"], cs.CS_MODE_MIXED)
+    img, redo = run(case["params"], case["ign_cbs"], cs.CS_MODE_MIXED, case.get("ign_new_switch", 0))
     m = written_mask(case["params"], img.shape)
     r = compare_to_reference(img, g["image"], g["cond"], mask=m, tol=TOL)
     print(name, "redo", redo, r)

@@ -13,6 +13,8 @@ CASES = golden_cases()["images"]
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_oracle_matches_reference_golden(name):
     case = CASES[name]
+    if case.get("ign_new_switch") or not cpu_oracle.supported(cpu_oracle.prepare(case["params"], case["ign_cbs"])):
+        pytest.skip("generic pixel function: pinned on the GPU against the reference's images directly")
     g = golden(name)
     img = cpu_oracle.image(case["params"], ign_cbs=case["ign_cbs"])
     assert img.shape == g["image"].shape
