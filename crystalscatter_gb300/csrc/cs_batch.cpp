@@ -243,7 +243,7 @@ int enqueue(cs_batch *b, double *d_out, cudaStream_t s, int mode, int schedule) 
                 if (S.npix > b->plain_scratch_cap) {
                     cudaFree(b->plain_scratch.d_list);
                     b->plain_scratch.d_list = nullptr;
-                    if (!b->plain_scratch.d_count && (e = cudaMalloc(&b->plain_scratch.d_count, sizeof(int))) != cudaSuccess)
+                    if (!b->plain_scratch.d_count && (e = cudaMalloc(&b->plain_scratch.d_count, 2 * sizeof(int))) != cudaSuccess)
                         return cuda_fail(b, e, "cudaMalloc(redo count)");
                     if ((e = cudaMalloc(&b->plain_scratch.d_list, sizeof(int) * (size_t)S.npix)) != cudaSuccess)
                         return cuda_fail(b, e, "cudaMalloc(redo list)");
@@ -573,7 +573,7 @@ int cs_batch_capture(cs_batch *b, double *d_out, size_t n_doubles, int mode, int
             cudaError_t e;
             cudaFree(b->plain_scratch.d_list);
             b->plain_scratch.d_list = nullptr;
-            if (!b->plain_scratch.d_count && (e = cudaMalloc(&b->plain_scratch.d_count, sizeof(int))) != cudaSuccess)
+            if (!b->plain_scratch.d_count && (e = cudaMalloc(&b->plain_scratch.d_count, 2 * sizeof(int))) != cudaSuccess)
                 return cuda_fail(b, e, "cudaMalloc(redo count)");
             if ((e = cudaMalloc(&b->plain_scratch.d_list, sizeof(int) * (size_t)most)) != cudaSuccess)
                 return cuda_fail(b, e, "cudaMalloc(redo list)");

@@ -197,7 +197,7 @@ int ensure_mixed(cs_handle *h) {
     const long npix = (long)(h->hprep->zzmax - h->hprep->zzmin) * (long)(h->hprep->iimax - h->hprep->iimin);
     if ((size_t)npix > h->redo_cap) {
         if (h->mscratch.d_list) cudaFree(h->mscratch.d_list);
-        if (!h->mscratch.d_count && (e = cudaMalloc(&h->mscratch.d_count, sizeof(int))) != cudaSuccess)
+        if (!h->mscratch.d_count && (e = cudaMalloc(&h->mscratch.d_count, 2 * sizeof(int))) != cudaSuccess)
             return cuda_fail(h, e, "cudaMalloc(redo count)");
         if ((e = cudaMalloc(&h->mscratch.d_list, sizeof(int) * (size_t)npix)) != cudaSuccess)
             return cuda_fail(h, e, "cudaMalloc(redo list)");

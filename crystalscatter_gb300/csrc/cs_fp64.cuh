@@ -321,6 +321,70 @@ __device__ inline double qromb_chi(const Ctx &C, const ChiArgs &A, double cd, do
     return pq;
 }
 
+// qromb_chi with the chi nodes of a level spread over the lanes of a warp:
+// lane k evaluates node base + k, every lane adds the level's values in node
+// order, so each lane returns qromb_chi's value bit for bit. Levels beyond the
+// node table run on every lane in turn. All lanes call it with the same
+// arguments.
+__device__ inline double qromb_chi_warp(const Ctx &C, const ChiArgs &A, double cd, double sd) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const double a = 0.0, b = C.P->romb_chi_b;
+    double win[5];
+    double cur;
+    int cnt;
+    double pq = 0.0, dss = 0.0;
+    {
+        double v = 0.0;
+        if (lane < 2) {
+            const cs_chi_node n = C.chi[lane];
+            v = chi_integrand(A, n.c, n.s, cd, sd);
+        }
+        const double pa = __shfl_sync(full, v, 0), pb = __shfl_sync(full, v, 1);
+        cur = 0.5 * (b - a) * (pa + pb);
+        cnt = 1;
+    }
+    win[4] = cur;
+    for (int j = 2; j <= 20; j++) {
+        const double tnm = cnt;
+        const double del = (b - a) / tnm;
+        double sump = 0.0;
+        if (j <= CS_NODE_LEVELS) {
+            const cs_chi_node *nd = C.chi + CS_NODE_OFFSET(j);
+            for (int base = 0; base < cnt; base += 32) {
+                double v = 0.0;
+                if (base + lane < cnt) {
+                    const cs_chi_node n = nd[base + lane];
+                    v = chi_integrand(A, n.c, n.s, cd, sd);
+                }
+                const int m = (cnt - base) < 32 ? (cnt - base) : 32;
+                for (int u = 0; u < m; u++) sump += __shfl_sync(full, v, u);
+            }
+        } else {
+            double x = a + 0.5 * del;
+            for (int k = 0; k < cnt; k++) {
+                double s, c;
+                sincos(x, &s, &c);
+                sump += chi_integrand(A, c, s, cd, sd);
+                x += del;
+            }
+        }
+        cur = 0.5 * (cur + (b - a) * sump / tnm);
+        cnt = 2 * cnt;
+        win[0] = win[1];
+        win[1] = win[2];
+        win[2] = win[3];
+        win[3] = win[4];
+        win[4] = cur;
+        if (j >= 5) {
+            polint5(win, pq, dss);
+            if (fabs(dss) < (1.0e-4 * fabs(pq))) break;
+            if (fabs(pq) < 1.0e-300) break;
+        }
+    }
+    return pq;
+}
+
 // qrombdeltac(i0 = 4): Gaussian-weighted delta integral of qrombchid.
 __device__ inline double qromb_delta_cyl(const Ctx &C, const ChiArgs &A) {
     // Orientation cases outside 1..4 (the 0-based general case) reach no
@@ -357,6 +421,79 @@ __device__ inline double qromb_delta_cyl(const Ctx &C, const ChiArgs &A) {
                 double px = qromb_chi(C, A, n.c, n.s);
                 px = n.w * px / (2.0 * M_PI);
                 sump = sump + px;
+            }
+        } else {
+            double x = a + 0.5 * del;
+            for (int k = 0; k < cnt; k++) {
+                double s, c;
+                sincos(x, &s, &c);
+                double px = qromb_chi(C, A, c, s);
+                px = s * exp(-x * x / (dbeta * dbeta)) * px / (2.0 * M_PI);
+                sump = sump + px;
+                x = x + del;
+            }
+        }
+        cur = 0.5 * (cur + (b - a) * sump / tnm);
+        cnt = 2 * cnt;
+        win[0] = win[1];
+        win[1] = win[2];
+        win[2] = win[3];
+        win[3] = win[4];
+        win[4] = cur;
+        if (j >= 5) {
+            polint5(win, pq, dss);
+            if (fabs(dss) < (1.0e-4 * fabs(pq))) break;
+            if (fabs(pq) < 1.0e-100) break;
+        }
+    }
+    return pq;
+}
+
+// The same integral with the delta nodes of a level spread over the lanes of a
+// warp: lane k computes node base + k (its chi integral and weighting exactly
+// as above), and every lane then adds the level's values in node order, so
+// each lane returns qromb_delta_cyl's value bit for bit. A pixel's latency
+// falls from one chi integral per node to about one per level. Levels beyond
+// the node table (never reached in practice) run on every lane in turn. All
+// lanes of the warp call it with the same arguments.
+__device__ inline double qromb_delta_cyl_warp(const Ctx &C, const ChiArgs &A) {
+    if (A.i1 < 1 || A.i1 > 4) return 0.0;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const cs_prepared &P = *C.P;
+    const double a = 0.0, b = P.romb_delta_b;
+    const double dbeta = P.romb_dbeta;
+    double win[5];
+    double cur;
+    int cnt;
+    double pq = 0.0, dss = 0.0;
+    {
+        double v = 0.0;
+        if (lane < 2) {
+            const cs_delta_node n = C.dnode[lane];
+            v = qromb_chi(C, A, n.c, n.s);
+            v = n.w * v / (2.0 * M_PI);
+        }
+        const double pa = __shfl_sync(full, v, 0), pb = __shfl_sync(full, v, 1);
+        cur = 0.5 * (b - a) * (pa + pb);
+        cnt = 1;
+    }
+    win[4] = cur;
+    for (int j = 2; j <= 20; j++) {
+        const double tnm = cnt;
+        const double del = (b - a) / tnm;
+        double sump = 0.0;
+        if (j <= CS_NODE_LEVELS) {
+            const cs_delta_node *nd = C.dnode + CS_NODE_OFFSET(j);
+            for (int base = 0; base < cnt; base += 32) {
+                double px = 0.0;
+                if (base + lane < cnt) {
+                    const cs_delta_node n = nd[base + lane];
+                    px = qromb_chi(C, A, n.c, n.s);
+                    px = n.w * px / (2.0 * M_PI);
+                }
+                const int m = (cnt - base) < 32 ? (cnt - base) : 32;
+                for (int u = 0; u < m; u++) sump = sump + __shfl_sync(full, px, u);
             }
         } else {
             double x = a + 0.5 * del;
@@ -447,6 +584,7 @@ __device__ __forceinline__ double len_factor_ref(double arglq, double zl) {
            (1 - cos((zl - 1) * atan(2.0 * arglq)) / pow(1.0 + 4 * arglq * arglq, (zl - 1) / 2.0));
 }
 
+template <bool WARP = false>
 __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, double q) {
     const cs_prepared &P = *C.P;
     double pqr = 0, pql = 0;
@@ -477,7 +615,7 @@ __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, d
                     pql = cyl_double_series(P, qxs, qys, P.carrp[0], 1);
             } else {
                 const ChiArgs A = chi_args(P, qxs, qys, P.sigmal, P.orcase);
-                pql = qromb_delta_cyl(C, A);
+                pql = WARP ? qromb_delta_cyl_warp(C, A) : qromb_delta_cyl(C, A);
                 pql = pql / P.norm;
             }
         }
@@ -640,18 +778,21 @@ __device__ inline double calc_sphere_fcc(const Ctx &C, double qx, double qy, dou
 
 // calc_partCylinder_lattNone_ordisGauss, Source/sc_gpu_pCyl_lNon_oGau.h:15-100
 // (the lattice branch for F(q) is not taken: lattice is "None").
+// (WARP: the orientation average's delta nodes spread over a warp, for the
+// FP64 redo of single pixels; same value)
+template <bool WARP = false>
 __device__ inline double calc_cyl_none_gauss(const Ctx &C, double qx, double qy, double qz) {
     const cs_prepared &P = *C.P;
     double pq = 0;
     const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
     switch (P.orcase) {
     case CS_ORC_GENERAL:
-        pq = formpq_cylinder(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q);
+        pq = formpq_cylinder<WARP>(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q);
         break;
     case CS_ORC_XAXIS:
     case CS_ORC_YAXIS:
     case CS_ORC_ZAXIS:
-        pq = formpq_cylinder(C, qx, qy, q);
+        pq = formpq_cylinder<WARP>(C, qx, qy, q);
         break;
     }
     return P.base + P.izero * (pq + P.iso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);

@@ -32,8 +32,6 @@ using cs64::Ctx;
 
 #define LOG2E_F 1.4426950408889634f
 
-// (1+x)^e for x >= 0 in FP32 via log1p (no rounding of 1+x)
-__device__ __forceinline__ float powp1f(float x, float e) { return exp2f(e * log1pf(x) * LOG2E_F); }
 
 // Relative error estimates of the form-factor parts: FP64 power series (a few
 // roundings; their own cancellation is that of the reference) and FP32
@@ -258,11 +256,16 @@ __device__ __forceinline__ float len_series(float a, float m) {
     return 1.0f + sum;
 }
 
-__device__ float cyl_len_factor(float a, float z) {
+// The orientation integrand's form (per quadrature node): 4 a1 = 2/(z(z-1)) is
+// a per-pixel constant, and the power enters as (1+4a^2)^(-m/2), so one
+// division remains.
+__device__ __forceinline__ float cyl_len_factor(float a, float z, float a4) {
     const float m = z - 1.0f;
     if (len_series_ok(a, m)) return len_series(a, m);
-    const float a1 = 1.0f / (2.0f * z * m);
-    return (a1 / (a * a)) * (1.0f - cosf(m * atanf(2.0f * a)) / powp1f(4.0f * a * a, m / 2.0f));
+    const float x = 4.0f * a * a;
+    const float c = cosf(m * atanf(2.0f * a));
+    const float ipw = exp2f((-0.5f * m) * (log1pf(x) * LOG2E_F));
+    return a4 * fmaf(-c, ipw, 1.0f) / x;
 }
 
 // the same with a relative error estimate (see the asymptotes above)
@@ -302,6 +305,8 @@ struct ChiArgsF {
     float qx, qy, lz;  // lz = l/(z+1)
     float z;
     float b;           // upper chi limit
+    float a4;          // 2/(z(z-1)) of the length factor
+    double qxs, qys;   // the FP64 arguments, for the FP64 fallback of one integral
     float p11, p12, p13, p21, p22, p23;
     int i1;
 };
@@ -330,7 +335,7 @@ __device__ __forceinline__ float chi_integrand_f(const ChiArgsF &A, float cx, fl
     }
     const float a = s * A.lz;
     if (fabsf((A.z - 1.0f) * a) < 1e-4f) guard = true;
-    return cyl_len_factor(a, A.z);
+    return cyl_len_factor(a, A.z, A.a4);
 }
 
 // Neville extrapolation to 0 of the last five trapezoid estimates, whose
@@ -417,9 +422,33 @@ __device__ float qromb_chi_f(const Ctx &C, const ChiArgsF &A, float cd, float sd
         KahanF sum;
         if (j <= CS_NODE_LEVELS) {
             const cs_chi_node_f *nd = nf + CS_NODE_OFFSET(j);
-            for (int k = 0; k < cnt; k++) {
-                const cs_chi_node_f n = nd[k];
-                sum.add(chi_integrand_f(A, n.c, n.s, cd, sd, guard));
+            if ((A.i1 == 2 || A.i1 == 3) && cnt >= 4) {
+                // the axis-along-x/y integrands depend on sin(chi) alone, and
+                // the nodes of a level come in pairs chi, pi - chi (3 pi - chi
+                // in the upper half) up to the rounding of the limit 2 pi to
+                // FP32 (their sines differ by < 1e-7): one evaluation at the
+                // pair's mean sine stands for both (second-order error ~1e-14)
+                const int qn = cnt >> 2;
+                for (int h = 0; h < 2; h++) {
+                    const cs_chi_node_f *hn = nd + h * 2 * qn;
+                    for (int k = 0; k < qn; k++) {
+                        const float sm = 0.5f * (hn[k].s + hn[2 * qn - 1 - k].s);
+                        sum.add(2.0f * chi_integrand_f(A, 0.0f, sm, cd, sd, guard));
+                    }
+                }
+            } else if (A.i1 == 4 && cnt >= 2) {
+                // axis along z: the integrand is even in its argument, which
+                // changes sign from chi to chi + pi (node k to k + cnt/2)
+                const int hn = cnt >> 1;
+                for (int k = 0; k < hn; k++) {
+                    const cs_chi_node_f u = nd[k], v = nd[k + hn];
+                    sum.add(2.0f * chi_integrand_f(A, 0.5f * (u.c - v.c), 0.5f * (u.s - v.s), cd, sd, guard));
+                }
+            } else {
+                for (int k = 0; k < cnt; k++) {
+                    const cs_chi_node_f n = nd[k];
+                    sum.add(chi_integrand_f(A, n.c, n.s, cd, sd, guard));
+                }
             }
         } else {
             const double del = (double)b / cnt;
@@ -498,6 +527,89 @@ __device__ double qromb_delta_f(const Ctx &C, const ChiArgsF &A, bool &guard) {
         win[4] = cur;
         if (j >= 5 && romb_stop(win, pq, 1.0e-100, guard)) break;
     }
+    return pq;
+}
+
+// The outer (delta) quadrature for the warp-level redo of one guarded pixel:
+// the delta nodes of a level spread over the lanes, each lane's inner
+// integral in FP32; an inner integral whose FP32 form is in its guard band is
+// recomputed by the whole warp in FP64 (cs64::qromb_chi_warp on the FP64
+// arguments: the FP64 path's value). Every lane returns the same value and
+// guard; what stays guarded (the outer decision, a non-finite value) is left
+// to the exact FP64 pixel.
+__device__ double qromb_delta_warp_f(const Ctx &C, const ChiArgsF &A, bool &guard) {
+    if (A.i1 < 1 || A.i1 > 4) return 0.0;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const cs_prepared &P = *C.P;
+    const double b = P.romb_delta_b;
+    const double inv2pi = 1.0 / (2.0 * M_PI);
+    const cs64::ChiArgs A64 = cs64::chi_args(P, A.qxs, A.qys, P.sigmal, A.i1);
+    bool bad = false;
+    // inner integral of this lane's node (c, s) when active; guarded ones in FP64 by the warp
+    auto node_value = [&](bool active, double c, double s) -> double {
+        bool g = false;
+        double v = 0.0;
+        if (active) v = qromb_chi_f(C, A, (float)c, (float)s, g);
+        unsigned m = __ballot_sync(full, g);
+        while (m) {
+            const int l = __ffs(m) - 1;
+            m &= m - 1;
+            const double cl = __shfl_sync(full, c, l), sl = __shfl_sync(full, s, l);
+            const double w = cs64::qromb_chi_warp(C, A64, cl, sl);
+            if (lane == l) v = w;
+        }
+        if (active && !isfinite(v)) bad = true;
+        return v;
+    };
+    double cur;
+    {
+        const bool act = lane < 2;
+        const cs_delta_node n = C.dnode[act ? lane : 0];
+        const double v = node_value(act, n.c, n.s);
+        const double c0 = __shfl_sync(full, v, 0), c1 = __shfl_sync(full, v, 1);
+        cur = 0.5 * b * (C.dnode[0].w * c0 * inv2pi + C.dnode[1].w * c1 * inv2pi);
+    }
+    double win[5];
+    win[4] = cur;
+    int cnt = 1;
+    double rcnt = 1.0, pq = 0.0;
+    for (int j = 2; j <= 20; j++) {
+        double sump = 0.0;
+        if (j <= CS_NODE_LEVELS) {
+            const cs_delta_node *nd = C.dnode + CS_NODE_OFFSET(j);
+            for (int base = 0; base < cnt; base += 32) {
+                const bool act = base + lane < cnt;
+                const cs_delta_node n = nd[act ? base + lane : 0];
+                const double v = node_value(act, n.c, n.s);
+                const double px = act ? n.w * v * inv2pi : 0.0;
+                const int m = (cnt - base) < 32 ? (cnt - base) : 32;
+                for (int u = 0; u < m; u++) sump += __shfl_sync(full, px, u);
+            }
+        } else {
+            // beyond the node table (not reached in practice): node by node
+            const double dbeta = P.romb_dbeta;
+            const double del = b / cnt;
+            double x = 0.5 * del;
+            for (int k = 0; k < cnt; k++) {
+                double sn, cs;
+                sincos(x, &sn, &cs);
+                const double v = __shfl_sync(full, node_value(lane == 0, cs, sn), 0);
+                sump += sn * exp(-x * x / (dbeta * dbeta)) * v * inv2pi;
+                x += del;
+            }
+        }
+        cur = 0.5 * (cur + b * sump * rcnt);
+        cnt *= 2;
+        rcnt *= 0.5;
+        win[0] = win[1];
+        win[1] = win[2];
+        win[2] = win[3];
+        win[3] = win[4];
+        win[4] = cur;
+        if (j >= 5 && romb_stop(win, pq, 1.0e-100, guard)) break;
+    }
+    if (__any_sync(full, bad)) guard = true;
     return pq;
 }
 
@@ -731,7 +843,7 @@ __device__ double sphere_fq_mixed(const cs_prepared &P, double q, bool &guard, d
 }
 
 // formpq_partCylinder, ordis 0 and 6, cs 0 (mixed)
-template <bool LAT>
+template <bool LAT, bool WARP = false>
 __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, bool &guard, double &err) {
     const cs_prepared &P = *C.P;
     if (P.cs != 0) {
@@ -778,6 +890,7 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             A.qx = (float)qxs;
             A.qy = (float)qys;
             A.lz = (float)(P.length / (z + 1));
+            A.a4 = (float)(2.0 / (z * (z - 1)));
             A.z = (float)z;
             A.p11 = (float)P.romb_p[0];
             A.p12 = (float)P.romb_p[1];
@@ -787,7 +900,9 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             A.p23 = (float)P.romb_p[5];
             A.i1 = P.orcase;
             A.b = (float)P.romb_chi_b;
-            pql = qromb_delta_f(C, A, guard) / P.norm;
+            A.qxs = qxs;
+            A.qys = qys;
+            pql = (WARP ? qromb_delta_warp_f(C, A, guard) : qromb_delta_f(C, A, guard)) / P.norm;
             el = EPS_PQ;
         }
     } else {
@@ -868,6 +983,7 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             A.qx = (float)qxs;
             A.qy = (float)qys;
             A.lz = (float)(P.length / (z + 1));
+            A.a4 = (float)(2.0 / (z * (z - 1)));
             A.z = (float)z;
             A.p11 = (float)P.romb_p[0];
             A.p12 = (float)P.romb_p[1];
@@ -877,6 +993,8 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             A.p23 = (float)P.romb_p[5];
             A.i1 = P.orcase;
             A.b = (float)P.romb_chi_b;
+            A.qxs = qxs;
+            A.qys = qys;
             pql = qromb_delta_f(C, A, guard) / P.norm;
             el = EPS_PQ;
         }
@@ -936,7 +1054,7 @@ __device__ __forceinline__ double lattice_combine(const cs_prepared &P, double q
     return res;
 }
 
-template <int KEY>
+template <int KEY, bool WARP = false>
 __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double qy, double qz, bool &guard) {
     const cs_prepared &P = *C.P;
     const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
@@ -957,9 +1075,9 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
     if (KEY == CS_KEY_CYL_NONE_GAUSS) {
         double pq;
         if (P.orcase == CS_ORC_GENERAL)
-            pq = cyl_pq_mixed<false>(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q, guard, ep);
+            pq = cyl_pq_mixed<false, WARP>(C, qx * P.cosphic - qy * P.sinphic, qx * P.sinphic + qy * P.cosphic, q, guard, ep);
         else
-            pq = cyl_pq_mixed<false>(C, qx, qy, q, guard, ep);
+            pq = cyl_pq_mixed<false, WARP>(C, qx, qy, q, guard, ep);
         if (!(ep <= 5e-6)) guard = true;
         return P.base + P.izero * (pq + P.iso) + tailv;
     }
@@ -1012,7 +1130,16 @@ __global__ void __launch_bounds__(256) k_image_mixed(Ctx C, PeakTab T, double *_
                                                       int redo_cap) {
     const cs_prepared &P = *C.P;
     const int xstride = P.xmax - P.xmin;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < npix; t += (long)gridDim.x * blockDim.x) {
+    // persistent warps take 32-pixel chunks from redo_count[1] (zeroed with
+    // the redo counter): balanced however unevenly the pixel cost varies
+    int *next = redo_count + 1;
+    for (;;) {
+        int base = 0;
+        if ((threadIdx.x & 31) == 0) base = atomicAdd(next, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if ((long)base >= npix) break;
+        const long t = (long)base + (threadIdx.x & 31);
+        if (t >= npix) continue;
         const int ihex = P.zzmin + (int)(t % nx);
         const int i = P.iimin + (int)(t / nx);
         double qx, qy, qz;
@@ -1058,6 +1185,62 @@ __global__ void __launch_bounds__(CS_BATCH_TILE) k_batch_mixed(const cs::BatchSe
             const int pos = atomicAdd(redo_count, 1);
             if (pos < redo_cap) redo_list[pos] = make_int2(k, (int)t);
         }
+    }
+}
+
+// Redo of the guarded pixels of the orientation-averaged cylinder, one pixel
+// per warp (qromb_delta_warp_f): most of them only had an inner integral in its
+// guard band, which the warp recomputes in FP64; the rest run the exact FP64
+// pixel with the warp over the delta nodes (cs64::calc_cyl_none_gauss<true>).
+// Where the geometry or thresholds matter, q is the FP64 path's own.
+__global__ void __launch_bounds__(128) k_redo_cyl_warp(Ctx C, double *__restrict__ out, int nx,
+                                                        const int *__restrict__ redo_count,
+                                                        const int *__restrict__ redo_list, int redo_cap) {
+    const cs_prepared &P = *C.P;
+    const int xstride = P.xmax - P.xmin;
+    int n = *redo_count;
+    if (n > redo_cap) n = redo_cap;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    const PeakTab T{};
+    for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += nw) {
+        const long t = redo_list[r];
+        const int ihex = P.zzmin + (int)(t % nx);
+        const int i = P.iimin + (int)(t / nx);
+        double qx, qy, qz;
+        cs64::convert_idx2q(P, ihex, i, qx, qy, qz);
+        bool guard = false;
+        double v = calc_mixed<CS_KEY_CYL_NONE_GAUSS, true>(C, T, qx, qy, qz, guard);
+        if (__any_sync(0xffffffffu, guard)) v = cs64::calc_cyl_none_gauss<true>(C, qx, qy, qz);
+        if (lane == 0) out[(long)(ihex - P.xmin) + (long)xstride * (long)(i - P.ymin)] = v;
+    }
+}
+
+// the same for the (set, pixel) redo list of a batch group
+__global__ void __launch_bounds__(128) k_batch_redo_cyl_warp(const cs::BatchSetDev *__restrict__ sets,
+                                                              const cs_chi_node *__restrict__ chi,
+                                                              double *__restrict__ out,
+                                                              const int *__restrict__ redo_count,
+                                                              const int2 *__restrict__ redo_list, long redo_cap) {
+    long n = *redo_count;
+    if (n > redo_cap) n = redo_cap;
+    const int lane = threadIdx.x & 31;
+    const long nw = ((long)gridDim.x * blockDim.x) >> 5;
+    const PeakTab T{};
+    for (long r = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += nw) {
+        const int2 e = redo_list[r];
+        const cs::BatchSetDev &S = sets[e.x];
+        const cs_prepared &P = *S.prep;
+        const Ctx C{S.prep, chi, S.delta};
+        const long t = e.y;
+        const int ihex = P.zzmin + (int)(t % S.nx);
+        const int i = P.iimin + (int)(t / S.nx);
+        double qx, qy, qz;
+        cs64::convert_idx2q(P, ihex, i, qx, qy, qz);
+        bool guard = false;
+        double v = calc_mixed<CS_KEY_CYL_NONE_GAUSS, true>(C, T, qx, qy, qz, guard);
+        if (__any_sync(0xffffffffu, guard)) v = cs64::calc_cyl_none_gauss<true>(C, qx, qy, qz);
+        if (lane == 0) out[S.out_offset + (long)(ihex - P.xmin) + (long)(P.xmax - P.xmin) * (long)(i - P.ymin)] = v;
     }
 }
 
@@ -1129,12 +1312,22 @@ static void launch_mixed_key(const DevSet &D, const csm::PeakTab &T, const cs_pr
     const int nx = P.zzmax - P.zzmin;
     const long npix = (long)nx * (long)(P.iimax - P.iimin);
     cs64::Ctx C{D.d_prep, D.d_chi, D.d_delta};
+    // persistent grid: the resident blocks of every SM (warps take work from
+    // a counter), fewer when the image is small
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, csm::k_image_mixed<KEY>, 256, 0);
+        if (per_sm < 1) per_sm = 1;
+    }
     const long need = (npix + 255) / 256;
-    const long cap = (long)sm_count_m() * 8;
+    const long cap = (long)sm_count_m() * per_sm;
     const int grid = (int)(need < cap ? (need < 1 ? 1 : need) : cap);
-    cudaMemsetAsync(S.d_count, 0, sizeof(int), s);
+    cudaMemsetAsync(S.d_count, 0, 2 * sizeof(int), s);  // redo counter and pixel queue
     csm::k_image_mixed<KEY><<<grid, 256, 0, s>>>(C, T, d_out, nx, npix, S.d_count, S.d_list, S.cap);
-    launch_redo(D, P, d_out, S, s);
+    if (KEY == CS_KEY_CYL_NONE_GAUSS)
+        csm::k_redo_cyl_warp<<<sm_count_m() * 4, 128, 0, s>>>(C, d_out, nx, S.d_count, S.d_list, S.cap);
+    else
+        launch_redo(D, P, d_out, S, s);
 }
 
 int launch_image_mixed(const DevSet &D, const csm::PeakTab &T, const cs_prepared &P, double *d_out, MixedScratch &S,
@@ -1142,6 +1335,7 @@ int launch_image_mixed(const DevSet &D, const csm::PeakTab &T, const cs_prepared
     const int nx = P.zzmax - P.zzmin, ny = P.iimax - P.iimin;
     if (nx <= 0 || ny <= 0) return CS_OK;
     if (P.twin) return CS_ERR_UNSUPPORTED;
+    if ((long)nx * (long)ny > (1L << 30)) return CS_ERR_SIZE;  // the pixel queue counts in int
     switch (P.key) {
     case CS_KEY_SPHERE_NONE_ISO: launch_mixed_key<CS_KEY_SPHERE_NONE_ISO>(D, T, P, d_out, S, s); break;
     case CS_KEY_SPHERE_GAUSS_FCC_GAUSS: launch_mixed_key<CS_KEY_SPHERE_GAUSS_FCC_GAUSS>(D, T, P, d_out, S, s); break;
@@ -1173,6 +1367,10 @@ int launch_batch_mixed(const BatchSetDev *d_sets, const BatchGroup &g, int group
     default: return CS_ERR_UNSUPPORTED;
     }
     if (cudaGetLastError() != cudaSuccess) return CS_ERR_CUDA;
+    if (g.key == CS_KEY_CYL_NONE_GAUSS) {
+        csm::k_batch_redo_cyl_warp<<<sm_count_m() * 4, 128, 0, s>>>(d_sets, d_chi, d_out, cnt, list, R.cap);
+        return cudaGetLastError() == cudaSuccess ? CS_OK : CS_ERR_CUDA;
+    }
     return launch_batch_redo(d_sets, g.key, d_chi, d_out, cnt, list, R.cap, s);
 }
 

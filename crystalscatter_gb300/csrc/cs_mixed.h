@@ -31,7 +31,7 @@ namespace cs {
 
 // Redo list of the mixed kernels (pixels recomputed in FP64).
 struct MixedScratch {
-    int *d_count = nullptr;
+    int *d_count = nullptr;  // [0] redo counter, [1] pixel queue of the mixed kernel
     int *d_list = nullptr;
     int cap = 0;
 };

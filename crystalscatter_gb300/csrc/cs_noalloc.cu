@@ -13,7 +13,7 @@
 
 #include "cs_noalloc.h"
 
-static __device__ __align__(256) int g_noalloc_count[64];  // [0] is the counter; padded to 256 B
+static __device__ __align__(256) int g_noalloc_count[64];  // [0] redo counter, [1] pixel queue; padded to 256 B
 static __device__ __align__(256) int g_noalloc_list[CS_NOALLOC_MAX_PIXELS];
 
 namespace cs {
