@@ -161,6 +161,13 @@ def fp_peaks():
             "sms": sms, "sm_mhz": mhz, "kind": "nominal (SMs x lanes x max clock)"}
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the headline kernel, k_image_mixed on the 512x512 cylinder, from an ncu
+# capture of three launches on a GB300 (the image stays in L2 during the
+# launch and reaches DRAM after it)
+TRAFFIC_BYTES_PER_LAUNCH = 101888
+
+
 def load_ops():
     p = os.path.join(ROOT, "crystalscatter_gb300", "config_ops.json")
     with open(p) as f:
@@ -367,7 +374,7 @@ def native(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(calc._lib.cs_prepared_size()),
                 "d2h_bytes_per_step": int(8 * n), "host_prep_ms": prep_ms},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak, "traffic": TRAFFIC_BYTES_PER_LAUNCH,
                      "note": f"peak {peak_kind}; 8 B written per pixel: the kernels are bound by arithmetic, "
                              f"see compute_roofline and profiles/"},
         "compute_roofline": {"flops_per_pixel": fl, "achieved_tflops": value * fl / 1e12,

@@ -707,6 +707,10 @@ __device__ inline double calc_sphere_none_iso(const Ctx &C, double qx, double qy
 
 // Peak sums shared by the FCC and BCT kernels
 // (Source/sc_gpu_pSph_pGau_lFCC_oGau.h:53-143, sc_gpu_pCyl_pGau_lBCT_oZDi.h:133-211).
+// exp(-4 x2/pi) is exactly +0 for x2 above ~585 (its argument below the
+// smallest subnormal's log, -744.4): such peak terms add exactly nothing
+constexpr double kPeakZero = 600.0;
+
 __device__ inline void peak_sums(const cs_prepared &P, double qx, double qy, double qz, double q, double &radintensity,
                           double &intensity) {
     double width = 1;
@@ -722,6 +726,7 @@ __device__ inline void peak_sums(const cs_prepared &P, double qx, double qy, dou
         if (mhkl == 0 || fhkl == 0) continue;
         const double qhkl = P.latpar3[ii][5];
         const double x2 = sqr(q - qhkl) / sqr(widthiso);
+        if (x2 > kPeakZero) continue;  // the term is exactly +0
         const double sq = exp(-4 * x2 / M_PI) / (M_PI * widthiso / 2.0);
         radintensity += sq * mhkl * fhkl;
     }
@@ -735,8 +740,11 @@ __device__ inline void peak_sums(const cs_prepared &P, double qx, double qy, dou
             const double qzhkl = P.latpar3[ii][4];
             const double g3 = P.latpar3[ii][10];
             const double peaknorm1 = P.latpar3[ii][11];
-            const double yphi = myacos((qx * qxhkl + qy * qyhkl + qz * qzhkl) / (q * qhkl));
             const double x2 = (q - qhkl) * (q - qhkl) / (width * width);
+            // a term whose radial Gaussian underflows is exactly +0 when its
+            // angular factor is finite: skipped (same sum, bit for bit)
+            if (x2 > kPeakZero && !P.twin && isfinite(g3) && isfinite(peaknorm1) && peaknorm1 != 0) continue;
+            const double yphi = myacos((qx * qxhkl + qy * qyhkl + qz * qzhkl) / (q * qhkl));
             const double sq = exp(-4 * x2 / M_PI) / (M_PI * width / 2.0);
             double psiord = g3 * exp(-x2phi * yphi * yphi) / peaknorm1;
             if (P.twin) {

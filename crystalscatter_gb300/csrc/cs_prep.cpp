@@ -641,13 +641,22 @@ bool Prep::coefficients() {
                     xln[n] = xln_n;
                     xrn[n] = xrn_n;
                 }
+                // pw11/pw13 are powers of numbers <= 1: once a power underflows
+                // to 0 all higher ones are 0, and so is every numerator that
+                // uses them (skipped below in any case): the ll loop runs over
+                // the window where both powers are non-zero
+                int e11 = nmax, e13 = nmax;
+                while (e11 > 0 && pw11[e11] == 0.0) e11--;
+                while (e13 > 0 && pw13[e13] == 0.0) e13--;
                 parallel_n(1, nmax, [&](int n) {
                     const long double xln_n = xln[n];
                     const double xrn_n = xrn[n];
                     for (int m = 0; m <= n; m++) {
                         double sump = 0.0;
                         double lim = lim0;  // negligible_lg2(sump)
-                        for (int ll = 0; ll <= m; ll++) {
+                        const int ll_lo = m - e13 > 0 ? m - e13 : 0;
+                        const int ll_hi = m < e11 ? m : e11;
+                        for (int ll = ll_lo; ll <= ll_hi; ll++) {
                             const double num = pw11[ll] * pw13[m - ll] * intl_const;
                             // a zero numerator adds exactly 0 (the long-double
                             // denominator is finite and non-zero): skipped
