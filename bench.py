@@ -53,6 +53,25 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(values, world, device):
+    """Per-rank timings reduced to their maximum over the ranks (the job's
+    time: every rank waits for the slowest); the values themselves on one
+    rank."""
+    if world <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def replica_rate(units_per_rank, world, seconds):
+    """Whole-job rate of `world` independent replicas that each process
+    units_per_rank units, over the slowest replica's time."""
+    return units_per_rank * world / seconds
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -345,14 +364,10 @@ def native(args):
     t_e2e = time.perf_counter() - t0
     prep_ms = calc.higResTimerElapsedPrep
     clk = clocks.stop()
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_kernel, t_e2e, t_fp64], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_kernel, t_e2e, t_fp64 = tt.tolist()
+    t_kernel, t_e2e, t_fp64 = max_over_ranks([t_kernel, t_e2e, t_fp64], world, "cuda")
 
-    value = npix * args.steps * world / t_kernel
-    e2e = npix * args.steps * world / t_e2e
+    value = replica_rate(npix * args.steps, world, t_kernel)
+    e2e = replica_rate(npix * args.steps, world, t_e2e)
     ms_per_step = 1e3 * t_kernel / args.steps
 
     # roofline: algorithmic HBM bytes per launch = the image (8 B per pixel)
