@@ -861,6 +861,42 @@ __device__ inline double formpq_cube(const cs_prepared &P, double q) {
     return P.por / (q * q * q * q);
 }
 
+// One term of polyvesicle: the averaged sin²/sincos/cos² moment of a
+// Schulz-distributed size, cos or sin of zm·atan(2y) over (1+4y²)^(zm/2),
+// with the exponent zm = z - k + 1 formed by the caller.
+__device__ inline double vesicle_moment(double zm, double y, bool use_sin) {
+    const double a = zm * atan(2. * y);
+    const double t = use_sin ? sin(a) : cos(a);
+    return t / exp(zm * log(1. + 4. * y * y) / 2.);
+}
+
+// polyvesicle, Schulz-polydisperse hollow shell between radius (inner) and
+// length (outer) with polydispersities sigma (radius) and sigmal (thickness),
+// Source/sc_calc_generic_gpu.cu:698-727
+__device__ inline double polyvesicle(const cs_prepared &P, double q) {
+    const double r = (P.length + P.radius) / 2.;
+    if (q * r < 0.001) return 1;
+    const double d = (P.length - P.radius) / 2.;
+    const double zr = (1. - sqr(P.sigma)) / sqr(P.sigma);
+    const double zd = (1. - sqr(P.sigmal)) / sqr(P.sigmal);
+    const double yr = q * r / (zr + 1.);
+    const double yd = q * d / (zd + 1.);
+    const double c = 1. + d * d / (12. * r * r);
+    const double gr1 = 1. / (2. * zr * (zr - 1.) * yr * yr);
+    const double gr2 = gr1 / ((zr - 2.) * yr);
+    const double gr3 = gr2 / ((zr - 3.) * yr);
+    const double gd1 = 1. / (2. * zd * (zd - 1.) * yd * yd);
+    const double gd2 = 1. / (2. * zd * yd);
+    const double gd3 = 1. / 2.;
+    const double hr1 = gr1 * (1. - vesicle_moment(zr - 2. + 1., yr, false));
+    const double hr2 = gr2 * vesicle_moment(zr - 3. + 1., yr, true);
+    const double hr3 = gr3 * (1. + vesicle_moment(zr - 4. + 1., yr, false));
+    const double hd1 = gd1 * (1. - vesicle_moment(zd - 2. + 1., yd, false));
+    const double hd2 = gd2 * vesicle_moment(zd - 1. + 1., yd, true);
+    const double hd3 = gd3 * (1. + vesicle_moment(zd + 0. + 1., yd, false));
+    return (hr1 * hd1 - 2. * hr2 * hd2 + 2. * hr2 * hd1 + hr3 * hd3 - 2. * hr3 * hd2 + hr3 * hd1) / (c * c);
+}
+
 // calc_partCube_lattNone_ordisIsotropic, Source/sc_gpu_pCub_lNon_oIso.h:16-77
 __device__ inline double calc_cube_none_iso(const Ctx &C, double qx, double qy, double qz) {
     const cs_prepared &P = *C.P;
@@ -869,9 +905,88 @@ __device__ inline double calc_cube_none_iso(const Ctx &C, double qx, double qy, 
     return P.base + P.izero * (pq + P.iso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
 }
 
+// formpq_partDisk, homogeneous disk, ordis 7 and 6 with its transverse part,
+// Source/sc_lib_formpq_partDisk.h:8-136 and :310-340. orcase is compared with
+// 1..4 as the reference compares it, although its enum is 0-based (1 = x
+// axis, 2 = y axis, 3 = z axis): the x axis takes the sum of qxs and qys, the
+// y axis qxs (which is 0 there), the z axis qys (= qy, not divided by q). The
+// general case (0) takes no series branch and reads an uninitialised argument
+// in the closed form; the preparation does not offer it.
+__device__ inline double formpq_disk(const cs_prepared &P, double limql, double qxs, double qys, double q, int ordis) {
+    const double zl = (1 - sqr(P.sigmal)) / sqr(P.sigmal);
+    const double zr = (1 - sqr(P.sigma)) / (sqr(P.sigma));
+    const double *c1 = P.carrp[0];
+    double pql = 0, pqr;
+    if (ordis == 7) {
+        if (q < (0.5 * P.limq[1])) {
+            pql = 1.0;
+            double oldpqsum = 0.0, qqnn = 1.0;
+            for (int nser = 1; nser <= 80; nser++) {
+                qqnn = qqnn * q * q;
+                pql += c1[nser] * qqnn;
+                if (series_converged(pql, oldpqsum)) break;
+                oldpqsum = pql;
+            }
+        } else {
+            const double arglq = q * P.length / (zl + 1);
+            pql = (2 / (zl * (zl - 1))) * pow(arglq, -2);
+        }
+    }
+    if (ordis == 6) {
+        if ((limql * P.length) < 5.0) {
+            pql = 1.0;
+            double oldpqsum = 0.0, qqnn = 1.0;
+            // the factor (1 - w^2)^n of orcase 1..3 (none for 4)
+            const double w = P.orcase == 1 ? qxs + qys : (P.orcase == 2 ? qxs : qys);
+            for (int nser = 1; nser <= 120; nser++) {
+                qqnn = qqnn * q * q;
+                if (P.orcase == 4)
+                    pql += c1[nser] * qqnn;
+                else if (P.orcase >= 1 && P.orcase <= 3)
+                    pql += c1[nser] * qqnn * pow(1.0 - w * w, nser);
+                else
+                    break;  // orcase 0: no branch, pql stays 1
+                if (series_converged(pql, oldpqsum)) break;
+                oldpqsum = pql;
+            }
+        } else {
+            double arglq = 0;
+            if (P.orcase == 1) {
+                const double qnarg = qxs + qys;
+                arglq = sqrt(1.0 - qnarg * qnarg) * q * P.length / (zl + 1) + CS_EPS9;
+            }
+            if (P.orcase == 2) arglq = sqrt(1.0 - qxs * qxs) * q * P.length / (zl + 1) + CS_EPS9;
+            if (P.orcase == 3) arglq = sqrt(1.0 - qys * qys) * q * P.length / (zl + 1) + CS_EPS9;
+            if (P.orcase == 4) arglq = q * P.length / (zl + 1) + CS_EPS9;
+            const double pqr1 = (1 / (zl * (zl - 1) * (zl - 2))) * pow(arglq, -3);
+            const double pqr2 = (1 / (zl * (zl - 1) * (zl - 2))) * pow(arglq, -3) * sin((zl - 2) * atan(2.0 * arglq)) /
+                                pow(1.0 + 4 * arglq * arglq, (zl - 2) / 2.0);
+            const double pqr3 = (1 / (zl * (zl - 1) * (zl - 2) * (zl - 3))) * pow(arglq, -4) *
+                                cos((zl - 3) * atan(2.0 * arglq)) / pow(1.0 + 4 * arglq * arglq, (zl - 3) / 2.0);
+            pql = (4 / M_PI) * (pqr1 - pqr2 - (9 / 8.0) * pqr3);
+        }
+    }
+    if (q < (0.5 * P.limq[4])) {
+        pqr = 1.0;
+        double oldpqsum = 0.0, qqnn = 1.0;
+        for (int nser = 1; nser <= 100; nser++) {
+            qqnn = qqnn * q * q;
+            pqr += P.carrp[3][nser] * qqnn;
+            if (series_converged(pqr, oldpqsum)) break;
+            oldpqsum = pqr;
+        }
+    } else {
+        const double argpq = q * P.radius / (zr + 1);
+        pqr = (1 / (2.0 * zr * (zr - 1))) * pow(argpq, -2) *
+              (1 - cos((zr - 1) * atan(2.0 * argpq)) / pow(1.0 + 4 * argpq * argpq, (zr - 1) / 2.0));
+    }
+    return pql * pqr;
+}
+
 // calc_GENERIC, Source/sc_gpu_generic.h:27-881, for the particles the
 // preparation supports (spheres, cylinders with z-direction or Gaussian
-// orientation, homogeneous isotropic cubes), any supported lattice and the
+// orientation, z-direction disks along an axis without a lattice, vesicles,
+// homogeneous isotropic cubes), any supported lattice and the
 // peak shapes 1-7 (the reference's shape 7 falls to its `default: return 0`).
 __device__ inline double calc_generic(const Ctx &C, double qx, double qy, double qz) {
     const cs_prepared &P = *C.P;
@@ -926,6 +1041,18 @@ __device__ inline double calc_generic(const Ctx &C, double qx, double qy, double
                 break;
             }
         }
+    } else if (P.particle == 2) {  // disks, :173-225 (z-direction, axis cases; no lattice)
+        if (P.ordis == 6) {
+            switch (P.orcase) {
+            case CS_ORC_XAXIS: pq = formpq_disk(P, fabs(qy), qx / q, 0, q, 6); break;
+            case CS_ORC_YAXIS: pq = formpq_disk(P, fabs(qx), 0, qy / q, q, 6); break;
+            case CS_ORC_ZAXIS: pq = formpq_disk(P, q, qx, qy, q, 6); break;
+            }
+        }
+        pqiso = (P.iso > 0) ? formpq_disk(P, q, qx, qy, q, 7) : 0.0;
+    } else if (P.particle == 3) {  // vesicles, :271-277
+        pq = polyvesicle(P, q);
+        fq = pq;
     } else if (P.particle == 4) {  // cubes, :291-320
         pq = formpq_cube(P, q);
         fq = pq;

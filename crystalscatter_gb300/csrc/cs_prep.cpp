@@ -1895,10 +1895,13 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
                           P.key == CS_KEY_CYL_GAUSS_BCT_ZDIR || P.key == CS_KEY_CUBE_NONE_ISO);
     if (!special) {
         // the generic pixel function covers the particles prepared above:
-        // spheres, cylinders (z-direction, Gaussian orientation) and
-        // homogeneous isotropic cubes
+        // spheres, cylinders (z-direction, Gaussian orientation), homogeneous
+        // isotropic cubes, z-direction disks along an axis without a lattice,
+        // and isotropic or z-direction vesicles
         const bool ok = P.particle == 0 || (P.particle == 1 && (P.ordis == 6 || P.ordis == 0)) ||
-                        (P.particle == 4 && P.ordis == 7 && P.cs == 0);
+                        (P.particle == 4 && P.ordis == 7 && P.cs == 0) ||
+                        (P.particle == 2 && P.ordis == 6 && P.cs == 0 && !P.lattice && P.orcase != CS_ORC_GENERAL) ||
+                        (P.particle == 3 && (P.ordis == 7 || P.ordis == 6));
         if (!ok) {
             err = "generic pixel function: particle " + std::to_string(P.particle) + " with ordis " +
                   std::to_string(P.ordis) + " is not implemented";

@@ -85,6 +85,14 @@ def image_cases():
     cases["sphere_fcc_ignswitch_g24"] = dict(sph)
     cases["cyl_zdir_fcc_g24"] = dict(C.scaled(C.bct_set(2), 24), LType=5)
     cases["cyl_gauss_x_ignswitch_g16"] = C.scaled(C.CYL_GAUSS_X, 16)
+    disk = dict(C.scaled(C.CYL_GAUSS, 32), ComboBoxParticle=2, Ordis=6, EditRadius=2.0, Length=30.0)
+    cases["disk_zdir_x_g32"] = dict(disk, phi=0.0, theta=90.0)
+    cases["disk_zdir_y_g32"] = dict(disk, phi=90.0, theta=90.0)
+    cases["disk_zdir_z_iso_g32"] = dict(disk, phi=0.0, theta=0.0, iso=0.3)
+    ves = dict(C.scaled(C.SPHERE, 32), ComboBoxParticle=3, Length=14.0, SigmaL=0.15)
+    cases["vesicle_iso_g32"] = dict(ves, iso=0.2)
+    cases["vesicle_zdir_g32"] = dict(ves, Ordis=6)
+    cases["vesicle_fcc_g24"] = dict(sph, ComboBoxParticle=3, Ordis=7, Length=12.0, SigmaL=0.15)
     return cases
 
 
