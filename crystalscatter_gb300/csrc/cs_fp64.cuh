@@ -897,6 +897,91 @@ __device__ inline double polyvesicle(const cs_prepared &P, double q) {
     return (hr1 * hd1 - 2. * hr2 * hd2 + 2. * hr2 * hd1 + hr3 * hd3 - 2. * hr3 * hd2 + hr3 * hd1) / (c * c);
 }
 
+// Integrand of trapzdchid for the isotropic biaxial ellipsoid, i1 = 13
+// (Source/sc_calc_generic_gpu.cu:2338-2350, :2878-2889): the Schulz-averaged
+// sphere form factor at the ellipsoid's radius seen at angle x from its long
+// axis, times sin(x). The pixel-independent factors are formed once, with the
+// reference's operations.
+struct EllArgs {
+    double qn, r, e2m1, zp1, a1, a1z4, a1z45, zm3, zm4, zm5, zm3h, zm4h, zm5h;
+};
+
+__device__ inline EllArgs ellipsoid_args(const cs_prepared &P, double qx, double qy) {
+    EllArgs A;
+    const double z = (1 - P.sigma * P.sigma) / (P.sigma * P.sigma);
+    const double epsi = P.length / P.radius;
+    A.qn = sqrt(qx * qx + qy * qy + 0.0000000001);
+    A.r = P.radius;
+    A.e2m1 = epsi * epsi - 1;
+    A.zp1 = z + 1;
+    A.a1 = (1 / (2.0 * z * (z - 1) * (z - 2) * (z - 3)));
+    A.a1z4 = A.a1 / (z - 4);
+    A.a1z45 = A.a1 / ((z - 4) * (z - 5));
+    A.zm3 = z - 3;
+    A.zm4 = z - 4;
+    A.zm5 = z - 5;
+    A.zm3h = (z - 3) / 2.0;
+    A.zm4h = (z - 4) / 2.0;
+    A.zm5h = (z - 5) / 2.0;
+    return A;
+}
+
+__device__ inline double ellipsoid_integrand(const EllArgs &A, double x) {
+    double sx, cx;
+    sincos(x, &sx, &cx);
+    const double arg = A.qn * A.r * sqrt(1.0 + A.e2m1 * cx * cx) / A.zp1;
+    const double at = atan(2.0 * arg);
+    const double den = 1.0 + 4 * arg * arg;
+    const double p1 = A.a1 * pow(arg, -4) * (1 + cos(A.zm3 * at) / pow(den, A.zm3h));
+    const double p2 = A.a1z4 * pow(arg, -5) * sin(A.zm4 * at) / pow(den, A.zm4h);
+    const double p3 = A.a1z45 * pow(arg, -6) * (1 - cos(A.zm5 * at) / pow(den, A.zm5h));
+    return 9 * (p1 - 2 * p2 + p3) * sx;
+}
+
+// qrombchid over x in [0, pi/2] (limits stored as float, :1429-1431) with the
+// ellipsoid integrand: trapezoid doubling, Neville extrapolation over the last
+// five estimates, stop at |dss| < 1e-4 |I| or |I| < 1e-300 (:1449-1463).
+__device__ inline double qromb_ellipsoid(const EllArgs &A) {
+    const double a = (double)0.0f, b = (double)(float)(M_PI / 2.0);
+    double win[5];
+    double cur = 0.5 * (b - a) * (ellipsoid_integrand(A, a) + ellipsoid_integrand(A, b));
+    int cnt = 1;
+    double pq = 0.0, dss = 0.0;
+    win[4] = cur;
+    for (int j = 2; j <= 20; j++) {
+        const double tnm = cnt;
+        const double del = (b - a) / tnm;
+        double x = a + 0.5 * del;
+        double sump = 0.0;
+        for (int k = 0; k < cnt; k++) {
+            sump += ellipsoid_integrand(A, x);
+            x += del;
+        }
+        cur = 0.5 * (cur + (b - a) * sump / tnm);
+        cnt = 2 * cnt;
+        win[0] = win[1];
+        win[1] = win[2];
+        win[2] = win[3];
+        win[3] = win[4];
+        win[4] = cur;
+        if (j >= 5) {
+            polint5(win, pq, dss);
+            if (fabs(dss) < (1.0e-4 * fabs(pq))) break;
+            if (fabs(pq) < 1.0e-300) break;
+        }
+    }
+    return pq;
+}
+
+// formpq_partEllips, homogeneous isotropic ellipsoid (ordis 7, cs 0),
+// Source/sc_lib_formpq_partEllips.h:46-86: series below 0.8 limq4, Porod
+// asymptote from 1.5 limq4, the orientation integral in between.
+__device__ inline double formpq_ellipsoid(const cs_prepared &P, double qx, double qy, double q) {
+    if (q < 0.8 * P.limq[4]) return series_q(P.carrp[3], q, 120);
+    if (q >= 1.5 * P.limq[4]) return P.por / (q * q * q * q);
+    return qromb_ellipsoid(ellipsoid_args(P, qx, qy));
+}
+
 // calc_partCube_lattNone_ordisIsotropic, Source/sc_gpu_pCub_lNon_oIso.h:16-77
 __device__ inline double calc_cube_none_iso(const Ctx &C, double qx, double qy, double qz) {
     const cs_prepared &P = *C.P;
@@ -986,7 +1071,7 @@ __device__ inline double formpq_disk(const cs_prepared &P, double limql, double 
 // calc_GENERIC, Source/sc_gpu_generic.h:27-881, for the particles the
 // preparation supports (spheres, cylinders with z-direction or Gaussian
 // orientation, z-direction disks along an axis without a lattice, vesicles,
-// homogeneous isotropic cubes), any supported lattice and the
+// homogeneous isotropic cubes and ellipsoids), any supported lattice and the
 // peak shapes 1-7 (the reference's shape 7 falls to its `default: return 0`).
 __device__ inline double calc_generic(const Ctx &C, double qx, double qy, double qz) {
     const cs_prepared &P = *C.P;
@@ -1052,6 +1137,9 @@ __device__ inline double calc_generic(const Ctx &C, double qx, double qy, double
         pqiso = (P.iso > 0) ? formpq_disk(P, q, qx, qy, q, 7) : 0.0;
     } else if (P.particle == 3) {  // vesicles, :271-277
         pq = polyvesicle(P, q);
+        fq = pq;
+    } else if (P.particle == 5) {  // ellipsoids, isotropic and homogeneous, :322-342
+        pq = formpq_ellipsoid(P, qx, qy, q);
         fq = pq;
     } else if (P.particle == 4) {  // cubes, :291-320
         pq = formpq_cube(P, q);

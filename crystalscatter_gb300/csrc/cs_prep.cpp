@@ -512,6 +512,51 @@ bool Prep::coefficients() {
         } else {
             supported = false;
         }
+    } else if ((P.ordis == 7) && (cdim == 5)) {
+        // isotropic case for ellipsoids, :2966-3021 (semi-axes radius, radius
+        // and length; eps = length/radius, :2166)
+        P.norm = 1;
+        P.order = 0;
+        const double eps = P.length / P.radius;
+        double area;
+        if (eps > 1)
+            area = 2 * M_PI * P.radius *
+                   (P.radius + (sqr(P.length) / std::sqrt(sqr(P.length) - sqr(P.radius))) *
+                                   std::asin(std::sqrt(sqr(P.length) - sqr(P.radius)) / P.length));
+        else if (eps < 1)
+            area = 2 * M_PI * P.radius *
+                   (P.radius + (sqr(P.length) / std::sqrt(sqr(P.radius) - sqr(P.length))) *
+                                   std::asinh(std::sqrt(sqr(P.radius) - sqr(P.length)) / P.length));
+        else
+            area = 4 * M_PI * P.radius * P.radius;
+        const double vol = (4 * M_PI / 3.0) * sqr(P.radius) * P.length;
+        P.por = 2 * M_PI * std::pow(z + 1, 4) * area / (z * (z - 1) * (z - 2) * (z - 3) * vol * vol);
+        if (P.cs == 0) {
+            // Only the P(q) coefficients: the reference's F(q) coefficients
+            // of this case read fsum[1..n] that nothing has written, and the
+            // ellipsoid pixel function takes F(q) = P(q).
+            double e1[kNmax + 1];
+            e1[0] = 1;
+            double z12v_n = 1.0;
+            double xrn_n = 1.0;
+            for (int n = 1; n <= nmax; n++) {
+                z12v_n = z12v_n * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
+                fkv[n] = fkv[n - 1] * n;
+                gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
+                e1[n] = e1[n - 1] * (eps * eps - 1);
+                xrn_n = -xrn_n * xr2z;
+                double sump = 0.0;
+                for (int m = 0; m <= n; m++) sump += e1[n - m] / (fkv[n - m] * fkv[m] * (2 * (n - m) + 1));
+                carr4p[n] = (9 * std::sqrt(M_PI) / 2.0) * std::pow(4.0, n) * z12v_n * xrn_n * sump /
+                            ((n + 3) * (n + 2) * (n + 3 / 2.0) * gam3[n]);
+                if (std::fabs(carr4p[n]) < kMin) {
+                    if (n < n4) n4 = n;
+                }
+            }
+            done = true;
+        } else {
+            supported = false;
+        }
     } else if ((P.ordis == 6) && (cdim != 3)) {
         // perfect orientation for cylinders and disks, :4124-4644
         P.norm = 1;
@@ -1897,11 +1942,13 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
         // the generic pixel function covers the particles prepared above:
         // spheres, cylinders (z-direction, Gaussian orientation), homogeneous
         // isotropic cubes, z-direction disks along an axis without a lattice,
-        // and isotropic or z-direction vesicles
+        // isotropic or z-direction vesicles, and homogeneous isotropic
+        // ellipsoids
         const bool ok = P.particle == 0 || (P.particle == 1 && (P.ordis == 6 || P.ordis == 0)) ||
                         (P.particle == 4 && P.ordis == 7 && P.cs == 0) ||
                         (P.particle == 2 && P.ordis == 6 && P.cs == 0 && !P.lattice && P.orcase != CS_ORC_GENERAL) ||
-                        (P.particle == 3 && (P.ordis == 7 || P.ordis == 6));
+                        (P.particle == 3 && (P.ordis == 7 || P.ordis == 6)) ||
+                        (P.particle == 5 && P.ordis == 7 && P.cs == 0);
         if (!ok) {
             err = "generic pixel function: particle " + std::to_string(P.particle) + " with ordis " +
                   std::to_string(P.ordis) + " is not implemented";

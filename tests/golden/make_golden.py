@@ -93,6 +93,10 @@ def image_cases():
     cases["vesicle_iso_g32"] = dict(ves, iso=0.2)
     cases["vesicle_zdir_g32"] = dict(ves, Ordis=6)
     cases["vesicle_fcc_g24"] = dict(sph, ComboBoxParticle=3, Ordis=7, Length=12.0, SigmaL=0.15)
+    ell = dict(C.scaled(C.SPHERE, 32), ComboBoxParticle=5, Ordis=7)
+    cases["ellipsoid_prolate_g32"] = dict(ell, Length=16.0)
+    cases["ellipsoid_oblate_g32"] = dict(ell, Length=6.0, iso=0.1)
+    cases["ellipsoid_fcc_g24"] = dict(sph, ComboBoxParticle=5, Ordis=7, Length=11.0)
     return cases
 
 

@@ -14,6 +14,16 @@ from helpers import golden, golden_cases, params_struct
 
 CASES = golden_cases()["images"]
 
+# The reference's isotropic-ellipsoid coefficients (Source/sc_calc_generic_cpu.cpp:
+# 3004-3011) build carr4f from fsum[1..n], which nothing in that case writes:
+# its values (and limq4f) are whatever the allocation held. The ellipsoid
+# pixel function takes F(q) = P(q) and reads neither.
+UNINIT_F = {"carr4f", "limq4f"}
+
+
+def _skipped(case, name):
+    return case["params"].get("ComboBoxParticle") == 5 and name in UNINIT_F
+
 ARR = {"carr1p": ("carrp", 0), "carr2p": ("carrp", 1), "carr3p": ("carrp", 2), "carr4p": ("carrp", 3),
        "carr5p": ("carrp", 4), "carr6p": ("carrp", 5), "carr1f": ("carrf", 0), "carr4f": ("carrf", 3),
        "carr5f": ("carrf", 4), "carr6f": ("carrf", 5)}
@@ -36,6 +46,8 @@ def test_prepared_constants_match_reference(name):
     rc, P, msg = prepared.prepare(p, 0, case["ign_cbs"])
     assert rc == 0, msg
     for a, (field, k) in ARR.items():
+        if _skipped(case, a):
+            continue
         ours = np.array(getattr(P, field)[k][:])
         assert _close(g[a], ours, 1e-15), a
     ours11 = np.array(P.carr11pm).reshape(131, 131)
@@ -43,6 +55,8 @@ def test_prepared_constants_match_reference(name):
     for s in ("limq1", "limq2", "limq3", "limq4", "limq5", "limq6"):
         assert _close(g["s_" + s], P.limq[int(s[4:])], 1e-15), s
     for s in ("limq1f", "limq4f"):
+        if _skipped(case, s):
+            continue
         assert _close(g["s_" + s], P.limqf[int(s[4])], 1e-15), s
     assert _close(g["s_norm"], P.norm, 1e-15)
     assert _close(g["s_order"], P.order, 1e-15)
