@@ -46,29 +46,43 @@ __device__ __forceinline__ bool near(double v, double t, double band) { return f
 // Detector geometry. In beam geometry it is taken in FP64 without
 // transcendentals: cos(phi)sin(theta) = xdet/L, sin(phi)sin(theta) = ydet/L,
 // cos(theta) = det/L, L = |(xdet,ydet,det)|, which agrees with the reference's
-// atan2/sin/cos form to a few ulp. The z-direction cylinder keys take the
-// drop-in's own convert_idx2q instead (same rounding: this unit is compiled
-// without contraction, as the drop-in is): their power series in (qx+qy)^2 can
-// cancel by up to 1e15, where a few-ulp change of q moves the reference's own
-// value by O(1), and the mixed path then reproduces the FP64 value exactly
-// instead of a different rounding of it.
+// atan2/sin/cos form to a few ulp; the pixel-independent factors (QGeom) are
+// formed once per thread, which leaves two FP64 divisions per pixel. The
+// z-direction cylinder keys take the drop-in's own convert_idx2q instead (same
+// rounding: this unit is compiled without contraction, as the drop-in is):
+// their power series in (qx+qy)^2 can cancel by up to 1e15, where a few-ulp
+// change of q moves the reference's own value by O(1), and the mixed path then
+// reproduces the FP64 value exactly instead of a different rounding of it.
+struct QGeom {
+    double sy, sx, k;  // pixnoy/(2 zmax), pixnox/(2 zmax), 2 pi/lambda
+};
+
+__device__ __forceinline__ QGeom q_geom(const cs_prepared &P) {
+    QGeom g;
+    g.sy = P.pixnoy / (2.0 * P.zmax);
+    g.sx = P.pixnox / (2.0 * P.zmax);
+    g.k = 2 * M_PI / P.wave;
+    return g;
+}
+
 template <int KEY>
-__device__ __forceinline__ void q_of_pixel(const cs_prepared &P, int ihex, int i, double &qx, double &qy, double &qz) {
+__device__ __forceinline__ void q_of_pixel(const cs_prepared &P, const QGeom &g, int ihex, int i, double &qx,
+                                           double &qy, double &qz) {
     if (KEY == CS_KEY_CYL_NONE_ZDIR || KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR || P.use1d || !P.usebeamstop) {
         cs64::convert_idx2q(P, ihex, i, qx, qy, qz);
         return;
     }
-    const double mdet = (ihex)*P.pixnoy / (2.0 * P.zmax);
-    const double ndet = (i)*P.pixnox / (2.0 * P.zmax);
+    const double mdet = (ihex)*g.sy;
+    const double ndet = (i)*g.sx;
     const double xdet = P.pixx_m * (ndet - P.beamx0);
     const double ydet = P.pixy_m * (mdet - P.beamy0);
     const double r2 = xdet * xdet + ydet * ydet;
     const double L = sqrt(r2 + P.det * P.det);
-    const double k = 2 * M_PI / P.wave;
-    qx = k * xdet / L;
-    qy = k * ydet / L;
+    const double kl = g.k / L;
+    qx = kl * xdet;
+    qy = kl * ydet;
     // 1 - cos(theta) = r^2 / (L (L + det)), free of cancellation
-    qz = k * r2 / (L * (L + P.det));
+    qz = kl * r2 / (L + P.det);
 }
 
 // ---------------------------------------------------------------- asymptotes
@@ -850,8 +864,9 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
         guard = true;
         return 0.0;
     }
-    const double zl = P.sigmal == 1.0 ? CS_EPS9 : (1 - cs64::sqr(P.sigmal)) / cs64::sqr(P.sigmal);
-    const double zr = P.sigma == 1.0 ? CS_EPS9 : (1 - cs64::sqr(P.sigma)) / cs64::sqr(P.sigma);
+    // Schulz exponents of length and radius, formed on the branches that use
+    // them (two FP64 divisions the other pixels do not pay)
+    auto z_of = [](double sg) { return sg == 1.0 ? CS_EPS9 : (1 - cs64::sqr(sg)) / cs64::sqr(sg); };
     double pql = 0, pqr = 0;
     double el = EPS_SERIES, er = EPS_SERIES;
     if (P.ordis == 6) {
@@ -860,6 +875,7 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
         if (q < thr) {
             pql = cs64::series_zdir(P.carrp[0], qxs, qys);
         } else {
+            const double zl = z_of(P.sigmal);
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
             if (LAT || fabs((zl - 1) * arglq) < 1e-3) {
                 // the reference's closed form cancels to rounding noise for
@@ -883,6 +899,11 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
                 pql = cs64::cyl_double_series(P, qxs, qys, P.carrp[0], 0);
             else if (P.orcase == 3)
                 pql = cs64::cyl_double_series(P, qxs, qys, P.carrp[0], 1);
+        } else if (P.orcase < 1 || P.orcase > 4) {
+            // the integrand is identically zero (trapzdchid has no case for
+            // the general orientation): the quadrature gives +0, and +0 / norm
+            // is +0 for a positive norm
+            pql = P.norm > 0 ? 0.0 : 0.0 / P.norm;
         } else {
             ChiArgsF A;
             const double s = P.sigmal;
@@ -909,24 +930,39 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
         guard = true;
         return 0.0;
     }
+    // A length factor of exactly zero (the general orientation's identically
+    // zero integrand, or an exact zero of the series) makes the product zero
+    // wherever the radial factor is finite. On the series side of its switch
+    // it is (a converged sum of finite terms): the FP64 series is skipped
+    // there, and the switch needs no guard (a zero either way, the closed form
+    // being finite at the switch). The closed form is still evaluated in FP32
+    // so that a non-finite value reaches the product as in the drop-in. The
+    // sign of a zero product does not change the pixel's value.
+    const bool zero_len = !LAT && pql == 0.0;
     if ((P.length / P.radius) < 2)
         pqr = 1;
     else {
         const double thr = 0.65 * P.limq[4];
-        if (near(q, thr, 1e-12)) guard = true;
-        if (q < thr)
+        if (!zero_len && near(q, thr, 1e-12)) guard = true;
+        if (q < thr) {
+            if (zero_len) {
+                err = el;
+                return 0.0;
+            }
             pqr = cs64::series_q(P.carrp[3], q, 120);
-        else {
+        } else {
             float rel;
+            const double zr = z_of(P.sigma);
             const double argpq = q * P.radius / (zr + 1);
             if (LAT) {
                 pqr = cyl_pqr_asym_d(argpq, zr, rel);
             } else {
                 pqr = cyl_pqr_asym<false>(argpq, zr, rel);
                 // (a zero length factor makes the product zero: no need to refine)
-                if (!(rel <= acc_switch<LAT>()) && pql != 0.0) pqr = cyl_pqr_asym<true>(argpq, zr, rel);
+                if (!(rel <= acc_switch<LAT>()) && !zero_len) pqr = cyl_pqr_asym<true>(argpq, zr, rel);
             }
-            er = rel;
+            // a finite factor of a zero product carries no error into it
+            er = (zero_len && isfinite(pqr)) ? 0.0f : rel;
         }
     }
     err = el + er;
@@ -1058,7 +1094,8 @@ template <int KEY, bool WARP = false>
 __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double qy, double qz, bool &guard) {
     const cs_prepared &P = *C.P;
     const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
-    const double tailv = P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+    // the fluctuation term (its FP64 division skipped when it is zero)
+    const double tailv = P.ifluc == 0.0 ? 0.0 : P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
     double ep = 0, ef = 0;  // relative error estimates of pq and fq
     if (KEY == CS_KEY_SPHERE_NONE_ISO) {
         const double pq = sphere_pq_mixed<false>(P, q, guard, ep);
@@ -1130,6 +1167,7 @@ __global__ void __launch_bounds__(256) k_image_mixed(Ctx C, PeakTab T, double *_
                                                       int redo_cap) {
     const cs_prepared &P = *C.P;
     const int xstride = P.xmax - P.xmin;
+    const QGeom g = q_geom(P);
     // persistent warps take 32-pixel chunks from redo_count[1] (zeroed with
     // the redo counter): balanced however unevenly the pixel cost varies
     int *next = redo_count + 1;
@@ -1138,18 +1176,19 @@ __global__ void __launch_bounds__(256) k_image_mixed(Ctx C, PeakTab T, double *_
         if ((threadIdx.x & 31) == 0) base = atomicAdd(next, 32);
         base = __shfl_sync(0xffffffffu, base, 0);
         if ((long)base >= npix) break;
-        const long t = (long)base + (threadIdx.x & 31);
-        if (t >= npix) continue;
-        const int ihex = P.zzmin + (int)(t % nx);
-        const int i = P.iimin + (int)(t / nx);
+        // images are below 2^30 pixels (checked on the host): 32-bit indices
+        const int t = base + (int)(threadIdx.x & 31);
+        if ((long)t >= npix) continue;
+        const int ihex = P.zzmin + t % nx;
+        const int i = P.iimin + t / nx;
         double qx, qy, qz;
-        q_of_pixel<KEY>(P, ihex, i, qx, qy, qz);
+        q_of_pixel<KEY>(P, g, ihex, i, qx, qy, qz);
         bool guard = false;
         const double v = calc_mixed<KEY>(C, T, qx, qy, qz, guard);
         out[(long)(ihex - P.xmin) + (long)xstride * (long)(i - P.ymin)] = v;
         if (guard) {
             const int pos = atomicAdd(redo_count, 1);
-            if (pos < redo_cap) redo_list[pos] = (int)t;
+            if (pos < redo_cap) redo_list[pos] = t;
         }
     }
 }
@@ -1177,7 +1216,7 @@ __global__ void __launch_bounds__(CS_BATCH_TILE) k_batch_mixed(const cs::BatchSe
         const int ihex = P.zzmin + (int)(t % S.nx);
         const int i = P.iimin + (int)(t / S.nx);
         double qx, qy, qz;
-        q_of_pixel<KEY>(P, ihex, i, qx, qy, qz);
+        q_of_pixel<KEY>(P, q_geom(P), ihex, i, qx, qy, qz);
         bool guard = false;
         const double v = calc_mixed<KEY>(C, S.peaks, qx, qy, qz, guard);
         out[S.out_offset + (long)(ihex - P.xmin) + (long)(P.xmax - P.xmin) * (long)(i - P.ymin)] = v;
