@@ -182,9 +182,9 @@ def fp_peaks():
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
 # the headline kernel, k_image_mixed on the 512x512 cylinder, from an ncu
-# capture of three launches on a GB300 (the image stays in L2 during the
-# launch and reaches DRAM after it)
-TRAFFIC_BYTES_PER_LAUNCH = 101888
+# capture of three launches on a GB300 (the median; the image stays in L2
+# during the launch and reaches DRAM after it)
+TRAFFIC_BYTES_PER_LAUNCH = 95232
 
 
 def load_ops():
