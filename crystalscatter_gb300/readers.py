@@ -1,0 +1,295 @@
+"""Measured and saved 2D images as fit targets.
+
+Host-side readers for the image files the reference loads as fit data, with
+the same layout and metadata keys, so that a target can go straight to
+``SasCalc_GENERIC_calculation.setFitData``:
+
+* the program's own saved images (``<name>.csv`` with ``<name>.txt``
+  metadata, ``Source/sc_readdata.cpp:534-650``; the binary ``<name>.dat``
+  written by ``Source/widimage.cpp:1480-1500``);
+* the no-fit rectangles saved beside an image (``<image>.nofit``,
+  ``Source/widimage.cpp:154-166`` and ``:243-262``);
+* KWS detector files (``Source/sc_readdata.cpp:655-876``);
+* the beam-stop centre finder (``SC_ReadData::findBeamCenter``,
+  ``Source/sc_readdata.cpp:878-1010``).
+
+An image is returned as :class:`Image`: ``data`` has shape (rows, cols) =
+(maxY - minY, maxX - minX), row y holds x = minX .. maxX - 1 (the order of
+the files and of ``setFitData``), and ``meta`` holds the metadata strings
+under the reference's keys.
+"""
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Image:
+    data: np.ndarray
+    minX: int
+    maxX: int
+    minY: int
+    maxY: int
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def rows(self):
+        return self.maxY - self.minY
+
+    @property
+    def cols(self):
+        return self.maxX - self.minX
+
+    def get(self, x, y):
+        """Value at detector coordinates (x, y), like widImage::getData."""
+        return self.data[y - self.minY, x - self.minX]
+
+
+def _base(path):
+    root, _ = os.path.splitext(path)
+    return root
+
+
+def read_sascrystal_csv(path):
+    """A saved image: ``<base>.csv`` and its ``<base>.txt`` metadata.
+
+    The CSV holds ``X:;minX;maxX``, ``Y:;minY;maxY`` and one ``Y=<y>:;v;v;...``
+    line per row. As in the reference, the image is returned with extents
+    0..cols, 0..rows (the values in file order), its metadata from the
+    tab-separated ``.txt`` plus ``From File``, ``NbRows`` and ``NbCols``.
+    Returns None when either file is missing, like the reference."""
+    base = _base(path)
+    fncsv, fntxt = base + ".csv", base + ".txt"
+    if not (os.path.exists(fncsv) and os.path.exists(fntxt)):
+        return None
+    vals = []
+    nrows = ncols = 0
+    with open(fncsv, "r", errors="replace") as f:
+        for line in f:
+            sl = [t for t in line.strip().split(";") if t != ""]
+            if len(sl) < 2:
+                continue
+            if sl[0] == "X:":
+                ncols = int(sl[2]) - int(sl[1])
+            elif sl[0] == "Y:":
+                nrows = int(sl[2]) - int(sl[1])
+            elif sl[0].startswith("Y=") and len(sl) > ncols:
+                vals.extend(float(t) for t in sl[1:])
+    data = np.asarray(vals, dtype=np.float64)
+    if data.size != nrows * ncols:
+        raise ValueError(f"{fncsv}: {data.size} values for {nrows} x {ncols}")
+    meta = {"From File": fncsv, "NbRows": str(nrows), "NbCols": str(ncols)}
+    meta.update(_read_meta(fntxt))
+    return Image(data.reshape(nrows, ncols), 0, ncols, 0, nrows, meta)
+
+
+def _read_meta(fntxt):
+    meta = {}
+    with open(fntxt, "r", errors="replace") as f:
+        for line in f:
+            sl = [t for t in line.strip().split("\t") if t != ""]
+            if len(sl) < 2 or sl[0] in ("From File", "NbRows", "NbCols"):
+                continue
+            meta[sl[0]] = sl[1]
+    return meta
+
+
+DAT_HEADER_BYTES = 19  # "%4d %4d %4d %4d" of minX maxX minY maxY
+
+
+def read_sascrystal_dat(path):
+    """The binary image file: a 19-byte text header with minX, maxX, minY,
+    maxY (each right-aligned in 4 characters), then the values as native
+    little-endian doubles, y outer, x inner. The ``.txt`` beside it, if
+    present, supplies the metadata."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    head = raw[:DAT_HEADER_BYTES].decode("ascii", errors="replace").split()
+    if len(head) != 4:
+        raise ValueError(f"{path}: header {raw[:DAT_HEADER_BYTES]!r} is not four integers")
+    minX, maxX, minY, maxY = (int(t) for t in head)
+    n = (maxX - minX) * (maxY - minY)
+    body = raw[DAT_HEADER_BYTES:]
+    if len(body) != 8 * n:
+        raise ValueError(f"{path}: {len(body)} bytes of data for {n} doubles")
+    data = np.frombuffer(body, dtype="<f8").reshape(maxY - minY, maxX - minX).copy()
+    meta = {"From File": path}
+    fntxt = _base(path) + ".txt"
+    if os.path.exists(fntxt):
+        meta.update(_read_meta(fntxt))
+    return Image(data, minX, maxX, minY, maxY, meta)
+
+
+def write_sascrystal(img, base):
+    """Writes ``<base>.dat`` and ``<base>.csv`` (and ``<base>.txt`` from
+    ``img.meta``) in the formats above, for round trips and for handing a
+    computed image to the reference's GUI."""
+    with open(base + ".dat", "wb") as f:
+        f.write(f"{img.minX:4d} {img.maxX:4d} {img.minY:4d} {img.maxY:4d}".encode("ascii"))
+        f.write(np.ascontiguousarray(img.data, dtype="<f8").tobytes())
+    with open(base + ".csv", "w") as f:
+        f.write(f"X:;{img.minX};{img.maxX}\n")
+        f.write(f"Y:;{img.minY};{img.maxY}\n")
+        for r in range(img.rows):
+            f.write(f"Y={img.minY + r}:" + "".join(";" + repr(float(v)) for v in img.data[r]) + "\n")
+    with open(base + ".txt", "w") as f:
+        for k, v in img.meta.items():
+            f.write(f"{k}\t{v}\n")
+
+
+def read_nofit(path):
+    """The four no-fit rectangles saved beside an image as (left, top, right,
+    bottom) tuples; missing numbers read as -1 and a missing file as four
+    unused rectangles, as in the reference. For a ``.csv`` image the file is
+    ``<base>.dat.nofit``, otherwise ``<image>.nofit``."""
+    if path.lower().endswith(".csv"):
+        fn = path[:-4] + ".dat.nofit"
+    else:
+        fn = path + ".nofit"
+    rects = [(-1, -1, -1, -1)] * 4
+    if not os.path.exists(fn):
+        return rects
+    with open(fn, "r", errors="replace") as f:
+        lines = f.read().split("\n")
+    out = []
+    for i in range(4):
+        sl = lines[i].split() if i < len(lines) else []
+        while len(sl) < 4:
+            sl.append("-1")
+        out.append(tuple(int(t) for t in sl[:4]))
+    return out
+
+
+def apply_nofit(calc, rects):
+    """Hands the rectangles to ``setNoFitRect`` (index 0..3)."""
+    for i, (x0, y0, x1, y1) in enumerate(rects):
+        calc.setNoFitRect(i, x0, y0, x1, y1)
+
+
+_KWS_SIZES = {128 * 128: (128, 64), 144 * 144: (144, 72), 256 * 256: (256, 128)}
+
+
+def read_kws(path):
+    """A KWS detector file: a header up to the line starting with ``$`` (the
+    wavelength from ``lambda=`` after the comment marker, in nm, converted
+    from Angstrom when it ends in ``A``; the sample-detector distance from the
+    detector description table), then whitespace-separated counts (lines of
+    at least 8 numbers; negative counts read as 0). 128², 144² and 256²
+    detectors are recognised, with the beam at the centre and 5.3 mm pixels.
+    Files whose first 40 lines name ``Data columns`` are 2D-SANS files, which
+    this reader does not handle (ValueError)."""
+    with open(path, "r", errors="replace") as f:
+        lines = f.read().split("\n")
+    for line in lines[:40]:
+        if "Data columns" in line.strip():
+            raise ValueError(f"{path}: a 2D-SANS file, not KWS data")
+    is_hdr = True
+    look_lambda = look_det = False
+    det_hdr = True
+    wavelen, detpos = "0.5 nm", "4.0 m"
+    vals = []
+    for line in lines:
+        line = line.strip()
+        if is_hdr:
+            if line.startswith("(* Comment *)"):
+                look_lambda = True
+            elif look_lambda and "lambda=" in line:
+                look_lambda = False
+                rest = line[line.index("lambda=") + 7:]
+                wl = float(rest[:-1].strip())
+                if rest.endswith("A"):
+                    wl = wl / 10
+                wavelen = f"{wl:g} nm"
+            if line.startswith("(* Detector Discription *)"):
+                look_det = True
+            elif look_det:
+                if line.startswith("(*"):
+                    look_det = False
+                elif det_hdr and line[:1] == "[":
+                    det_hdr = False
+                elif not det_hdr:
+                    sl = line.split()
+                    if len(sl) == 4:
+                        detpos = sl[1] + " m"
+            if line.startswith("$"):
+                is_hdr = False
+            continue
+        sl = line.split()
+        if len(sl) < 8:
+            continue
+        vals.extend(max(float(t), 0.0) for t in sl)
+    if len(vals) not in _KWS_SIZES:
+        raise ValueError(f"{path}: {len(vals)} values, not a 128², 144² or 256² detector")
+    n, beam = _KWS_SIZES[len(vals)]
+    meta = {"From File": path, "NbRows": str(n), "NbCols": str(n), "BeamPosX": str(beam),
+            "BeamPosY": str(beam), "wavelength": wavelen, "EditWAXSangle": "0.0 deg", "SampleDist": detpos,
+            "Pixel_X": "5.3", "Pixel_Y": "5.3"}
+    return Image(np.asarray(vals, dtype=np.float64).reshape(n, n), 0, n, 0, n, meta)
+
+
+def find_beam_center(img, x0, y0):
+    """Centre of the beam stop, SC_ReadData::findBeamCenter: pixels at or
+    below the reference level (the first pixel's value when that is at most
+    0.001, else 0) are shadow. If (x0, y0) is in the shadow, the shadow is
+    walked outward from it along its row and column; otherwise every row and
+    column is scanned for its widest inner run of shadow pixels (longer than
+    2), and the centre of the widest runs is returned. Returns (x, y)."""
+    d = img.data
+    ref = d.flat[0]
+    if ref > 0.001:
+        ref = 0.0
+    get = img.get
+    bsxmin = bsxmax = x0
+    bsymin = bsymax = y0
+    if get(x0, y0) > ref:
+        bsxmin, bsxmax = img.minX, img.maxX - 1
+        bsymin, bsymax = img.minY, img.maxY - 1
+        maxbsx = maxbsy = 2
+        for y in range(img.minY, img.maxY):
+            row = d[y - img.minY]
+            xx0, xx1 = img.minX, img.maxX - 1
+            while xx0 < xx1 and row[xx0 - img.minX] <= ref:
+                xx0 += 1
+            while xx0 < xx1 and row[xx1 - img.minX] <= ref:
+                xx1 -= 1
+            inner, tmp = False, 0
+            for x in range(xx0, xx1 + 1):
+                if row[x - img.minX] <= ref:
+                    if not inner:
+                        tmp, inner = x, True
+                elif inner:
+                    if x - tmp > maxbsx:
+                        bsxmin, bsxmax, maxbsx = tmp, x - 1, x - tmp
+                    inner = False
+        for x in range(img.minX, img.maxX):
+            col = d[:, x - img.minX]
+            yy0, yy1 = img.minY, img.maxY - 1
+            while yy0 < yy1 and col[yy0 - img.minY] <= ref:
+                yy0 += 1
+            while yy0 < yy1 and col[yy1 - img.minY] <= ref:
+                yy1 -= 1
+            inner, tmp = False, 0
+            for y in range(yy0, yy1 + 1):
+                if col[y - img.minY] <= ref:
+                    if not inner:
+                        tmp, inner = y, True
+                elif inner:
+                    if y - tmp > maxbsy:
+                        bsymin, bsymax, maxbsy = tmp, y - 1, y - tmp
+                    inner = False
+    else:
+        while bsxmin >= img.minX and get(bsxmin, y0) <= ref:
+            bsxmin -= 1
+        while bsxmax < img.maxX and get(bsxmax, y0) <= ref:
+            bsxmax += 1
+        while bsymin >= img.minY and get(x0, bsymin) <= ref:
+            bsymin -= 1
+        while bsymax < img.maxY and get(x0, bsymax) <= ref:
+            bsymax += 1
+    return _cdiv2(bsxmin + bsxmax), _cdiv2(bsymin + bsymax)
+
+
+def _cdiv2(v):
+    """C integer division by 2 (truncation toward zero)."""
+    return v // 2 if v >= 0 else -((-v) // 2)
