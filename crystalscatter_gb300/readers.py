@@ -10,6 +10,7 @@ the same layout and metadata keys, so that a target can go straight to
 * the no-fit rectangles saved beside an image (``<image>.nofit``,
   ``Source/widimage.cpp:154-166`` and ``:243-262``);
 * KWS detector files (``Source/sc_readdata.cpp:655-876``);
+* EDF detector files (``Source/sc_readdata.cpp:1769-2121``);
 * the beam-stop centre finder (``SC_ReadData::findBeamCenter``,
   ``Source/sc_readdata.cpp:878-1010``).
 
@@ -18,6 +19,7 @@ An image is returned as :class:`Image`: ``data`` has shape (rows, cols) =
 the files and of ``setFitData``), and ``meta`` holds the metadata strings
 under the reference's keys.
 """
+import math
 import os
 from dataclasses import dataclass, field
 
@@ -226,6 +228,143 @@ def read_kws(path):
             "BeamPosY": str(beam), "wavelength": wavelen, "EditWAXSangle": "0.0 deg", "SampleDist": detpos,
             "Pixel_X": "5.3", "Pixel_Y": "5.3"}
     return Image(np.asarray(vals, dtype=np.float64).reshape(n, n), 0, n, 0, n, meta)
+
+
+_EDF_TYPES = {
+    ("FloatValue", 4): "f4", ("FloatIEEE32", 4): "f4",
+    ("SignedInteger", 4): "i4", ("Signed32", 4): "i4", ("SignedLong", 4): "i4",
+    ("UnsignedShort", 2): "u2", ("Unsigned16", 2): "u2",
+    ("DoubleValue", 8): "f8", ("DoubleIEEE64", 8): "f8",
+}
+
+_EDF_K1_KEYS = ["EDF_BinarySize", "EDF_HeaderSize", "ByteOrder", "DataType", "Dim_1", "Dim_2", "Title",
+                "ExposureTime", "Center_1", "Center_2", "PSize_1", "PSize_2", "SampleDistance", "WaveLength",
+                "DetectorPosition"]
+
+
+def _fmt_num(v):
+    # QString::number(double): up to 6 significant digits
+    return f"{v:.6g}"
+
+
+def read_edf(path):
+    """An EDF detector file with one data block. The header runs from the
+    line starting with ``{`` to the line holding ``}``; the data follow that
+    line. Two header kinds are read as in the reference:
+
+    * ``EDF_DataBlockID`` first ("K1"): sizes, byte order, type, centre,
+      pixel size (m, reported in mm), sample distance (m) and wavelength (m,
+      reported in nm) from their keys;
+    * ``HeaderID`` first ("E1"): byte order, type, Dim_1/Dim_2 and Size, with
+      the beam at the centre, 0.26 mm pixels, 5.005 m and 0.124 nm.
+
+    ``EDF_DataFormatVersion`` headers are not read (None), as in the
+    reference. Types: 32-bit float and signed integer, 16-bit unsigned, 64-bit
+    float, in either byte order. Pixel k of the file (row r = k / Dim_1,
+    column c = k % Dim_1) lands at x = rows - 1 - r, y = c, the reference's
+    layout, which is defined for square detectors (others raise
+    ValueError). Each record is read once; the reference's loops for the types
+    other than little-endian float also visit one record past every
+    2048-byte block (a stale value that shifts the pixels after it, and a
+    write past the image at the end), which is not reproduced."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    pos = 0
+
+    def readline():
+        nonlocal pos
+        if pos >= len(raw):
+            return None
+        e = raw.find(b"\n", pos)
+        e = len(raw) if e < 0 else e + 1
+        line = raw[pos:e]
+        pos = e
+        return line.decode("latin-1").strip()
+
+    while True:
+        line = readline()
+        if line is None or line.startswith("{"):
+            break
+    vals = {"EDF_BinarySize": 0, "EDF_HeaderSize": 0, "ByteOrder": "", "DataType": "", "Dim_1": 0, "Dim_2": 0,
+            "Title": "", "ExposureTime": 0.0, "Center_1": 0.0, "Center_2": 0.0, "PSize_1": 0.0, "PSize_2": 0.0,
+            "SampleDistance": 0.0, "WaveLength": 0.0, "DetectorPosition": 0.0}
+    line = readline() or ""
+
+    def header(keys):
+        while True:
+            ln = readline()
+            if ln is None or "}" in ln:
+                return
+            tmp = ln.split(" = ")
+            if len(tmp) < 2:
+                continue
+            v = tmp[1]
+            if v.endswith(";"):
+                v = v[:-1].strip()
+            if tmp[0] in keys:
+                yield tmp[0], v
+
+    def num(v, conv):
+        try:
+            return conv(v)
+        except ValueError:
+            return conv(0)
+
+    if line.startswith("EDF_DataBlockID"):
+        file_type = "K1"
+        for k, v in header(_EDF_K1_KEYS):
+            if k in ("EDF_BinarySize", "EDF_HeaderSize", "Dim_1", "Dim_2"):
+                vals[k] = num(v, int)
+            elif k in ("ByteOrder", "DataType", "Title"):
+                vals[k] = v
+            else:
+                vals[k] = num(v, float)
+        beam_x, beam_y = vals["Center_1"], vals["Center_2"]
+        pixel_x, pixel_y = 1e3 * vals["PSize_1"], 1e3 * vals["PSize_2"]
+        dist, wavelen = vals["SampleDistance"], 1e9 * vals["WaveLength"]
+    elif line.startswith("EDF_DataFormatVersion"):
+        return None
+    elif line.startswith("HeaderID"):
+        file_type = "E1"
+        for k, v in header(["ByteOrder", "DataType", "Dim_1", "Dim_2", "Size"]):
+            if k == "Size":
+                vals["EDF_BinarySize"] = num(v, int)
+            elif k in ("Dim_1", "Dim_2"):
+                vals[k] = num(v, int)
+            else:
+                vals[k] = v
+        # C round(): halves away from zero
+        beam_x = float(math.floor(vals["Dim_1"] / 2.0 + 0.5))
+        beam_y = float(math.floor(vals["Dim_2"] / 2.0 + 0.5))
+        pixel_x = pixel_y = 0.260
+        dist, wavelen = 5.005, 1.24e-1
+    else:
+        raise ValueError(f"{path}: unknown EDF header kind {line!r}")
+    ncols, nrows = vals["Dim_1"], vals["Dim_2"]
+    if ncols <= 0 or nrows <= 0:
+        raise ValueError(f"{path}: image size {ncols} x {nrows}")
+    if ncols != nrows:
+        raise ValueError(f"{path}: the EDF pixel layout is defined for square detectors only")
+    rec = vals["EDF_BinarySize"] // ncols // nrows
+    key = (vals["DataType"], rec)
+    if key not in _EDF_TYPES:
+        raise ValueError(f"{path}: data type {vals['DataType']} with {rec}-byte records is not supported")
+    order = "<" if vals["ByteOrder"] == "LowByteFirst" else ">"
+    n = ncols * nrows
+    body = raw[pos:pos + n * rec]
+    if len(body) < n * rec:
+        raise ValueError(f"{path}: {len(body)} data bytes for {n} records of {rec}")
+    flat = np.frombuffer(body, dtype=order + _EDF_TYPES[key]).astype(np.float64)
+    # x = rows - 1 - r, y = c  ->  out[c, rows-1-r] = file[r, c]
+    data = flat.reshape(nrows, ncols)[::-1].T.copy()
+    meta = {"From File": path, "NbRows": str(nrows), "NbCols": str(ncols), "BeamPosX": _fmt_num(beam_x),
+            "BeamPosY": _fmt_num(beam_y), "FileType": file_type, "Pixel_x": _fmt_num(pixel_x),
+            "Pixel_y": _fmt_num(pixel_y), "SampleDist": _fmt_num(dist), "wavelength": _fmt_num(wavelen),
+            "EditWAXSangle": "0.0 deg", "EDF_BinarySize": str(vals["EDF_BinarySize"]),
+            "headSize": str(vals["EDF_HeaderSize"]), "ByteOrder": vals["ByteOrder"], "DataType": vals["DataType"],
+            "Title": vals["Title"], "ExposureTime": _fmt_num(vals["ExposureTime"]),
+            "DetectorPos": _fmt_num(vals["DetectorPosition"])}
+    return Image(data, 0, ncols, 0, nrows, meta)
 
 
 def find_beam_center(img, x0, y0):

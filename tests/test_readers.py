@@ -1,7 +1,8 @@
 """Fit-target file formats: the program's saved images (.dat/.csv/.txt), the
-no-fit rectangles, KWS detector files and the beam-stop centre finder, on
-synthetic files built byte by byte in the formats the reference writes
-(Source/widimage.cpp:1480-1500 and :154-166, Source/sc_readdata.cpp:534-1010)."""
+no-fit rectangles, KWS and EDF detector files and the beam-stop centre
+finder, on synthetic files built byte by byte in the formats the reference
+reads and writes (Source/widimage.cpp:1480-1500 and :154-166,
+Source/sc_readdata.cpp:534-1010 and :1769-2121)."""
 import struct
 
 import numpy as np
@@ -157,3 +158,59 @@ def test_beam_center_negative_extents():
     img = R.Image(data, -5, 6, -4, 5)
     # shadow x in -1..1, y in -1..1
     assert R.find_beam_center(img, 0, 0) == (0, 0)
+
+
+def _edf_bytes(kind, data, dtype, order="LowByteFirst", extra=()):
+    n = data.shape[0]
+    bo = "<" if order == "LowByteFirst" else ">"
+    body = data.astype(bo + dtype).tobytes()
+    names = {"f4": "FloatValue", "i4": "SignedInteger", "u2": "UnsignedShort", "f8": "DoubleValue"}
+    if kind == "K1":
+        hdr = ["EDF_DataBlockID = 0.Image.Psd ;", f"EDF_BinarySize = {len(body)} ;", "EDF_HeaderSize = 1024 ;",
+               f"ByteOrder = {order} ;", f"DataType = {names[dtype]} ;", f"Dim_1 = {n} ;", f"Dim_2 = {n} ;",
+               "Title = test image ;", "Center_1 = 12.5 ;", "Center_2 = 7 ;", "PSize_1 = 0.000172 ;",
+               "PSize_2 = 0.000172 ;", "SampleDistance = 3.2 ;", "WaveLength = 1.54e-10 ;"]
+    else:
+        hdr = ["HeaderID = EH:000001:000000:000000 ;", f"ByteOrder = {order} ;", f"DataType = {names[dtype]} ;",
+               f"Dim_1 = {n} ;", f"Dim_2 = {n} ;", f"Size = {len(body)} ;"]
+    hdr += list(extra)
+    text = "{\n" + "\n".join(hdr) + "\n"
+    text += " " * ((-(len(text) + 2)) % 512) + "}\n"
+    return text.encode("latin-1") + body
+
+
+@pytest.mark.parametrize("dtype", ["f4", "i4", "u2", "f8"])
+@pytest.mark.parametrize("order", ["LowByteFirst", "HighByteFirst"])
+def test_edf_types_and_layout(tmp_path, dtype, order):
+    n = 9
+    rng = np.random.default_rng(3)
+    filedata = rng.integers(0, 60000, size=(n, n)).astype(np.float64)
+    if dtype in ("f4", "f8"):
+        filedata = filedata / 7.0
+    fn = tmp_path / "a.edf"
+    fn.write_bytes(_edf_bytes("K1", filedata, dtype, order))
+    img = R.read_edf(str(fn))
+    want = filedata.astype(dtype).astype(np.float64)
+    # file pixel (r, c) lands at x = n-1-r, y = c
+    for r, c in [(0, 0), (0, 5), (3, 2), (8, 8)]:
+        assert img.get(n - 1 - r, c) == want[r, c]
+    assert img.meta["FileType"] == "K1" and img.meta["BeamPosX"] == "12.5" and img.meta["BeamPosY"] == "7"
+    assert img.meta["Pixel_x"] == "0.172" and img.meta["SampleDist"] == "3.2"
+    assert img.meta["wavelength"] == "0.154" and img.meta["Title"] == "test image"
+
+
+def test_edf_e1_defaults_and_rejects(tmp_path):
+    n = 7
+    data = np.arange(n * n, dtype=np.float64).reshape(n, n)
+    fn = tmp_path / "b.edf"
+    fn.write_bytes(_edf_bytes("E1", data, "f4"))
+    img = R.read_edf(str(fn))
+    assert img.meta["FileType"] == "E1" and img.meta["BeamPosX"] == "4"  # round(3.5) = 4
+    assert img.meta["Pixel_x"] == "0.26" and img.meta["wavelength"] == "0.124"
+    assert img.get(n - 1, 0) == 0.0 and img.get(0, n - 1) == data[n - 1, n - 1]
+    fn.write_bytes(b"{\nEDF_DataFormatVersion = 2.0 ;\n}\n")
+    assert R.read_edf(str(fn)) is None
+    bad = _edf_bytes("K1", data, "f4").replace(b"DataType = FloatValue", b"DataType = Complex128  ")
+    fn.write_bytes(bad)
+    with pytest.raises(ValueError):
+        R.read_edf(str(fn))
