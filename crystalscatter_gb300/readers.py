@@ -11,6 +11,7 @@ the same layout and metadata keys, so that a target can go straight to
   ``Source/widimage.cpp:154-166`` and ``:243-262``);
 * KWS detector files (``Source/sc_readdata.cpp:655-876``);
 * EDF detector files (``Source/sc_readdata.cpp:1769-2121``);
+* spreadsheet text images (``Source/sc_readdata.cpp:2123-2190``);
 * the beam-stop centre finder (``SC_ReadData::findBeamCenter``,
   ``Source/sc_readdata.cpp:878-1010``).
 
@@ -365,6 +366,38 @@ def read_edf(path):
             "Title": vals["Title"], "ExposureTime": _fmt_num(vals["ExposureTime"]),
             "DetectorPos": _fmt_num(vals["DetectorPosition"])}
     return Image(data, 0, ncols, 0, nrows, meta)
+
+
+def read_spreadsheet(path):
+    """A text image whose first line is ``<rows> <cols> Start pixel = ...``
+    followed by one line of values per row (lines with fewer than ``cols``
+    values are skipped, and count against the rows). The beam position starts
+    at (cols/2, rows/2) and is then placed at the beam-stop centre
+    (:func:`find_beam_center`), as the reference does for these files, which
+    carry no metadata. Returns None when the first line has no ``Start
+    pixel``."""
+    with open(path, "r", errors="replace") as f:
+        lines = f.read().split("\n")
+    first = lines[0].strip() if lines else ""
+    pos = first.find("Start pixel")
+    if pos < 0:
+        return None
+    sl = first[:pos].split()
+    nrows, ncols = int(sl[0]), int(sl[1])
+    vals = []
+    for line in lines[1:1 + nrows]:
+        sl = line.split()
+        if len(sl) < ncols:
+            continue
+        vals.extend(float(t) for t in sl)
+    if len(vals) != nrows * ncols:
+        raise ValueError(f"{path}: {len(vals)} values for {nrows} x {ncols}")
+    img = Image(np.asarray(vals, dtype=np.float64).reshape(nrows, ncols), 0, ncols, 0, nrows,
+                {"From File": path, "NbRows": str(nrows), "NbCols": str(ncols)})
+    bx, by = find_beam_center(img, ncols // 2, nrows // 2)
+    img.meta["BeamPosX"] = str(bx)
+    img.meta["BeamPosY"] = str(by)
+    return img
 
 
 def find_beam_center(img, x0, y0):

@@ -214,3 +214,20 @@ def test_edf_e1_defaults_and_rejects(tmp_path):
     fn.write_bytes(bad)
     with pytest.raises(ValueError):
         R.read_edf(str(fn))
+
+
+def test_spreadsheet(tmp_path):
+    n = 20
+    data = np.ones((n, n)) * 3.0
+    data[8:13, 5:10] = 0.0  # beam stop centred at x = 7, y = 10
+    lines = [f"    {n}    {n} Start pixel = (       1       1)"]
+    for r in range(n):
+        lines.append("  " + " ".join(f"{v:13.6e}" for v in data[r]))
+    fn = tmp_path / "img.spr"
+    fn.write_text("\n".join(lines) + "\n")
+    img = R.read_spreadsheet(str(fn))
+    assert np.array_equal(img.data, data)
+    assert img.get(7, 10) == 0.0
+    assert (img.meta["BeamPosX"], img.meta["BeamPosY"]) == ("7", "10")
+    fn.write_text("no header\n1 2\n")
+    assert R.read_spreadsheet(str(fn)) is None
