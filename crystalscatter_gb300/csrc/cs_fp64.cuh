@@ -588,8 +588,9 @@ template <bool WARP = false>
 __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, double q) {
     const cs_prepared &P = *C.P;
     double pqr = 0, pql = 0;
-    const double zl = P.sigmal == 1.0 ? CS_EPS9 : (1 - sqr(P.sigmal)) / sqr(P.sigmal);
-    const double zr = P.sigma == 1.0 ? CS_EPS9 : (1 - sqr(P.sigma)) / (sqr(P.sigma));
+    // Schulz exponents, formed on the branches that use them
+    auto zl_of = [&P]() { return P.sigmal == 1.0 ? CS_EPS9 : (1 - sqr(P.sigmal)) / sqr(P.sigmal); };
+    auto zr_of = [&P]() { return P.sigma == 1.0 ? CS_EPS9 : (1 - sqr(P.sigma)) / (sqr(P.sigma)); };
     if (P.ordis == 6) {
         if (P.orcase == 4)
             pql = 1.0;
@@ -597,6 +598,7 @@ __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, d
             if (q < (0.6 * P.limq[1])) {
                 pql = series_zdir(P.carrp[0], qxs, qys);
             } else {
+                const double zl = zl_of();
                 const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
                 pql = len_factor_ref(arglq, zl);
             }
@@ -613,6 +615,11 @@ __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, d
                     pql = cyl_double_series(P, qxs, qys, P.carrp[0], 0);
                 else if (P.orcase == 3)
                     pql = cyl_double_series(P, qxs, qys, P.carrp[0], 1);
+            } else if (P.orcase < 1 || P.orcase > 4) {
+                // the quadrature of trapzdchid's identically zero integrand
+                // (no case for the general orientation) is +0, which
+                // qromb_delta_cyl returns without evaluating it
+                pql = 0.0 / P.norm;
             } else {
                 const ChiArgs A = chi_args(P, qxs, qys, P.sigmal, P.orcase);
                 pql = WARP ? qromb_delta_cyl_warp(C, A) : qromb_delta_cyl(C, A);
@@ -624,9 +631,22 @@ __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, d
         if ((P.length / P.radius) < 2)
             pqr = 1;
         else {
+            // Without a lattice, a zero length factor times a finite radial
+            // factor is a zero whose sign cannot change the pixel's value
+            // (with a lattice it would decide the sign of F/P): the radial
+            // factor is not formed where it is known to be finite, on the
+            // series side of the switch (a converged sum of finite terms near
+            // 1) and on the closed-form side when zr > 3 and the argument is
+            // not tiny (finite Gamma-ratio prefactors, powers of 1 + 4x^2 >= 1
+            // with positive exponents), both read off sigma without a division.
+            const bool zero_len = (pql == 0.0) && !P.lattice;
             if (q < (0.65 * P.limq[4])) {
+                if (zero_len) return 0.0;
                 pqr = series_q(P.carrp[3], q, 120);
             } else {
+                // zr > 3.16 for sigma < 0.49; argpq = q R sigma^2 to rounding
+                if (zero_len && P.sigma > 0 && P.sigma < 0.49 && q * P.radius * P.sigma * P.sigma > 1e-28) return 0.0;
+                const double zr = zr_of();
                 const double argpq = q * P.radius / (zr + 1);
                 const double pqr1 = (1 / (zr * (zr - 1) * (zr - 2))) * pow(argpq, -3);
                 const double pqr2 = (1 / (zr * (zr - 1) * (zr - 2))) * pow(argpq, -3) * sin((zr - 2) * atan(2.0 * argpq)) /

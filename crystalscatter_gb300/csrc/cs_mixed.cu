@@ -935,9 +935,10 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
     // wherever the radial factor is finite. On the series side of its switch
     // it is (a converged sum of finite terms): the FP64 series is skipped
     // there, and the switch needs no guard (a zero either way, the closed form
-    // being finite at the switch). The closed form is still evaluated in FP32
-    // so that a non-finite value reaches the product as in the drop-in. The
-    // sign of a zero product does not change the pixel's value.
+    // being finite at the switch). On the closed-form side it is skipped where
+    // it is provably finite; elsewhere it is still evaluated so that a
+    // non-finite value reaches the product as in the drop-in. The sign of a
+    // zero product does not change the pixel's value.
     const bool zero_len = !LAT && pql == 0.0;
     if ((P.length / P.radius) < 2)
         pqr = 1;
@@ -951,6 +952,12 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             }
             pqr = cs64::series_q(P.carrp[3], q, 120);
         } else {
+            // the closed form is finite for zr > 3.16 (sigma < 0.49) and an
+            // argument q R sigma^2 that is not tiny: a zero product then
+            if (zero_len && P.sigma > 0 && P.sigma < 0.49 && q * P.radius * P.sigma * P.sigma > 1e-28) {
+                err = el;
+                return 0.0;
+            }
             float rel;
             const double zr = z_of(P.sigma);
             const double argpq = q * P.radius / (zr + 1);
