@@ -451,6 +451,11 @@ bool Prep::coefficients() {
 
     bool done = false;
     bool supported = true;
+    // The F(q) coefficients (carr*f, limq*f) are read only by the lattice
+    // pixel functions (the structure factor's F/P); in the orientation-averaged
+    // cylinder block, whose F sums cost as much as the rest of it, they are
+    // formed only for lattices.
+    const bool need_f = P.lattice != 0;
 
     if (cdim == 3) {
         // isotropic case for spheres, :2509-2754
@@ -725,17 +730,22 @@ bool Prep::coefficients() {
                     carr1p[n] = std::pow(4.0, n) * z12vl[n] * xln_n / ((2.0 * n + 1) * (n + 1));
                     carr2p[n] = std::pow(4.0, n + 1) * gam3[n] * z12vl[n] * xln_n /
                                 (std::sqrt(M_PI) * (n + 2) * (n + 1) * (n + 1) * fkv[n] * fkv[n] * fkv[n]);
-                    double sump = 0.0;
-                    for (int m = 0; m <= n; m++)
-                        sump = sump + z12vl[m] * z12vl[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
-                    carr1f[n] = fk2v[n] * xln_n * sump / (std::pow(4.0, n));
+                    if (need_f) {
+                        double sump = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            sump = sump + z12vl[m] * z12vl[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                        carr1f[n] = fk2v[n] * xln_n * sump / (std::pow(4.0, n));
+                    }
                     carr2f[n] = carr2p[n];
                     carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
                                 ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n]);
-                    sump = 0.0;
-                    for (int m = 0; m <= n; m++)
-                        sump = sump + z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
-                    carr4f[n] = xrn_n * sump;
+                    if (need_f) {
+                        double sump = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            sump = sump + z12v[m] * z12v[n - m] /
+                                              ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                        carr4f[n] = xrn_n * sump;
+                    }
                 });
                 for (int n = 1; n <= nmax; n++) {
                     if (search1) {
