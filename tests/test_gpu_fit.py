@@ -119,3 +119,33 @@ def test_simplex_reproduces_first_parameter_initialisation():
     assert res["EditRadius"] == 0.0
     assert rep["chi2"] == c0
     assert res["EditSigma"] == table[1]["start"] and res["I0"] == table[2]["start"]
+
+
+def test_fit_from_saved_target_files(tmp_path):
+    """The golden target written as the program's saved image (.dat and
+    .csv/.txt) with its no-fit rectangles (.dat.nofit), read back with
+    crystalscatter_gb300.readers: the chi^2, count and NaN count are the
+    reference's for that mask."""
+    from crystalscatter_gb300 import readers
+
+    fc = golden_cases()["fit"]
+    v = fc["variants"]["nofit_rects"]
+    target = np.load(os.path.join(GOLDEN, "fit_target.npy"))
+    h, w = target.shape
+    base = str(tmp_path / "target")
+    readers.write_sascrystal(readers.Image(target, 0, w, 0, h, {"Comment": "fit target"}), base)
+    rects = [list(r) for r in v["nofit"]] + [[-1, -1, -1, -1]] * (4 - len(v["nofit"]))
+    with open(base + ".dat.nofit", "w") as f:
+        for r in rects:
+            f.write(" ".join(str(t) for t in r) + "\n")
+    for fn, read in ((base + ".dat", readers.read_sascrystal_dat), (base + ".csv", readers.read_sascrystal_csv)):
+        img = read(fn)
+        assert np.array_equal(img.data, target)
+        c = cs.SasCalc_GENERIC_calculation()
+        c.setParams(fc["params"])
+        c.setFitData(img.cols, img.rows, img.data)
+        readers.apply_nofit(c, readers.read_nofit(fn))
+        chi2, cnt, nan = c.doFitCalculation(0, v["bstop"], v["border"])
+        c.cleanup()
+        assert cnt == v["cnt"] and nan == v["nancnt"], fn
+        assert abs(chi2 - v["chi2"]) <= 1e-10 * abs(v["chi2"]), (fn, chi2, v["chi2"])
