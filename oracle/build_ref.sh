@@ -1,6 +1,7 @@
 #!/bin/sh
 # Builds the reference's own FP64 CPU calculation path (test oracle only) into
-# oracle/_ref/libscref.so, straight from the reference sources where they lie.
+# oracle/_ref/libscref.so (and its r-phi transform into libscpost.so),
+# straight from the reference sources where they lie.
 # The reference tree is read-only and is not copied: g++ reads the two
 # translation units below in place. The .cu file is compiled as plain C++,
 # which leaves exactly the reference's CPU path (no __CUDACC__).
@@ -34,3 +35,10 @@ WRAP="-Wl,--wrap=sin,--wrap=cos,--wrap=atan,--wrap=atan2,--wrap=pow,--wrap=exp,-
 g++ -shared $WRAP -o "$OUT/libscref_probe.so" "$OUT/probe_cpu.o" "$OUT/probe_gpu.o" "$OUT/probe_driver.o" \
     "$OUT/ref_probe.o" -lpthread -lm
 echo "built $OUT/libscref_probe.so"
+# the r-phi transform of the post-processing unit (its FFT needs FFTW, which
+# is absent: fftw3.h in ref_stubs only lets the unit compile)
+g++ $CXXFLAGS -c -x c++ "$REF/Source/sc_postproc.cpp" -o "$OUT/sc_postproc.o" &
+g++ $CXXFLAGS -c "$HERE/ref_postproc.cpp" -o "$OUT/ref_postproc.o" &
+wait
+g++ -shared -o "$OUT/libscpost.so" "$OUT/sc_postproc.o" "$OUT/ref_postproc.o"
+echo "built $OUT/libscpost.so"
