@@ -85,6 +85,7 @@ class CsParams(ctypes.Structure):
         ("waxs", ctypes.c_int),
         ("p1", ctypes.c_double),
         ("iso", ctypes.c_double), ("izero", ctypes.c_double), ("base", ctypes.c_double),
+        ("tpv_domain_dev", ctypes.c_double), ("tpv_dw_dev", ctypes.c_double),
     ]
 
 

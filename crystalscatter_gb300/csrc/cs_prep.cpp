@@ -1706,7 +1706,9 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
     P.uca = in.uca;
     P.ucb = in.ucb;
     P.domainsize = in.domainsize;
-    P.width_zuf = 1;
+    // domain-size width factor: 1, or its training-data randomisation
+    // 1 * (1 + dev) (tpvPerformRandom, :1076, :1112-1113)
+    P.width_zuf = 1 + in.tpv_domain_dev;
     P.ceff = in.ceff;
     P.qmax = in.qmax;
     P.qmin = in.qmin;
@@ -1731,6 +1733,8 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
         P.sig[i] = 4.0 / in.sigxyz[i];
     }
     S.dwfactor = in.debyewaller * in.debyewaller / 3.0;  // setDisplacement
+    // training-data randomisation of dwfactor (tpvPerformRandom, :1126-1129)
+    if (in.tpv_dw_dev != 0) S.dwfactor = S.dwfactor * (1 + in.tpv_dw_dev);
     P.dwfactor = S.dwfactor;
 
     S.phiwidth = 4. / in.azi;

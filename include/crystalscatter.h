@@ -81,6 +81,10 @@ typedef struct cs_params {
     double p1;
     /* Pixel manipulation group: setPixelManipulationParams, sc_calc_generic_gpu.h:348-353 */
     double iso, izero, base;
+    /* Training-data randomisation (tpvPerformRandom, Source/sc_calc_generic_cpu.cpp:1028-1143) of two
+       values that are not setter parameters: the domain-size width factor is 1 + tpv_domain_dev and
+       the Debye-Waller factor d^2/3 is multiplied by 1 + tpv_dw_dev. 0 = not randomised. */
+    double tpv_domain_dev, tpv_dw_dev;
 } cs_params;
 
 typedef struct cs_handle cs_handle;

@@ -16,7 +16,9 @@ if [ ! -f "$REF/Source/sc_calc_generic_cpu.cpp" ]; then
     exit 3
 fi
 mkdir -p "$OUT"
-CXXFLAGS="-O2 -std=gnu++17 -fPIC -ffp-contract=off -w -I$HERE/ref_stubs -I$REF/Source"
+# Q_OS_LINUX: the platform macro a Linux Qt build defines (it selects the "\n"
+# line end of the reference's log texts)
+CXXFLAGS="-O2 -std=gnu++17 -fPIC -ffp-contract=off -w -DQ_OS_LINUX -I$HERE/ref_stubs -I$REF/Source"
 g++ $CXXFLAGS -c -x c++ "$REF/Source/sc_calc_generic_cpu.cpp" -o "$OUT/sc_calc_generic_cpu.o" &
 g++ $CXXFLAGS -c -x c++ "$REF/Source/sc_calc_generic_gpu.cu" -o "$OUT/sc_calc_generic_gpu.o" &
 g++ $CXXFLAGS -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o" &

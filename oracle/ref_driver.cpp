@@ -280,4 +280,37 @@ long ref_fit_fqs(void *p, double *out, long cap) {
     return n;
 }
 
+// Training-data randomisation then calculation, as the generator does per
+// image (Source/sc_mainCons.cpp:1170, :1236-1246): the handle's values are
+// applied, the saved TPV state is cleared, the C library's generator is
+// seeded, tpvPerformRandom (sc_calc_generic_cpu.cpp:1028) randomises the
+// entries of ids ('\n'-separated "key=value"), and doCalculation runs. Its
+// log text goes to log.
+int ref_tpv_run(void *p, const char *ids, unsigned seed, int nthreads, int ign_cbs, char *log, size_t cap) {
+    RefHandle *h = static_cast<RefHandle *>(p);
+    apply(h);
+    h->calc->tpvPerformRandom(std::list<std::string>());
+    std::list<std::string> lst;
+    std::string cur;
+    for (const char *c = ids; *c; c++) {
+        if (*c == '\n') {
+            if (!cur.empty()) lst.push_back(cur);
+            cur.clear();
+        } else {
+            cur += *c;
+        }
+    }
+    if (!cur.empty()) lst.push_back(cur);
+    srand(seed);
+    const std::string rv = h->calc->tpvPerformRandom(lst);
+    if (log && cap) {
+        std::strncpy(log, rv.c_str(), cap - 1);
+        log[cap - 1] = 0;
+    }
+    if (nthreads < 1) nthreads = 1;
+    h->calc->doCalculation(nthreads, false, ign_cbs != 0);
+    h->err = h->calc->getLastErrorMessage();
+    return h->err.empty() ? 0 : 1;
+}
+
 }  // extern "C"

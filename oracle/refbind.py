@@ -56,6 +56,9 @@ def _bind(lib):
     lib.ref_get_latpar.argtypes = [V, ctypes.c_int, ctypes.c_void_p]
     lib.ref_set_fit_data.argtypes = [V, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
     lib.ref_set_nofit_rect.argtypes = [V] + [ctypes.c_int] * 5
+    if hasattr(lib, "ref_tpv_run"):
+        lib.ref_tpv_run.argtypes = [V, ctypes.c_char_p, ctypes.c_uint, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+                                    ctypes.c_size_t]
     lib.ref_fit.argtypes = [V, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_long),
                             ctypes.POINTER(ctypes.c_long)]
     lib.ref_fit.restype = ctypes.c_double
@@ -88,6 +91,14 @@ class RefCalc:
     def run(self, nthreads=1, ign_new_switch=False, ign_cbs=False):
         rc = self.lib.ref_run(self.h, int(nthreads), int(ign_new_switch), int(ign_cbs))
         return rc, self.lib.ref_error(self.h).decode()
+
+    def tpv_run(self, ids, seed, nthreads=1, ign_cbs=False):
+        """(status, log text) of tpvPerformRandom(ids) after srand(seed), then
+        the calculation (oracle/ref_driver.cpp ref_tpv_run)."""
+        buf = ctypes.create_string_buffer(4096)
+        rc = self.lib.ref_tpv_run(self.h, "\n".join(ids).encode(), int(seed), int(nthreads), int(ign_cbs), buf,
+                                  len(buf))
+        return rc, buf.value.decode()
 
     def dims(self):
         d = [ctypes.c_int() for _ in range(4)]
