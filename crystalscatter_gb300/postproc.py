@@ -32,11 +32,10 @@ F32 = np.float32
 def scale_and_clip(a, scale=False, clip=False, clip40=False):
     """scaleAndClipData without the log option, in place; returns a."""
     if scale:
-        m = 0.0
-        for v in a.reshape(-1):
-            if m < v:
-                m = v
-        a /= m
+        # the reference's running maximum from 0 (NaN entries never win)
+        m = float(np.nanmax(a, initial=0.0)) if a.size else 0.0
+        with np.errstate(divide="ignore", invalid="ignore"):
+            a /= m
     if clip:
         with np.errstate(divide="ignore"):
             a[:] = ((np.log(np.abs(a) / 1e-20) / math.log(10)) + 6.0) / 6.0
