@@ -19,11 +19,17 @@ LIB = os.path.join(OUT, "libcrystalscatter.so")
 
 HOST_SOURCES = ["cs_prep.cpp", "cs_params.cpp", "cs_capi.cpp", "cs_batch.cpp", "cs_simplex.cpp"]
 CUDA_SOURCES = ["cs_kernels.cu", "cs_mixed.cu", "cs_noalloc.cu", "cs_mlp.cu"]
+# cs_fp64_unit.cu is compiled once per dispatch key (the FP64 drop-in kernels
+# of that key), so that the keys' kernels compile in parallel
+FP64_UNIT = "cs_fp64_unit.cu"
+UNIT_KEYS = ["CS_KEY_SPHERE_NONE_ISO", "CS_KEY_SPHERE_GAUSS_FCC_GAUSS", "CS_KEY_CYL_NONE_GAUSS",
+             "CS_KEY_CYL_NONE_ZDIR", "CS_KEY_CYL_GAUSS_BCT_ZDIR", "CS_KEY_CUBE_NONE_ISO", "CS_KEY_GENERIC"]
 # No automatic multiply-add contraction in either unit: the FP64 drop-in keeps
 # the reference's separate multiply and add roundings, and the mixed kernels
 # share its FP64 functions (pixel geometry, power series, math library calls),
 # which must round identically there; FP32 code asks for fmaf where it wants one
-FMAD = {"cs_kernels.cu": "false", "cs_mixed.cu": "false", "cs_noalloc.cu": "false", "cs_mlp.cu": "true"}
+FMAD = {"cs_kernels.cu": "false", "cs_mixed.cu": "false", "cs_noalloc.cu": "false", "cs_mlp.cu": "true",
+        FP64_UNIT: "false"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -65,14 +71,19 @@ def build(verbose=False, force=False):
         if force or _stale(obj, [src] + headers):
             jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I" + cuda_inc,
                          "-c", src, "-o", obj])
-    for f in CUDA_SOURCES:
+    units = [(f, f + ".o", []) for f in CUDA_SOURCES]
+    units += [(FP64_UNIT, "cs_fp64_unit_" + k[len("CS_KEY_"):].lower() + ".o", ["-DCS_UNIT_KEY=" + k])
+              for k in UNIT_KEYS]
+    for f, oname, defs in units:
         src = os.path.join(SRC, f)
-        obj = os.path.join(OUT, f + ".o")
+        obj = os.path.join(OUT, oname)
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([_nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=" + FMAD[f],
-                         "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills", "-c", src, "-o", obj])
-    with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
+            jobs.append([_nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=" + FMAD[f]] + defs +
+                        ["-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills", "-c", src, "-o", obj])
+    # longest units first (the generic pixel function's kernels)
+    jobs.sort(key=lambda j: 0 if any("GENERIC" in a for a in j) else 1)
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:
         for o in outs:

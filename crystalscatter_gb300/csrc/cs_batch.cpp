@@ -225,7 +225,7 @@ int enqueue(cs_batch *b, double *d_out, cudaStream_t s, int mode, int schedule) 
                          ? cs::launch_batch_mixed(b->dsets, g, (int)gi, b->d_counters + gi, b->d_chi, d_out, b->redo,
                                                   (int)grid, s)
                          : cs::launch_batch_fp64(b->dsets, g, b->d_counters + gi, b->d_chi, d_out, (int)grid, s);
-            if (rc == CS_ERR_CUDA) return cuda_fail(b, cudaGetLastError(), "batch kernel launch");
+            if (rc == CS_ERR_CUDA) return cuda_fail(b, cs::last_launch_error(), "batch kernel launch");
             if (rc) return fail(b, rc, "no batch kernel for this combination");
         }
     } else if (schedule == CS_SCHED_PLAIN) {
@@ -254,7 +254,7 @@ int enqueue(cs_batch *b, double *d_out, cudaStream_t s, int mode, int schedule) 
             } else {
                 rc = cs::launch_image(D, P, out, s);  // mirrors expanded quadrants itself
             }
-            if (rc == CS_ERR_CUDA) return cuda_fail(b, cudaGetLastError(), "kernel launch");
+            if (rc == CS_ERR_CUDA) return cuda_fail(b, cs::last_launch_error(), "kernel launch");
             if (rc) return fail(b, rc, "no kernel for this combination");
         }
         return CS_OK;
@@ -755,7 +755,7 @@ int cs_batch_fit_chi2(cs_batch *b, int mode, double *chi2, long *cnt, long *nanc
         e = cudaStreamEndCapture(b->stream, &g);
         if (rc != CS_OK) {
             if (g) cudaGraphDestroy(g);
-            return rc == CS_ERR_CUDA ? cuda_fail(b, cudaGetLastError(), "fit evaluation") : rc;
+            return rc == CS_ERR_CUDA ? cuda_fail(b, cs::last_launch_error(), "fit evaluation") : rc;
         }
         if (e != cudaSuccess) return cuda_fail(b, e, "cudaStreamEndCapture");
         e = cudaGraphInstantiate(&b->fit_exec, g, 0);

@@ -56,6 +56,9 @@ struct cs_handle {
     size_t peak_cap = 0;
     cs::MixedScratch mscratch;
     size_t redo_cap = 0;
+    // redo counter of the last launch (the handle's own scratch or the
+    // allocation-free launch's static one); null after an FP64 launch
+    const int *last_count = nullptr;
 
     // fit
     double *dfit = nullptr, *dfqs = nullptr;
@@ -253,11 +256,13 @@ int run_image(cs_handle *h, double *d_out, cudaStream_t s, int mode) {
     }
     int rc;
     if (mode == CS_MODE_FP64) {
+        h->last_count = nullptr;
         rc = cs::launch_image(D, *h->hprep, d_out, s);
     } else if (mode == CS_MODE_MIXED && (!cs::mixed_key(h->hprep->key) || h->hprep->twin)) {
         // no mixed-precision kernel for this combination: the FP64 kernel
         // serves the request (no pixel needs a redo)
         if (h->mscratch.d_count) cudaMemsetAsync(h->mscratch.d_count, 0, sizeof(int), s);
+        h->last_count = h->mscratch.d_count;
         rc = cs::launch_image(D, *h->hprep, d_out, s);
     } else if (mode == CS_MODE_MIXED) {
         if ((rc = ensure_mixed(h))) return rc;
@@ -272,15 +277,15 @@ int run_image(cs_handle *h, double *d_out, cudaStream_t s, int mode) {
             T.iq = h->d_iq;
             T.imf = h->d_imf;
         }
+        h->last_count = h->mscratch.d_count;
         rc = cs::launch_image_mixed(D, T, *h->hprep, d_out, h->mscratch, s);
         if (rc == CS_ERR_UNSUPPORTED) return fail(h, rc, "no mixed-precision kernel for this combination");
     } else {
         return fail(h, CS_ERR_PARAM, "unknown precision mode");
     }
-    if (rc != CS_OK) {
-        cudaError_t e = cudaGetLastError();
-        return rc == CS_ERR_CUDA ? cuda_fail(h, e, "kernel launch") : fail(h, rc, "no kernel for this combination");
-    }
+    if (rc != CS_OK)
+        return rc == CS_ERR_CUDA ? cuda_fail(h, cs::last_launch_error(), "kernel launch")
+                                 : fail(h, rc, "no kernel for this combination");
     return CS_OK;
 }
 
@@ -436,7 +441,8 @@ int cs_launch_prepared_mixed_noalloc(cs_handle *h, double *d_out, size_t n_doubl
                       npix, CS_NOALLOC_MAX_PIXELS);
         return fail(h, CS_ERR_SIZE, buf);
     }
-    if (P.lattice && !h->peaks_valid)
+    const bool fp64_kernel = !cs::mixed_key(P.key) || P.twin;
+    if (P.lattice && !fp64_kernel && !h->peaks_valid)
         return fail(h, CS_ERR_STATE,
                     "reflection tables of this preparation are not on the device: run one CS_MODE_MIXED calculation "
                     "on it first");
@@ -457,21 +463,32 @@ int cs_launch_prepared_mixed_noalloc(cs_handle *h, double *d_out, size_t n_doubl
         if ((e = cudaMemsetAsync(d_out, 0, sizeof(double) * image_count(h), s)) != cudaSuccess)
             return cuda_fail(h, e, "cudaMemsetAsync");
     }
-    csm::PeakTab T;
-    if (P.lattice) {
-        T.n_aniso = (int)h->hpeaks.aq.size();
-        T.aq = h->d_aq;
-        T.av = h->d_av;
-        T.amf = h->d_amf;
-        T.aidx = h->d_aidx;
-        T.n_iso = (int)h->hpeaks.iq.size();
-        T.iq = h->d_iq;
-        T.imf = h->d_imf;
+    h->last_count = S.d_count;
+    int rc;
+    if (fp64_kernel) {
+        // no mixed-precision kernel for this combination: the FP64 kernel
+        // serves the request exactly as cs_launch_prepared(..., CS_MODE_MIXED)
+        // does (it needs no scratch; the static counter reads 0 redone pixels)
+        if ((e = cudaMemsetAsync(S.d_count, 0, sizeof(int), s)) != cudaSuccess)
+            return cuda_fail(h, e, "cudaMemsetAsync(redo counter)");
+        rc = cs::launch_image(D, P, d_out, s);
+    } else {
+        csm::PeakTab T;
+        if (P.lattice) {
+            T.n_aniso = (int)h->hpeaks.aq.size();
+            T.aq = h->d_aq;
+            T.av = h->d_av;
+            T.amf = h->d_amf;
+            T.aidx = h->d_aidx;
+            T.n_iso = (int)h->hpeaks.iq.size();
+            T.iq = h->d_iq;
+            T.imf = h->d_imf;
+        }
+        // clears the static counter on s, then the mixed kernel and the FP64 redo
+        rc = cs::launch_image_mixed(D, T, P, d_out, S, s);
     }
-    // clears the static counter on s, then the mixed kernel and the FP64 redo
-    const int rc = cs::launch_image_mixed(D, T, P, d_out, S, s);
-    if (rc == CS_ERR_UNSUPPORTED) return fail(h, rc, "no mixed-precision kernel for this combination");
-    if (rc != CS_OK) return cuda_fail(h, cudaGetLastError(), "kernel launch");
+    if (rc == CS_ERR_CUDA) return cuda_fail(h, cs::last_launch_error(), "kernel launch");
+    if (rc != CS_OK) return fail(h, rc, "no kernel for this combination");
     return CS_OK;
 }
 
@@ -582,7 +599,8 @@ int cs_fit_chi2(cs_handle *h, int num_threads, int bstop, int border, int mode, 
         return cuda_fail(h, e, "cudaMemsetAsync(fqs)");
     D.d_prep = h->dprep;
     rc = cs::launch_fit(D, P, h->dfit, h->dfqs, nbuf, h->red, h->stream);
-    if (rc != CS_OK) return fail(h, rc, "fit kernel launch failed");
+    if (rc == CS_ERR_CUDA) return cuda_fail(h, cs::last_launch_error(), "fit kernel launch");
+    if (rc != CS_OK) return fail(h, rc, "no fit kernel for this combination");
     double s = 0;
     unsigned long long c = 0, nn = 0;
     cudaMemcpyAsync(&s, h->red.d_sum, sizeof(double), cudaMemcpyDeviceToHost, h->stream);
@@ -601,10 +619,10 @@ const char *cs_last_error(cs_handle *h) { return h ? h->err.c_str() : "null hand
 int cs_mixed_redo_pixels(cs_handle *h, long *n) {
     if (!h || !n) return CS_ERR_PARAM;
     *n = 0;
-    if (!h->mscratch.d_count) return CS_OK;
+    if (!h->last_count) return CS_OK;
     int v = 0;
     cudaStreamSynchronize(h->stream);
-    cudaError_t e = cudaMemcpy(&v, h->mscratch.d_count, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpy(&v, h->last_count, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(h, e, "read redo count");
     *n = v;
     return CS_OK;

@@ -1093,7 +1093,9 @@ __device__ inline double formpq_disk(const cs_prepared &P, double limql, double 
 // orientation, z-direction disks along an axis without a lattice, vesicles,
 // homogeneous isotropic cubes and ellipsoids), any supported lattice and the
 // peak shapes 1-7 (the reference's shape 7 falls to its `default: return 0`).
-__device__ inline double calc_generic(const Ctx &C, double qx, double qy, double qz) {
+// (not inlined: the five kernels of the generic key share one copy, which
+// keeps that unit's compile time down)
+static __device__ __noinline__ double calc_generic(const Ctx &C, double qx, double qy, double qz) {
     const cs_prepared &P = *C.P;
     double pq = 0, fq = 0, intensity, radintensity;
     const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;  // :33

@@ -26,6 +26,14 @@ struct FitReduce {
     unsigned long long *d_cnt = nullptr, *d_nan = nullptr;
 };
 
+// The CUDA error seen by the most recent launcher in this host thread
+// (cudaSuccess after a good launch). Launchers end with launch_status(),
+// which reads cudaGetLastError() once, records the code here and returns
+// CS_OK or CS_ERR_CUDA; callers build their message from this code (a second
+// cudaGetLastError() would already read cudaSuccess).
+cudaError_t last_launch_error();
+int launch_status();
+
 bool key_supported(const cs_prepared &P);
 // keys with a mixed-precision kernel; the others (and twinned lattices) run
 // their FP64 kernel when mixed precision is requested (exact, so within any

@@ -1391,7 +1391,7 @@ int launch_image_mixed(const DevSet &D, const csm::PeakTab &T, const cs_prepared
     default: return CS_ERR_UNSUPPORTED;
     }
     if (P.expand && P.calc_quadrants != CS_RADQ4 && P.calc_quadrants != CS_RAD1D) launch_mirror(P, d_out, s);
-    return cudaGetLastError() == cudaSuccess ? CS_OK : CS_ERR_CUDA;
+    return launch_status();
 }
 
 
@@ -1412,10 +1412,10 @@ int launch_batch_mixed(const BatchSetDev *d_sets, const BatchGroup &g, int group
 #undef CS_CASE
     default: return CS_ERR_UNSUPPORTED;
     }
-    if (cudaGetLastError() != cudaSuccess) return CS_ERR_CUDA;
+    if (launch_status() != CS_OK) return CS_ERR_CUDA;
     if (g.key == CS_KEY_CYL_NONE_GAUSS) {
         csm::k_batch_redo_cyl_warp<<<sm_count_m() * 4, 128, 0, s>>>(d_sets, d_chi, d_out, cnt, list, R.cap);
-        return cudaGetLastError() == cudaSuccess ? CS_OK : CS_ERR_CUDA;
+        return launch_status();
     }
     return launch_batch_redo(d_sets, g.key, d_chi, d_out, cnt, list, R.cap, s);
 }

@@ -82,10 +82,17 @@ class TpvRandom:
         if not ids:
             self.clear()
             p.tpv_domain_dev = 0.0
+            # the reference's next parameter load overwrites its randomised
+            # dwfactor; here the draw is a separate factor, reset with the rest
+            p.tpv_dw_dev = 0.0
             return "TPV: clear"
         if self.old is None:
             self.old = {f: getattr(p, f) for f, _ in _KEYS.values() if f and not f.startswith("tpv_")}
             self.old["tpv_domain_dev"] = 1.0  # width factor at the first call
+            # the azimuthal width and the displacement are restored from their
+            # values at the first call before every draw (hlp->oldval)
+            self.old["azi"] = p.azi
+            self.old["debyewaller"] = p.debyewaller
         out = ""
         for entry in ids:
             key, _, val = entry.partition("=")
@@ -117,8 +124,10 @@ class TpvRandom:
                 p.phi = v
             elif kind == "azi":
                 # phiwidth = 4/aziwidth * (1 + dval*zuf), recomputed by the preparation
+                p.azi = self.old["azi"]
                 v = 4.0 / p.azi * (1 + dval * zuf())
             else:  # dw
+                p.debyewaller = self.old["debyewaller"]
                 z = zuf()
                 v = p.debyewaller * p.debyewaller / 3.0 * (1 + dval * z)
                 p.tpv_dw_dev = dval * z

@@ -159,7 +159,11 @@ int cs_launch_prepared(cs_handle *h, double *d_out, size_t n_doubles, void *stre
      the static array (cudaGetSymbolAddress), which may load the library's
      device module. Make that first call before any stream capture.
    - The static list is cleared (a memset on `stream`) at the start of every
-     call; the result is the same as cs_launch_prepared(..., CS_MODE_MIXED).
+     call; the result is the same as cs_launch_prepared(..., CS_MODE_MIXED),
+     also for combinations without a mixed-precision kernel (twinned
+     lattices, the generic pixel function, cubes), which run their FP64
+     kernel there as here. cs_mixed_redo_pixels then reports this launch's
+     redo count (read from the static counter).
    - There is one static list per device: calls whose work overlaps on the GPU
      (other streams, other handles, other threads) race on it. Order them on
      one stream or synchronise between them. */
@@ -179,7 +183,8 @@ const char *cs_last_error(cs_handle *h);
 
 /* Pixels of the last mixed-precision calculation whose FP32 result sat inside
    a decision guard band and were recomputed in FP64 (no counterpart in the
-   reference; reported alongside accuracy figures). */
+   reference; reported alongside accuracy figures). It covers the handle's
+   last launch of either mixed entry point; after an FP64 launch it is 0. */
 int cs_mixed_redo_pixels(cs_handle *h, long *n);
 
 /* Host preparation alone, without any CUDA call (the reference's private

@@ -6,9 +6,11 @@
 # translation units below in place. The .cu file is compiled as plain C++,
 # which leaves exactly the reference's CPU path (no __CUDACC__).
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# The reference root is the argument, else $CS_REFERENCE_ROOT, else
+# /root/reference. Exit status 3: no reference sources there (nothing built).
 set -e
-REF="${1:-/root/reference}"
+REF="${1:-${CS_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/Source/sc_calc_generic_cpu.cpp" ]; then

@@ -74,6 +74,26 @@ def test_tpv_clear_and_repeat():
     assert t.perform(p, []) == "TPV: clear" and p.tpv_domain_dev == 0.0
 
 
+def test_tpv_dw_and_azi_restore_first_values():
+    p = _params(C.scaled(C.SPHERE_FCC, 8))
+    dw0, azi0 = p.debyewaller, p.azi
+    t = tpv.TpvRandom()
+    tpv.srand(5)
+    t.perform(p, ["EditDebyeWaller=0.4", "EditAzi=0.2"])
+    assert p.tpv_dw_dev != 0.0
+    # a caller changes both between calls without clearing: the next draw
+    # starts again from the values saved at the first call, as the reference's
+    # hlp->oldval does
+    p.debyewaller, p.azi = 2 * dw0, 3 * azi0
+    log = t.perform(p, ["EditDebyeWaller=0.4", "EditAzi=0.2"])
+    assert p.debyewaller == dw0 and p.azi == azi0
+    v_dw = float(log.split("EditDebyeWaller = ")[1].split()[0])
+    assert abs(v_dw / (dw0 * dw0 / 3.0) - 1) <= 0.4 + 1e-6
+    # clearing resets both randomised factors
+    assert t.perform(p, []) == "TPV: clear"
+    assert p.tpv_dw_dev == 0.0 and p.tpv_domain_dev == 0.0
+
+
 def test_tpv_length_adjustments():
     p = _params(dict(C.scaled(C.SPHERE, 8), ComboBoxParticle=2, EditRadius=10.0, Length=5.0))
     tpv.TpvRandom().perform(p, ["I0=0.0001"])

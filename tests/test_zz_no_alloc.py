@@ -4,8 +4,10 @@ CS_MODE_MIXED) on the same prepared handle: two calls in a row, each within
 the mixed path's 1e-5 bar (the same kernels run, so the images agree exactly
 in practice). Also its documented rejections: images beyond the fixed scratch
 (CS_ERR_SIZE) and a lattice preparation whose reflection tables were never
-uploaded by a mixed call (CS_ERR_STATE). Independent of test order: the static
-scratch is cleared by every call."""
+uploaded by a mixed call (CS_ERR_STATE). Combinations without a mixed kernel
+(generic pixel function, twinned lattice, cube) run the FP64 kernel through
+both entry points. Independent of test order: the static scratch is cleared by
+every call."""
 import ctypes
 
 import numpy as np
@@ -40,6 +42,10 @@ CASES = {
     "sphere_fcc_128": C.scaled(C.SPHERE_FCC, 64),             # lattice: reflection tables
     "cyl_gauss_x_64": C.scaled(C.CYL_GAUSS_X, 32),            # orientation average with FP64 redo
     "sphere_q1_expand_64": dict(C.scaled(C.SPHERE, 32), RadioButtonQ1=1, RadioButtonQ4=0, ExpandImage=1),
+    # combinations without a mixed kernel: both entry points run the FP64 kernel
+    "ellipsoid_generic_64": dict(C.scaled(C.SPHERE, 32), ComboBoxParticle=5, Ordis=7, Length=16.0),
+    "sphere_fcc_twin_48": dict(C.scaled(C.SPHERE_FCC, 24), LType=4, CheckBoxTwinned=1, EditCeff=0.7),
+    "cube_64": dict(C.scaled(C.SPHERE, 32), ComboBoxParticle=4),
 }
 
 
@@ -51,6 +57,7 @@ def test_noalloc_matches_existing_entry_twice(name):
     c.setParams(CASES[name])
     c.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)  # existing entry point
     ref = c.data()
+    redo_ref = c.mixed_redo_pixels()
     n = ref.size
     d = torch.empty(n, dtype=torch.float64, device="cuda")
     s = torch.cuda.Stream()
@@ -64,6 +71,8 @@ def test_noalloc_matches_existing_entry_twice(name):
         worst, same_class = rel(got, ref)
         assert same_class, name
         assert worst <= TOL, (name, worst)
+        # the redo count now comes from the static counter of this launch
+        assert c.mixed_redo_pixels() == redo_ref, name
     c.cleanup()
 
 
