@@ -2,23 +2,39 @@
 """Benchmark: detector pixels per second of the 2D scattering-pattern
 calculation on one GB300 (or N replicas on N GPUs).
 
-Workload (one step = one full image): cylinders, no lattice, Gaussian
-orientation (pCyl_lNon_oGau), 512x512 detector, pixel 0.5 mm, 4 m, 0.6 nm,
-radius 5 nm / length 60 nm (Schulz sigma 0.10), axis in the detector plane at
-azimuth 30 deg, orientation width 15 deg (crystalscatter_gb300.configs
-"cyl_gauss"). Reported:
+Headline workload (one step = one pass over the whole batch): the batched
+sweep of cylinders on a BCT lattice with z-direction orientation
+(pCyl_pGau_lBCT_oZDi), 4096 seeded parameter sets of detector size
+128^2..1024^2 (crystalscatter_gb300.configs.bct_sweep: radius, length, lattice
+constants, Schulz widths and orientation width drawn per set), wavelength
+0.154 nm, 3 m, pixel 0.172 mm, HKLmax 3 -- 1.41e9 pixels per step. The
+mixed-precision kernels run all sets in one persistent launch per step,
+replayed as a CUDA graph. Reported:
 
-* value   pixels/s with the prepared parameter set resident in device memory
-          (kernel launches only), summed over all ranks
-* e2e     pixels/s through the drop-in call with host buffers: host
-          preparation, upload of the prepared block, kernel, image download
-* roofline / cpu_baseline / clocks as the benchmark contract asks
-* extra   per-workload kernel rates for the other workloads (sphere, the
-          x-axis cylinder that runs the full orientation integral, FCC)
+* value        pixels/s of the graph replays with the prepared batch resident
+               in device memory, summed over all ranks
+* e2e          the same through the C-ABI host-buffer batch call: host
+               parameters in, host preparation, upload, kernels, download of
+               all images into pinned host memory, per step
+* roofline     the dominant kernel (k_batch_mixed of the sweep's key) against
+               the measured issue rate of the pipe that bounds it
+               (cs_measure_pipe_peaks), from its executed instructions per
+               pixel (ncu, crystalscatter_gb300/kernel_work.json) and its
+               CUDA-event duration measured here
+* accuracy     mixed vs the FP64 GPU drop-in over every pixel of the sweep,
+               and vs the CPU oracle (the reference's algorithm in C, on the
+               reference's own prepared constants) on 64 sample sets
+* configs      per configuration (sphere 256^2, cylinder 512^2 at phi = 30 and
+               phi = 0, FCC spheres 1024^2): mixed and FP64 kernel rates,
+               accuracy vs FP64 and vs the CPU oracle, a CPU baseline
+* cpu_baseline the CPU oracle on all host cores on a bounded sample of the
+               sweep (64 reference-prepared sample sets)
 
 ``--impl reference`` times the reference's algorithm on the host cores: the
-CPU port of the reference in oracle/ (the reference's own sources cannot be
-built on the GPU host), with all host threads, on the same workload.
+CPU oracle (oracle/cs_oracle.c, the reference's per-pixel code restated in C;
+the reference's own sources cannot travel to the GPU host) on the
+reference-prepared sample sets of the same sweep, all host threads, one
+sample set per step. It loads no part of this library.
 """
 import argparse
 import json
@@ -33,7 +49,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "pixels/s at <=1e-5 rel err vs FP64"
 UNIT = "pixels/s"
-WORKLOAD = "cyl_gauss"
+SINGLE = ("sphere", "cyl_gauss", "cyl_gauss_x", "sphere_fcc")
+WORKLOAD_TEXT = {
+    "sphere": "pSph_lNon_oIso 256x256 (sphere r=10, sigma 0.10)",
+    "cyl_gauss": "pCyl_lNon_oGau 512x512 (cylinder r=5 L=60, Gaussian 15 deg, phi=30)",
+    "cyl_gauss_x": "pCyl_lNon_oGau 512x512 (the same at phi=0: full orientation integral)",
+    "sphere_fcc": "pSph_pGau_lFCC_oGau 1024x1024 (sphere r=8 on FCC a=40, HKLmax 5)",
+}
 
 
 def parse():
@@ -42,16 +64,19 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--no-extra", action="store_true")
+    ap.add_argument("--sweep-sets", type=int, default=4096, help="parameter sets of the headline sweep")
+    ap.add_argument("--e2e-steps", type=int, default=2, help="steps of the host-buffer (e2e) timing")
+    ap.add_argument("--no-extra", action="store_true", help="skip the per-config table")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison legs of the sweep")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--sweep-sets", type=int, default=4096, help="parameter sets of the batched sweep (0 = skip)")
-    ap.add_argument("--sweep-steps", type=int, default=2)
     ap.add_argument("--surrogate", default="", help="surrogate-seeded fits of this family ('2', '2x'); off by default")
     ap.add_argument("--surrogate-train", type=int, default=32768)
     ap.add_argument("--surrogate-epochs", type=int, default=200)
     ap.add_argument("--surrogate-targets", type=int, default=8)
     return ap.parse_args()
 
+
+# ------------------------------------------------------------------ helpers
 
 def max_over_ranks(values, world, device):
     """Per-rank timings reduced to their maximum over the ranks (the job's
@@ -77,6 +102,23 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def sweep_pixels(nsets):
+    """Calculated pixels of the first nsets sweep sets (N^2 each), from the
+    seeded parameter draws alone."""
+    from crystalscatter_gb300 import configs as C
+    return sum(C.bct_set(k)["EditPixelNoX"] ** 2 for k in range(nsets))
+
+
+def headline_config(nsets, world):
+    """The workload description both arms print (identical by construction)."""
+    return {"workload": f"pCyl_pGau_lBCT_oZDi batched sweep: {nsets} seeded parameter sets (configs.bct_set), "
+                        f"detector 128^2..1024^2, 0.154 nm, 3 m, HKLmax 3",
+            "sets_per_step": nsets, "pixels_per_step": sweep_pixels(nsets),
+            "mode": "mixed FP32/FP64, <=1e-5 vs FP64",
+            "l2": "no flush: each step writes the whole image buffer (11.3 GB for 4096 sets, > 129 MB L2)",
+            "parallelism": f"replicas x{world}"}
 
 
 class ClockSampler:
@@ -132,20 +174,130 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def load_peaks():
-    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            d = json.load(f)
-        return float(d.get("hbm_gbs", 6800.0)), "measured"
-    return 6800.0, "fallback"
+def rel_stats(img, ref, cond=None):
+    """max / median / p99.99 of |img - ref| / max(|ref|, tau), tau = 1e-30
+    max|ref|, over pixels finite in both; non-finite class mismatches counted.
+    With a conditioning map: the count of ill-conditioned pixels (the
+    reference's own value moves by more than 1e-12 / 1e-6 under one-ulp
+    changes of the math library) and the maximum over the others."""
+    import numpy as np
+    fin_r = np.isfinite(ref)
+    tau = 1e-30 * (np.max(np.abs(ref[fin_r])) if fin_r.any() else 1.0)
+    with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
+        rel = np.abs(img - ref) / np.maximum(np.abs(ref), tau)
+    fin = fin_r & np.isfinite(img)
+    mism = int((np.isnan(ref) != np.isnan(img)).sum() + ((np.isinf(ref) | np.isinf(img)) & (ref != img)).sum())
+    r = rel[fin]
+    out = {"pixels": int(ref.size), "max": float(r.max()) if r.size else 0.0,
+           "median": float(np.median(r)) if r.size else 0.0,
+           "p99_99": float(np.quantile(r, 0.9999)) if r.size else 0.0, "nonfinite_mismatch": mism}
+    if cond is not None:
+        good = fin & (cond <= 1e-6)
+        out["ill_conditioned_1e-12"] = int((cond > 1e-12).sum())
+        out["ill_conditioned_1e-6"] = int((cond > 1e-6).sum())
+        out["max_where_cond_le_1e-6"] = float(rel[good].max()) if good.any() else 0.0
+    return out
 
+
+def rel_stats_device(img, ref):
+    """rel_stats (without conditioning) of two device tensors, chunked."""
+    import torch
+    fin_r = torch.isfinite(ref)
+    amax = torch.where(fin_r, ref.abs(), torch.zeros_like(ref)).max().item()
+    tau = 1e-30 * (amax if amax > 0 else 1.0)
+    mx, mism, n = 0.0, 0, 0
+    sample = []
+    step = 1 << 27
+    for a in range(0, ref.numel(), step):
+        r = ref[a:a + step]
+        g = img[a:a + step]
+        fin = torch.isfinite(r) & torch.isfinite(g)
+        rel = ((g - r).abs() / torch.clamp(r.abs(), min=tau))[fin]
+        if rel.numel():
+            mx = max(mx, rel.max().item())
+            sample.append(rel[:: max(1, rel.numel() // 200000)].cpu())
+        mism += int((torch.isnan(r) != torch.isnan(g)).sum().item())
+        mism += int(((torch.isinf(r) | torch.isinf(g)) & (r != g)).sum().item())
+        n += r.numel()
+    s = torch.cat(sample) if sample else torch.zeros(1, dtype=torch.float64)
+    return {"pixels": n, "max": mx, "median": float(s.median().item()),
+            "p99_99": float(torch.quantile(s.float(), 0.9999).item()), "nonfinite_mismatch": mism,
+            "note": "median and p99.99 from an even subsample of ~200k pixels per 128M"}
+
+
+def cpu_threads():
+    return os.cpu_count() or 1
+
+
+def load_kernel_work():
+    p = os.path.join(ROOT, "crystalscatter_gb300", "kernel_work.json")
+    if not os.path.exists(p):
+        return {}
+    with open(p) as f:
+        return json.load(f)
+
+
+def roofline(work, key, pixels, seconds, peaks, traffic_per_pixel=None):
+    """Compute roofline of one kernel launch: executed FP32 / FP64 flops and
+    special-function ops per pixel (ncu counts, kernel_work.json) times the
+    pixels of the launch over its CUDA-event duration, against the measured
+    pipe peaks; the bound is the pipe with the largest fraction."""
+    w = work.get(key)
+    if not w:
+        return None
+    fp32_peak = max(peaks["fp32_tflops"], peaks["fp32x2_tflops"])
+    rates = {
+        "fp32": (w["fp32_flops_per_pixel"] * pixels / seconds / 1e12, fp32_peak, "TFLOP/s"),
+        "fp64": (w["fp64_flops_per_pixel"] * pixels / seconds / 1e12, peaks["fp64_tflops"], "TFLOP/s"),
+        "sfu": (w["mufu_ops_per_pixel"] * pixels / seconds / 1e12, peaks["mufu_tops"], "Tops/s"),
+    }
+    bound = max(rates, key=lambda k: rates[k][0] / rates[k][1])
+    a, p, u = rates[bound]
+    t = w.get("dram_bytes_per_pixel")
+    return {"bound": bound, "achieved": a, "peak": p, "unit": u, "frac": a / p,
+            "traffic": (t * pixels) if t is not None else None,
+            "algorithmic_bytes": 8.0 * pixels,
+            "pipes": {k: {"achieved": v[0], "peak": v[1], "unit": v[2], "frac": v[0] / v[1]} for k, v in rates.items()},
+            "kernel": w.get("kernel"), "kernel_ms": seconds * 1e3, "pixels": pixels,
+            "peaks": "measured here (cs_measure_pipe_peaks: FFMA, FFMA2, DFMA, MUFU.EX2 chains)",
+            "work_source": w.get("source")}
+
+
+# ------------------------------------------------------------ CPU baseline
+
+def cpu_baseline_blocks(names, seconds, whole=True):
+    """The CPU oracle on all host cores over reference-prepared blocks, whole
+    images, cycling through `names` until `seconds` elapse."""
+    from oracle import ref_prepared as R
+    blocks = [R.load(n) for n in names]
+    nt = cpu_threads()
+    t0 = time.perf_counter()
+    pix, reps, i = 0, 0, 0
+    while True:
+        _, n = blocks[i % len(blocks)].image(nt)
+        pix += n
+        reps += 1
+        i += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": pix / dt, "unit": UNIT, "cores": nt, "kind": "port",
+            "sample": f"{reps} whole images ({pix} pixels) of {len(blocks)} reference-prepared parameter set(s), "
+                      f"{dt:.1f} s, the reference's per-pixel algorithm restated in C (oracle/cs_oracle.c), "
+                      f"rows over {nt} host threads"}
+
+
+def sweep_sample_names():
+    from oracle import ref_prepared as R
+    return [f"bct_set{k:04d}" for k in R.sweep_sample()]
+
+
+# --------------------------------------------------------------- native arm
 
 def time_kernel(calc, torch, d_out, n, steps, warmup, flush, mode=0):
-    """Device-resident launches of the prepared calculation on a dedicated
-    stream: per step an L2 flush outside the timed events, then one launch
-    between two events recorded on that same stream. Returns (total seconds
-    over steps, per-step list)."""
+    """Device-resident launches of the prepared calculation: per step an L2
+    flush outside the timed events, then one launch between two events on the
+    launching stream. Returns (total seconds over steps, per-step list)."""
     stream = torch.cuda.current_stream()
     sp = stream.cuda_stream
     assert sp != 0, "run on a created stream: handle 0 would select the library's own stream"
@@ -165,50 +317,16 @@ def time_kernel(calc, torch, d_out, n, steps, warmup, flush, mode=0):
     return sum(times), times
 
 
-def fp_peaks():
-    """Nominal arithmetic peaks of the GPU from its SM count and clock: FP64
-    (2 DFMA per SM per clock, FMA = 2 flops) and FP32 (128 lanes per SM)."""
-    import torch
-    props = torch.cuda.get_device_properties(torch.cuda.current_device())
-    sms = props.multi_processor_count
-    mhz = 2070.0
-    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(p):
-        with open(p) as f:
-            mhz = float(json.load(f).get("sm_max_mhz", mhz))
-    return {"fp64_tflops": sms * 2 * 2 * mhz * 1e6 / 1e12, "fp32_tflops": sms * 128 * 2 * mhz * 1e6 / 1e12,
-            "sms": sms, "sm_mhz": mhz, "kind": "nominal (SMs x lanes x max clock)"}
-
-
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
-# the headline kernel, k_image_mixed on the 512x512 cylinder, from an ncu
-# capture of three launches on a GB300 (the median; the image stays in L2
-# during the launch and reaches DRAM after it)
-TRAFFIC_BYTES_PER_LAUNCH = 95232
-
-
-def load_ops():
-    p = os.path.join(ROOT, "crystalscatter_gb300", "config_ops.json")
-    with open(p) as f:
-        return json.load(f)["workloads"]
-
-
-def rel_stats(img, ref):
+def config_row(cs, torch, name, flush, steps, cpu_seconds):
+    """Mixed and FP64 kernel rates of one workload; accuracy of mixed vs FP64
+    (GPU) and of both vs the CPU oracle on the reference-prepared block (whole
+    image, or a row sample for the orientation-averaged cylinder); a CPU
+    baseline on that block."""
     import numpy as np
-    with np.errstate(invalid="ignore", divide="ignore"):
-        rel = np.abs(img - ref) / np.maximum(np.abs(ref), 1e-300)
-    fin = np.isfinite(ref) & np.isfinite(img)
-    mism = int(((~np.isfinite(ref)) != (~np.isfinite(img))).sum())
-    r = rel[fin]
-    return {"max": float(r.max()) if r.size else 0.0, "median": float(np.median(r)) if r.size else 0.0,
-            "p99_99": float(np.quantile(r, 0.9999)) if r.size else 0.0, "nonfinite_mismatch": mism}
-
-
-def config_row(cs, torch, name, params, flush, ops, peaks, steps):
-    """Mixed and FP64 kernel rates of one workload, accuracy of mixed vs FP64
-    over the full image, and the compute roofline fractions."""
+    from crystalscatter_gb300 import configs as C
+    from oracle import ref_prepared as R
     c = cs.SasCalc_GENERIC_calculation()
-    c.setParams(params)
+    c.setParams(C.WORKLOADS[name])
     c.doCalculation(0, False, False, mode=cs.CS_MODE_FP64)
     ref = c.data()
     c.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)
@@ -217,76 +335,158 @@ def config_row(cs, torch, name, params, flush, ops, peaks, steps):
     n = img.size
     npix = c.prepared_pixels()
     d = torch.empty(n, dtype=torch.float64, device="cuda")
-    row = {"pixels": npix, "accuracy_mixed_vs_fp64": rel_stats(img, ref), "fp64_redo_pixels": redo}
+    row = {"workload": WORKLOAD_TEXT[name], "pixels": npix, "accuracy_mixed_vs_fp64": rel_stats(img, ref),
+           "fp64_redo_pixels": redo}
     for mname, mode, k in (("mixed", cs.CS_MODE_MIXED, steps), ("fp64", cs.CS_MODE_FP64, max(2, steps // 4))):
         tk, _ = time_kernel(c, torch, d, n, k, 2, flush, mode=mode)
         row[mname + "_pixels_per_s"] = npix * k / tk
         row[mname + "_ms_per_image"] = 1e3 * tk / k
     row["speedup_mixed_over_fp64"] = row["mixed_pixels_per_s"] / row["fp64_pixels_per_s"]
-    fl = ops[name]["flops_per_pixel"]
-    row["compute"] = {"flops_per_pixel": fl,
-                      "fp64_dropin_tflops": row["fp64_pixels_per_s"] * fl / 1e12,
-                      "fp64_dropin_frac_of_fp64_peak": row["fp64_pixels_per_s"] * fl / 1e12 / peaks["fp64_tflops"],
-                      "mixed_tflops": row["mixed_pixels_per_s"] * fl / 1e12,
-                      "mixed_frac_of_fp32_peak": row["mixed_pixels_per_s"] * fl / 1e12 / peaks["fp32_tflops"]}
     c.cleanup()
+    # the CPU oracle on the reference's own prepared constants
+    blk = R.load(name)
+    nt = cpu_threads()
+    if name == "cyl_gauss_x":
+        rows = R.sample_rows(blk, 48)
+        o, _ = blk.image_rows(rows, nt)
+        cond = blk.condition(rows, nt, base=o)
+        sel = np.zeros(blk.shape, dtype=bool)
+        sel[:, np.asarray(rows) - blk.xmin] = True
+        sample = f"{len(rows)} evenly spaced ihex rows ({int(sel.sum())} pixels)"
+    else:
+        o, _ = blk.image(nt)
+        rows = list(range(blk.zzmin, blk.zzmax))
+        cond = blk.condition(rows, nt, base=o)
+        sel = np.ones(blk.shape, dtype=bool)
+        sample = "whole image"
+    row["accuracy_vs_cpu"] = {"sample": sample,
+                              "mixed": rel_stats(img[sel], o[sel], cond[sel]),
+                              "fp64": rel_stats(ref[sel], o[sel], cond[sel])}
+    row["cpu_baseline"] = cpu_baseline_blocks([name], cpu_seconds)
     return row
 
 
-def sweep(cs, torch, C, nsets, ops, peaks, steps):
-    """Config 4: nsets seeded cylinder/BCT parameter sets of detector size
-    128..1024 in one batch; one persistent launch per step (captured as a CUDA
-    graph) against one plain launch per set, in both precision modes."""
+def sweep_accuracy_vs_cpu(b, out_host_view, names, rows_per_set=8):
+    """Mixed sweep images vs the CPU oracle on the reference-prepared sample
+    sets (row samples), with the oracle's conditioning probe."""
     import numpy as np
+    from oracle import ref_prepared as R
+    nt = cpu_threads()
+    gi, ri, ci = [], [], []
+    for name in names:
+        k = int(name[len("bct_set"):])
+        blk = R.load(name)
+        rows = R.sample_rows(blk, rows_per_set)
+        o, _ = blk.image_rows(rows, nt)
+        cond = blk.condition(rows, nt, base=o)
+        off, x0, x1, y0, y1 = b.layout(k)
+        g = out_host_view(off, (x1 - x0) * (y1 - y0)).reshape(y1 - y0, x1 - x0)
+        cols = np.asarray(rows) - blk.xmin
+        gi.append(g[:, cols].ravel())
+        ri.append(o[:, cols].ravel())
+        ci.append(cond[:, cols].ravel())
+    st = rel_stats(np.concatenate(gi), np.concatenate(ri), np.concatenate(ci))
+    st["sample"] = f"{len(names)} reference-prepared sets (k = 0, 64, ..., 4032), {rows_per_set} ihex rows each"
+    return st
+
+
+def sweep(cs, torch, C, args, world, peaks, work, clocks_start):
+    """The headline: the batched BCT sweep. Returns (result dict, timings)."""
+    nsets = args.sweep_sets
     sets = C.bct_sweep(nsets)
+    params = [cs.params_from_mapping(s) for s in sets]
     b = cs.SasCalcBatch()
     t0 = time.perf_counter()
-    b.prepare(sets, bIgnoreCbs=True)
+    b.prepare(params, bIgnoreCbs=True)
     t_prep = time.perf_counter() - t0
     total, npix, groups = b.info()
     out = torch.empty(total, dtype=torch.float64, device="cuda")
     s = torch.cuda.current_stream()
     sp = s.cuda_stream
-
-    def timed(fn, k):
-        fn()
-        s.synchronize()
-        a = torch.cuda.Event(enable_timing=True)
-        e = torch.cuda.Event(enable_timing=True)
-        a.record(s)
-        for _ in range(k):
-            fn()
-        e.record(s)
-        e.synchronize()
-        return a.elapsed_time(e) / 1e3 / k
-
     row = {"sets": nsets, "pixels": npix, "key_groups": groups, "host_prep_s": t_prep,
            "image_buffer_gb": total * 8 / 1e9}
     b.capture(out.data_ptr(), total, mode=cs.CS_MODE_MIXED, schedule=cs.CS_SCHED_PERSISTENT)
     row["graph_nodes_persistent"] = b.graph_nodes()
-    t_graph = timed(lambda: b.replay(sp), steps)
+
+    # timed region: graph replays (persistent mixed kernels + FP64 redo)
+    clocks = clocks_start()
+    for _ in range(args.warmup):
+        b.replay(sp)
+    s.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        a = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        b.replay(sp)
+        e.record(s)
+        e.synchronize()
+        times.append(a.elapsed_time(e) / 1e3)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    t_kernel = sum(times)
     redo, cap = b.redo_pixels(sp)
-    mixed = out.cpu().numpy()
-    t_mp = timed(lambda: b.launch(out.data_ptr(), total, sp, cs.CS_MODE_MIXED, cs.CS_SCHED_PLAIN), 1)
-    t_fp = timed(lambda: b.launch(out.data_ptr(), total, sp, cs.CS_MODE_FP64, cs.CS_SCHED_PERSISTENT), 1)
-    fp64 = out.cpu().numpy()
-    t_fplain = timed(lambda: b.launch(out.data_ptr(), total, sp, cs.CS_MODE_FP64, cs.CS_SCHED_PLAIN), 1)
-    fl = ops["bct_sweep"]["flops_per_pixel"]
-    row.update({
-        "mixed_persistent_graph_s": t_graph, "mixed_persistent_graph_pixels_per_s": npix / t_graph,
-        "mixed_plain_launches_s": t_mp, "fp64_persistent_s": t_fp, "fp64_plain_launches_s": t_fplain,
-        "fp64_plain_launches_pixels_per_s": npix / t_fplain,
-        "speedup_graph_mixed_over_plain_fp64": t_fplain / t_graph,
-        "speedup_persistent_over_plain_fp64": t_fplain / t_fp,
-        "fp64_redo_pixels": redo, "accuracy_mixed_vs_fp64": rel_stats(mixed, fp64),
-        "compute": {"flops_per_pixel_sampled": fl,
-                    "mixed_frac_of_fp32_peak": npix / t_graph * fl / 1e12 / peaks["fp32_tflops"],
-                    "fp64_plain_frac_of_fp64_peak": npix / t_fplain * fl / 1e12 / peaks["fp64_tflops"]},
-        "launches": {"persistent_graph": 2 * groups, "plain": nsets},
-    })
+    # the dominant kernel alone: CUDA events around it on its stream
+    prof = [b.profile(out.data_ptr(), total, sp, cs.CS_MODE_MIXED) for _ in range(2)]
+    main_ms = min(p[0] for p in prof)
+    redo_ms = min(p[1] for p in prof)
+    row.update({"mixed_persistent_graph_s": t_kernel / args.steps, "step_seconds": times,
+                "mixed_kernel_ms": main_ms, "redo_kernel_ms": redo_ms, "fp64_redo_pixels": redo,
+                "launches_per_step": {"persistent_graph": 2 * groups}})
+    # FP64 drop-in: one plain launch per set (the drop-in's own call pattern)
+    if not args.no_fp64:
+        ref = torch.empty_like(out)
+
+        def timed(fn):
+            fn()
+            s.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            e = torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            fn()
+            e.record(s)
+            e.synchronize()
+            return a.elapsed_time(e) / 1e3
+
+        t_fplain = timed(lambda: b.launch(ref.data_ptr(), total, sp, cs.CS_MODE_FP64, cs.CS_SCHED_PLAIN))
+        t_mplain = timed(lambda: b.launch(out.data_ptr(), total, sp, cs.CS_MODE_MIXED, cs.CS_SCHED_PLAIN))
+        b.replay(sp)
+        s.synchronize()
+        row.update({"fp64_plain_launches_s": t_fplain, "fp64_plain_launches_pixels_per_s": npix / t_fplain,
+                    "mixed_plain_launches_s": t_mplain,
+                    "speedup_mixed_graph_over_fp64_plain": t_fplain / (t_kernel / args.steps),
+                    "speedup_persistent_graph_over_plain_mixed": t_mplain / (t_kernel / args.steps),
+                    "accuracy_mixed_vs_fp64": rel_stats_device(out, ref)})
+        row["launches_per_step"]["plain"] = nsets
+        del ref
+    # accuracy vs the CPU oracle on the reference-prepared sample sets
+    host = out.cpu()
+    hv = host.numpy()
+    row["accuracy_vs_cpu"] = sweep_accuracy_vs_cpu(b, lambda o, n: hv[o:o + n], sweep_sample_names())
+    del host, hv
+    # e2e: the C-ABI host-buffer call, host parameters in, images out
+    pinned = torch.empty(total, dtype=torch.float64, pin_memory=True)
+    pv = pinned.numpy()
+    b2 = cs.SasCalcBatch()
+    b2.prepare(params, bIgnoreCbs=True)
+    b2.run_host(cs.CS_MODE_MIXED, out=pv)  # warm-up (allocations)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        b2.prepare(params, bIgnoreCbs=True)
+        b2.run_host(cs.CS_MODE_MIXED, out=pv)
+    t_e2e = time.perf_counter() - t0
+    up = b2.upload_bytes()
+    b2.cleanup()
+    del pinned, pv
     b.cleanup()
     del out
-    return row, redo
+    return row, {"t_kernel": t_kernel, "t_e2e": t_e2e, "npix": npix, "clocks": clk, "main_ms": main_ms,
+                 "upload_bytes": up, "total_doubles": total}
 
 
 def surrogate_fits(args):
@@ -306,7 +506,6 @@ def surrogate_fits(args):
 
 
 def native(args):
-    import numpy as np
     import torch
     import crystalscatter_gb300 as cs
     from crystalscatter_gb300 import configs as C
@@ -318,156 +517,86 @@ def native(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    params = C.WORKLOADS[WORKLOAD]
-    ops = load_ops()
-    peaks = fp_peaks()
+    peaks = cs.measure_pipe_peaks()
+    work = load_kernel_work()
 
-    calc = cs.SasCalc_GENERIC_calculation()
-    calc.setParams(params)
-    # one drop-in call to prepare (and validate) the parameter set
-    calc.doCalculation(0, False, False)
-    ref_img = calc.data()
-    n = ref_img.size
-    npix = calc.prepared_pixels()
-    d_out = torch.empty(n, dtype=torch.float64, device="cuda")
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    stream = torch.cuda.current_stream()
+    def clocks_start():
+        c = ClockSampler(local)
+        c.start()
+        time.sleep(0.3)
+        return c
 
-    # correctness of the device-resident launches against the drop-in image
-    calc.launch_prepared(d_out.data_ptr(), n, stream.cuda_stream)
-    torch.cuda.synchronize()
-    assert np.array_equal(d_out.cpu().numpy().reshape(ref_img.shape), ref_img, equal_nan=True)
-
-    # mixed path (FP32 bulk, FP64 guards): the metric's <= 1e-5 bar, checked here
-    calc.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)
-    mixed_img = calc.data()
-    redo = calc.mixed_redo_pixels()
-    acc = rel_stats(mixed_img, ref_img)
-    assert acc["max"] <= 1e-5 and acc["nonfinite_mismatch"] == 0, f"mixed path exceeds 1e-5 vs FP64: {acc}"
-
-    clocks = ClockSampler(local)
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    time.sleep(0.3)
-    t_kernel, per_step = time_kernel(calc, torch, d_out, n, args.steps, args.warmup, flush, mode=cs.CS_MODE_MIXED)
-    t_fp64, _ = time_kernel(calc, torch, d_out, n, args.steps, args.warmup, flush, mode=cs.CS_MODE_FP64)
-    # end-to-end: the drop-in call with host buffers (prep + upload + kernel + download)
-    for _ in range(args.warmup):
-        calc.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        calc.doCalculation(0, False, False, mode=cs.CS_MODE_MIXED)
-        _ = calc.data()
-    t_e2e = time.perf_counter() - t0
-    prep_ms = calc.higResTimerElapsedPrep
-    clk = clocks.stop()
-    t_kernel, t_e2e, t_fp64 = max_over_ranks([t_kernel, t_e2e, t_fp64], world, "cuda")
-
+    row, T = sweep(cs, torch, C, args, world, peaks, work, clocks_start)
+    t_kernel, t_e2e = max_over_ranks([T["t_kernel"], T["t_e2e"]], world, "cuda")
+    npix = T["npix"]
     value = replica_rate(npix * args.steps, world, t_kernel)
-    e2e = replica_rate(npix * args.steps, world, t_e2e)
-    ms_per_step = 1e3 * t_kernel / args.steps
-
-    # roofline: algorithmic HBM bytes per launch = the image (8 B per pixel)
-    peak, peak_kind = load_peaks()
-    launch_s = t_kernel / args.steps
-    bytes_per_launch = 8.0 * npix
-    achieved = bytes_per_launch / launch_s / 1e9
-    fl = ops[WORKLOAD]["flops_per_pixel"]
+    e2e = replica_rate(npix * args.e2e_steps, world, t_e2e)
+    key = "0x01020806"
+    rl = roofline(work, key, npix, T["main_ms"] / 1e3, peaks)
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded parameter sets, no dataset)",
-        "config": {"workload": "pCyl_lNon_oGau 512x512 (cylinder r=5 L=60, Gaussian 15 deg, phi=30)",
-                   "pixels_per_step": npix, "mode": "mixed FP32/FP64, <=1e-5 vs FP64",
-                   "l2": "256 MB write between timed steps (flush)", "parallelism": f"replicas x{world}"},
-        "accuracy": {"mixed_vs_fp64": acc, "fp64_redo_pixels": redo},
-        "fp64_dropin": {"value": npix * args.steps * world / t_fp64, "unit": UNIT,
-                        "ms_per_step": 1e3 * t_fp64 / args.steps},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(calc._lib.cs_prepared_size()),
-                "d2h_bytes_per_step": int(8 * n), "host_prep_ms": prep_ms},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": TRAFFIC_BYTES_PER_LAUNCH,
-                     "note": f"peak {peak_kind}; 8 B written per pixel: the kernels are bound by arithmetic, "
-                             f"see compute_roofline and profiles/"},
-        "compute_roofline": {"flops_per_pixel": fl, "achieved_tflops": value * fl / 1e12,
-                             "fp32_peak_tflops": peaks["fp32_tflops"],
-                             "frac_of_fp32_peak": value * fl / 1e12 / peaks["fp32_tflops"],
-                             "fp64_peak_tflops": peaks["fp64_tflops"], "peaks": peaks["kind"],
-                             "flops_source": "crystalscatter_gb300/config_ops.json (counted on the oracle)"},
-        "gpu_launches": 2 * args.steps,
-        "clocks": clk,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_kernel / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded parameter sets, no dataset)",
+        "config": headline_config(args.sweep_sets, world),
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(T["upload_bytes"]),
+                "d2h_bytes_per_step": int(8 * T["total_doubles"]), "steps": args.e2e_steps,
+                "path": "SasCalcBatch.prepare(host parameters) + run_host(CS_MODE_MIXED, pinned host buffer): "
+                        "cs_batch_prepare (host preparation on all host threads, upload) + cs_batch_run_host "
+                        "(persistent kernels, FP64 redo, image download)"},
+        "roofline": rl,
+        "pipe_peaks": peaks,
+        "sweep": row,
+        # per replay: the persistent mixed kernel and its FP64 redo kernel per key group
+        "gpu_launches": 2 * row["key_groups"] * args.steps,
+        "clocks": T["clocks"],
     }
-    if not args.no_extra and rank == 0:
-        rows = {}
-        for name in ("sphere", "cyl_gauss", "cyl_gauss_x", "sphere_fcc"):
-            rows[name] = config_row(cs, torch, name, C.WORKLOADS[name], flush, ops, peaks, max(3, args.steps // 2))
-        result["configs"] = rows
-        if args.sweep_sets > 0:
-            result["sweep"], _ = sweep(cs, torch, C, args.sweep_sets, ops, peaks, max(1, args.sweep_steps))
+    if rank == 0 and not args.no_extra:
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        result["configs"] = {name: config_row(cs, torch, name, flush, max(3, args.steps // 2),
+                                              min(5.0, args.cpu_seconds)) for name in SINGLE}
+        del flush
     if args.surrogate and rank == 0:
         result["surrogate"] = surrogate_fits(args)
     if rank == 0:
-        result["cpu_baseline"] = cpu_baseline(params, args.cpu_seconds)
+        result["cpu_baseline"] = cpu_baseline_blocks(sweep_sample_names(), args.cpu_seconds)
         print(json.dumps(result))
-    calc.cleanup()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
 
 
-def cpu_baseline(params, seconds):
-    """The oracle port of the reference on all host cores, on a bounded sample
-    of the same workload: whole calculations (host preparation, as the
-    reference's doCalculation runs it, then the image) repeated until
-    `seconds` elapse."""
-    from oracle import cpu_oracle
-    nthreads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    pix = 0
-    reps = 0
-    while True:
-        P = cpu_oracle.prepare(params)
-        _, n = cpu_oracle.image_prepared(P, nthreads)
-        pix += n
-        reps += 1
-        if time.perf_counter() - t0 >= seconds:
-            break
-    dt = time.perf_counter() - t0
-    return {"value": pix / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{reps} full 512x512 calculations (preparation + image) of the same workload, {dt:.1f} s"}
-
+# ------------------------------------------------------------ reference arm
 
 def reference(args):
+    """The reference's algorithm on the host cores: the CPU oracle on the
+    reference-prepared sample sets of the sweep, one whole image per step,
+    cycling through the sample (k = 0, 64, ..., 4032)."""
     rank, world, local = dist_env()
     if rank != 0:
         return
-    from crystalscatter_gb300 import configs as C
-    from oracle import cpu_oracle
-    params = C.WORKLOADS[WORKLOAD]
-    nthreads = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        cpu_oracle.image_prepared(cpu_oracle.prepare(params), nthreads)
+    from oracle import ref_prepared as R
+    names = sweep_sample_names()
+    blocks = [R.load(n) for n in names]
+    nt = cpu_threads()
+    for i in range(args.warmup):
+        blocks[i % len(blocks)].image(nt)
     t0 = time.perf_counter()
     pix = 0
-    for _ in range(args.steps):
-        P = cpu_oracle.prepare(params)  # doCalculation prepares on every call
-        _, n = cpu_oracle.image_prepared(P, nthreads)
+    for i in range(args.steps):
+        _, n = blocks[(args.warmup + i) % len(blocks)].image(nt)
         pix += n
     dt = time.perf_counter() - t0
     value = pix / dt
+    sample = (f"{args.steps} whole images ({pix} pixels) of the reference-prepared sweep sample sets, one per step, "
+              f"the reference's per-pixel algorithm restated in C (oracle/cs_oracle.c), rows over {nt} host threads")
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded parameter sets, no dataset)",
-        "config": {"workload": "pCyl_lNon_oGau 512x512 (cylinder r=5 L=60, Gaussian 15 deg, phi=30)",
-                   "pixels_per_step": pix // args.steps, "parallelism": f"{nthreads} host threads"},
+        "config": headline_config(args.sweep_sets, world),
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": f"{args.steps} full calculations (host preparation + image), the reference's "
-                                   f"algorithm restated in C (oracle/cs_oracle.c), row-parallel over host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nt, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))

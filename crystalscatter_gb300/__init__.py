@@ -114,6 +114,8 @@ def _sig(lib):
     P = ctypes.POINTER
     lib.cs_version.restype = ctypes.c_char_p
     lib.cs_gpu_available.restype = ctypes.c_int
+    lib.cs_measure_pipe_peaks.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+    lib.cs_measure_pipe_peaks.restype = ctypes.c_int
     lib.cs_create.restype = H
     lib.cs_destroy.argtypes = [H]
     lib.cs_default_params.argtypes = [P(CsParams)]
@@ -151,8 +153,11 @@ def _sig(lib):
     lib.cs_batch_last_error.argtypes = [B]
     lib.cs_batch_prepare.argtypes = [B, P(CsParams), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.cs_batch_info.argtypes = [B, P(ctypes.c_size_t), P(ctypes.c_long), P(ctypes.c_int)]
+    lib.cs_batch_upload_bytes.argtypes = [B, P(ctypes.c_size_t)]
     lib.cs_batch_layout.argtypes = [B, ctypes.c_int, P(ctypes.c_size_t)] + [P(ctypes.c_int)] * 4
     lib.cs_batch_launch.argtypes = [B, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    lib.cs_batch_profile.argtypes = [B, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     lib.cs_batch_capture.argtypes = [B, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int, ctypes.c_int]
     lib.cs_batch_replay.argtypes = [B, ctypes.c_void_p]
     lib.cs_batch_graph_nodes.argtypes = [B, P(ctypes.c_size_t)]
@@ -205,6 +210,17 @@ def load_library(path=None):
     if path is None:
         _lib = lib
     return lib
+
+
+def measure_pipe_peaks(stream=None):
+    """Measured FMA rates (TFLOP/s: FP32, packed FP32 pairs, FP64) and the
+    special-function unit's ex2 rate (Tops/s) of the current device
+    (cs_measure_pipe_peaks)."""
+    out = (ctypes.c_double * 4)()
+    rc = load_library().cs_measure_pipe_peaks(_torch_stream(stream), out, 4)
+    if rc != 0:
+        raise CrystalScatterError(rc, "cs_measure_pipe_peaks failed")
+    return {"fp32_tflops": out[0], "fp32x2_tflops": out[1], "fp64_tflops": out[2], "mufu_tops": out[3]}
 
 
 def default_params():
@@ -452,6 +468,12 @@ class SasCalcBatch:
         self._check(self._lib.cs_batch_info(self._b, ctypes.byref(d), ctypes.byref(p), ctypes.byref(g)))
         return d.value, p.value, g.value
 
+    def upload_bytes(self):
+        """host-to-device bytes of the last prepare"""
+        n = ctypes.c_size_t()
+        self._check(self._lib.cs_batch_upload_bytes(self._b, ctypes.byref(n)))
+        return n.value
+
     def layout(self, k):
         """(offset, xmin, xmax, ymin, ymax) of set k's image in the buffer"""
         o = ctypes.c_size_t()
@@ -462,6 +484,15 @@ class SasCalcBatch:
     def launch(self, d_out_ptr, n_doubles, stream_ptr=0, mode=CS_MODE_FP64, schedule=CS_SCHED_PERSISTENT):
         self._check(self._lib.cs_batch_launch(self._b, ctypes.c_void_p(d_out_ptr), int(n_doubles),
                                               ctypes.c_void_p(stream_ptr), int(mode), int(schedule)))
+
+    def profile(self, d_out_ptr, n_doubles, stream_ptr=0, mode=CS_MODE_MIXED):
+        """One persistent run with CUDA events around the main and redo kernels:
+        (main_ms, redo_ms)."""
+        a, r = ctypes.c_double(), ctypes.c_double()
+        self._check(self._lib.cs_batch_profile(self._b, ctypes.c_void_p(d_out_ptr), int(n_doubles),
+                                               ctypes.c_void_p(stream_ptr), int(mode), ctypes.byref(a),
+                                               ctypes.byref(r)))
+        return a.value, r.value
 
     def capture(self, d_out_ptr, n_doubles, mode=CS_MODE_FP64, schedule=CS_SCHED_PERSISTENT):
         self._check(self._lib.cs_batch_capture(self._b, ctypes.c_void_p(d_out_ptr), int(n_doubles), int(mode),

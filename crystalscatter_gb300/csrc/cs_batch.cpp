@@ -58,6 +58,7 @@ struct cs_batch {
     std::vector<size_t> offset;  // caller's order
     size_t total_doubles = 0;
     long total_pixels = 0;
+    size_t upload_bytes = 0;  // host-to-device bytes of the last cs_batch_prepare
     std::vector<int> expand_sets;  // caller's indices of sets that need zeroing + mirroring
     bool any_twin = false;
 
@@ -196,8 +197,10 @@ int ensure_redo(cs_batch *b) {
     return CS_OK;
 }
 
-// Enqueue one evaluation of all sets on stream s.
-int enqueue(cs_batch *b, double *d_out, cudaStream_t s, int mode, int schedule) {
+// Enqueue one evaluation of all sets on stream s. marks (persistent schedule
+// only): three events per group, recorded before the group's main kernel,
+// between it and its redo kernel, and after the redo.
+int enqueue(cs_batch *b, double *d_out, cudaStream_t s, int mode, int schedule, cudaEvent_t *marks = nullptr) {
     cudaError_t e;
     for (int k : b->expand_sets) {
         // pixels the mirroring never writes read as 0
@@ -221,10 +224,15 @@ int enqueue(cs_batch *b, double *d_out, cudaStream_t s, int mode, int schedule) 
             const int per_sm = mixed ? cs::batch_blocks_per_sm_mixed(g.key) : cs::batch_blocks_per_sm_fp64(g.key);
             long grid = (long)b->sm_count * std::max(per_sm, 1);
             grid = std::min(grid, std::max(g.tiles, 1L));
+            if (marks) cudaEventRecord(marks[3 * gi], s);
             int rc = mixed
                          ? cs::launch_batch_mixed(b->dsets, g, (int)gi, b->d_counters + gi, b->d_chi, d_out, b->redo,
-                                                  (int)grid, s)
+                                                  (int)grid, s, marks ? marks[3 * gi + 1] : nullptr)
                          : cs::launch_batch_fp64(b->dsets, g, b->d_counters + gi, b->d_chi, d_out, (int)grid, s);
+            if (marks) {
+                if (!mixed) cudaEventRecord(marks[3 * gi + 1], s);
+                cudaEventRecord(marks[3 * gi + 2], s);
+            }
             if (rc == CS_ERR_CUDA) return cuda_fail(b, cs::last_launch_error(), "batch kernel launch");
             if (rc) return fail(b, rc, "no batch kernel for this combination");
         }
@@ -515,6 +523,9 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
     if ((e = cudaMemcpy(b->dsets, b->hsets.data(), sizeof(cs::BatchSetDev) * (size_t)nsets, cudaMemcpyHostToDevice)) != cudaSuccess)
         return cuda_fail(b, e, "upload set table");
     if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return cuda_fail(b, e, "batch upload");
+    b->upload_bytes = sizeof(cs_prepared) * (size_t)nsets + sizeof(float) * pk.size() + sizeof(float4) * av.size() +
+                      sizeof(int) * ai.size() + sizeof(cs_delta_node) * dt.size() +
+                      sizeof(cs::BatchSetDev) * (size_t)nsets;
     b->t_prep = now_ms() - t0;
     b->prepared = true;
     return CS_OK;
@@ -526,6 +537,13 @@ int cs_batch_info(cs_batch *b, size_t *total_doubles, long *total_pixels, int *n
     if (total_doubles) *total_doubles = b->total_doubles;
     if (total_pixels) *total_pixels = b->total_pixels;
     if (ngroups) *ngroups = (int)b->groups.size();
+    return CS_OK;
+}
+
+int cs_batch_upload_bytes(cs_batch *b, size_t *bytes) {
+    if (!b || !bytes) return CS_ERR_PARAM;
+    if (!b->prepared) return fail(b, CS_ERR_STATE, "no prepared batch");
+    *bytes = b->upload_bytes;
     return CS_OK;
 }
 
@@ -556,6 +574,36 @@ int cs_batch_launch(cs_batch *b, double *d_out, size_t n_doubles, void *stream, 
     // the uploads of cs_batch_prepare have completed, so any stream may run the batch
     cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
     return enqueue(b, d_out, s, mode, schedule);
+}
+
+int cs_batch_profile(cs_batch *b, double *d_out, size_t n_doubles, void *stream, int mode, double *main_ms,
+                     double *redo_ms) {
+    if (!b || !main_ms || !redo_ms) return CS_ERR_PARAM;
+    int rc = check_run_args(b, d_out, n_doubles, mode);
+    if (rc) return rc;
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    const size_t ng = b->groups.size();
+    std::vector<cudaEvent_t> ev(3 * ng, nullptr);
+    cudaError_t e = cudaSuccess;
+    for (auto &x : ev)
+        if (e == cudaSuccess) e = cudaEventCreate(&x);
+    if (e == cudaSuccess) {
+        rc = enqueue(b, d_out, s, mode, CS_SCHED_PERSISTENT, ev.data());
+        if (rc == CS_OK && (e = cudaStreamSynchronize(s)) != cudaSuccess) rc = cuda_fail(b, e, "profiled batch run");
+    } else {
+        rc = cuda_fail(b, e, "cudaEventCreate");
+    }
+    *main_ms = *redo_ms = 0;
+    for (size_t g = 0; rc == CS_OK && g < ng; g++) {
+        float a = 0, c = 0;
+        cudaEventElapsedTime(&a, ev[3 * g], ev[3 * g + 1]);
+        cudaEventElapsedTime(&c, ev[3 * g + 1], ev[3 * g + 2]);
+        *main_ms += a;
+        *redo_ms += c;
+    }
+    for (auto &x : ev)
+        if (x) cudaEventDestroy(x);
+    return rc;
 }
 
 int cs_batch_capture(cs_batch *b, double *d_out, size_t n_doubles, int mode, int schedule) {

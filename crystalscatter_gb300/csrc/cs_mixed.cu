@@ -1398,7 +1398,8 @@ int launch_image_mixed(const DevSet &D, const csm::PeakTab &T, const cs_prepared
 // ---- batch launchers -------------------------------------------------------
 
 int launch_batch_mixed(const BatchSetDev *d_sets, const BatchGroup &g, int group_index, unsigned long long *d_counter,
-                       const cs_chi_node *d_chi, double *d_out, const BatchRedo &R, int grid, cudaStream_t s) {
+                       const cs_chi_node *d_chi, double *d_out, const BatchRedo &R, int grid, cudaStream_t s,
+                       cudaEvent_t mid) {
     if (g.tiles <= 0) return CS_OK;
     int *cnt = R.d_count + group_index;
     int2 *list = R.d_list + (size_t)group_index * (size_t)R.cap;
@@ -1413,6 +1414,7 @@ int launch_batch_mixed(const BatchSetDev *d_sets, const BatchGroup &g, int group
     default: return CS_ERR_UNSUPPORTED;
     }
     if (launch_status() != CS_OK) return CS_ERR_CUDA;
+    if (mid) cudaEventRecord(mid, s);
     if (g.key == CS_KEY_CYL_NONE_GAUSS) {
         csm::k_batch_redo_cyl_warp<<<sm_count_m() * 4, 128, 0, s>>>(d_sets, d_chi, d_out, cnt, list, R.cap);
         return launch_status();

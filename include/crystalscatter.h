@@ -93,6 +93,15 @@ typedef struct cs_handle cs_handle;
 const char *cs_version(void);
 int cs_gpu_available(void); /* 1 when a CUDA device is usable (reference gpuAvailable, sc_calc_generic_gpu.h:441) */
 
+/* Measured arithmetic peaks of the current device (no counterpart in the
+   reference; the denominators of the pixel kernels' compute roofline), each
+   from a few milliseconds of independent dependent chains on every SM, timed
+   with CUDA events on `stream` (cudaStream_t as void*, NULL = the default
+   stream). out[0] FP32 FMA, out[1] packed FP32 pair FMA (f32x2), out[2] FP64
+   FMA, all in TFLOP/s (2 flops per FMA); out[3] the special-function unit's
+   ex2.approx.f32 in Tops/s. n >= 4. */
+int cs_measure_pipe_peaks(void *stream, double *out, int n);
+
 /* Handle lifetime: constructor / cleanup() (sc_calc_generic_cpu.cpp:102, 994) */
 cs_handle *cs_create(void);
 void cs_destroy(cs_handle *h);
@@ -220,10 +229,20 @@ const char *cs_batch_last_error(cs_batch *b);
 /* host_threads: threads for the host preparation (0 = all hardware threads). */
 int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_switch, int ign_cbs, int host_threads);
 int cs_batch_info(cs_batch *b, size_t *total_doubles, long *total_pixels, int *ngroups);
+/* Host-to-device bytes that the last cs_batch_prepare uploaded (prepared
+   blocks, reflection and node tables, set table). */
+int cs_batch_upload_bytes(cs_batch *b, size_t *bytes);
 int cs_batch_layout(cs_batch *b, int k, size_t *offset, int *xmin, int *xmax, int *ymin, int *ymax);
 /* Enqueue all images of the prepared batch into d_out (device memory,
    n_doubles capacity) on stream (NULL = the batch's stream); asynchronous. */
 int cs_batch_launch(cs_batch *b, double *d_out, size_t n_doubles, void *stream, int mode, int schedule);
+/* One persistent run of the batch (as cs_batch_launch with
+   CS_SCHED_PERSISTENT) with CUDA events on `stream` around each key group's
+   main kernel and its FP64 redo kernel; waits for it and returns the summed
+   durations in milliseconds (redo_ms is 0 for CS_MODE_FP64). Kernel timing
+   for benchmarks; no counterpart in the reference. */
+int cs_batch_profile(cs_batch *b, double *d_out, size_t n_doubles, void *stream, int mode, double *main_ms,
+                     double *redo_ms);
 /* Capture the same work as a CUDA graph (once) and replay it. The graph
    writes into the d_out given at capture; preparing the batch again drops it. */
 int cs_batch_capture(cs_batch *b, double *d_out, size_t n_doubles, int mode, int schedule);

@@ -37,6 +37,10 @@ def load():
         lib.oracle_pixel.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         lib.oracle_pixel.restype = ctypes.c_double
         lib.oracle_supported.argtypes = [ctypes.c_void_p]
+        lib.oracle_extents.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        lib.oracle_image_rowlist.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.c_int]
+        lib.oracle_image_rowlist.restype = ctypes.c_long
         lib.oracle_fit.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_long),
                                    ctypes.POINTER(ctypes.c_long)]
         lib.oracle_fit.restype = ctypes.c_double
@@ -54,6 +58,9 @@ def load_probe():
         lib.oracle_image_rows.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         lib.oracle_image_rows.restype = ctypes.c_long
         lib.oracle_set_probe.argtypes = [ctypes.c_int]
+        lib.oracle_image_rowlist.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                             ctypes.c_int]
+        lib.oracle_image_rowlist.restype = ctypes.c_long
         _probe = lib
     return _probe
 

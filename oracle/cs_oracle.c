@@ -808,6 +808,21 @@ int oracle_supported(const cs_prepared *P) {
     }
 }
 
+/* Image extents, calculated region and dispatch key of a prepared block, for
+   callers that hold the block as raw bytes:
+   e = {xmin, xmax, ymin, ymax, zzmin, zzmax, iimin, iimax, key}. */
+void oracle_extents(const cs_prepared *P, int *e) {
+    e[0] = P->xmin;
+    e[1] = P->xmax;
+    e[2] = P->ymin;
+    e[3] = P->ymax;
+    e[4] = P->zzmin;
+    e[5] = P->zzmax;
+    e[6] = P->iimin;
+    e[7] = P->iimax;
+    e[8] = P->key;
+}
+
 double oracle_pixel(const cs_prepared *P, int ihex, int i) {
     double qx, qy, qz;
     convert_idx2q(P, ihex, i, &qx, &qy, &qz);
@@ -820,6 +835,7 @@ typedef struct {
     const cs_prepared *P;
     double *out;
     int next_row, row_end;
+    const int *list; /* when set: rows list[next_row], next_row < row_end */
     pthread_mutex_t lock;
 } row_queue;
 
@@ -829,14 +845,44 @@ static void *row_worker(void *arg) {
     const int xs = P->xmax - P->xmin;
     for (;;) {
         pthread_mutex_lock(&Q->lock);
-        int ihex = Q->next_row++;
+        int pos = Q->next_row++;
         pthread_mutex_unlock(&Q->lock);
-        if (ihex >= Q->row_end) break;
+        if (pos >= Q->row_end) break;
+        const int ihex = Q->list ? Q->list[pos] : pos;
+        if (ihex < P->zzmin || ihex >= P->zzmax) continue;
         /* one image row per step as the reference's threads (doThreadCalculation) */
         for (int i = P->iimin; i < P->iimax; i++)
             Q->out[(long)(ihex - P->xmin) + (long)xs * (long)(i - P->ymin)] = oracle_pixel(P, ihex, i);
     }
     return NULL;
+}
+
+/* Computes the ihex rows listed in rows[0..nrows) (a sample of the image;
+   rows outside the calculated region are skipped) with nthreads threads.
+   Returns the pixel count. */
+long oracle_image_rowlist(const cs_prepared *P, double *out, const int *rows, int nrows, int nthreads) {
+    if (!oracle_supported(P)) return -1;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 512) nthreads = 512;
+    row_queue Q;
+    Q.P = P;
+    Q.out = out;
+    Q.next_row = 0;
+    Q.row_end = nrows;
+    Q.list = rows;
+    pthread_mutex_init(&Q.lock, NULL);
+    pthread_t th[512];
+    int started = 0;
+    for (int t = 0; t < nthreads; t++)
+        if (pthread_create(&th[t], NULL, row_worker, &Q) == 0) started++;
+        else break;
+    if (started == 0) row_worker(&Q);
+    for (int t = 0; t < started; t++) pthread_join(th[t], NULL);
+    pthread_mutex_destroy(&Q.lock);
+    long n = 0;
+    for (int r = 0; r < nrows; r++)
+        if (rows[r] >= P->zzmin && rows[r] < P->zzmax) n += P->iimax - P->iimin;
+    return n;
 }
 
 /* Computes the ihex rows [row0,row1) of the calculated region (all rows when
@@ -857,6 +903,7 @@ long oracle_image_rows(const cs_prepared *P, double *out, int row0, int row1, in
     Q.out = out;
     Q.next_row = row0;
     Q.row_end = row1;
+    Q.list = NULL;
     pthread_mutex_init(&Q.lock, NULL);
     if (nthreads == 1)
         row_worker(&Q);

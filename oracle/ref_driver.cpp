@@ -28,6 +28,9 @@
 #include "sc_calc_generic_gpu.h"
 #undef private
 
+// layout of the prepared block that the CPU oracle (oracle/cs_oracle.c) reads
+#include "../crystalscatter_gb300/csrc/cs_prepared.h"
+
 namespace {
 
 struct RefHandle {
@@ -269,6 +272,151 @@ double ref_fit(void *p, int nthreads, int bstop, int border, long *cnt, long *na
     apply(h);
     if (nthreads < 1) nthreads = 1;
     return h->calc->doFitCalculation(nthreads, bstop, border, *cnt, *nancnt);
+}
+
+// The reference's own host preparation without the image: the checks and
+// prepareCalculation() of doCalculation (sc_calc_generic_cpu.cpp:1151-1166).
+// Returns 0, or 1 with the error message (ref_error) when the parameters are
+// rejected or the preparation fails.
+int ref_prepare(void *p, int ign_new_switch, int ign_cbs) {
+    RefHandle *h = static_cast<RefHandle *>(p);
+    apply(h);
+    SasCalc_GENERIC_calculation *c = h->calc;
+    c->numberOfThreads = 1;
+    c->bIgnoreNewSwitch = ign_new_switch != 0;
+    h->err = c->checkAllParameters(ign_cbs != 0);
+    if (!h->err.empty()) return 1;
+    if (!c->prepareCalculation()) {
+        h->err = c->getLastErrorMessage();
+        if (h->err.empty()) h->err = "prepareCalculation failed";
+        return 1;
+    }
+    return 0;
+}
+
+// The prepared constants of the last ref_prepare / ref_run, written into the
+// prepared-block layout that the CPU oracle evaluates (cs_prepared.h): every
+// field the oracle reads, taken from the reference object's own members after
+// its prepareCalculation. The dispatch key is formed as calcCPU_selection
+// forms it (sc_calc_generic_gpu.cu:190-218). Fields the oracle does not read
+// stay zero. Returns the block size, or -1 when out_size is too small.
+long ref_export_prepared(void *p, void *out, size_t out_size) {
+    if (out_size < sizeof(cs_prepared)) return -1;
+    SasCalc_GENERIC_calculation *c = static_cast<RefHandle *>(p)->calc;
+    auto &R = c->params;
+    cs_prepared *P = static_cast<cs_prepared *>(out);
+    std::memset(P, 0, sizeof(cs_prepared));
+    const int lt = (int)c->ltype;
+    P->particle = (int)c->ComboBoxParticle;
+    P->shp = (int)c->shp;
+    P->ltype = lt;
+    P->ordis = (int)R.ordis;
+    P->ign_switch = c->bIgnoreNewSwitch ? 1 : 0;
+    const int key = (P->particle << 24) | (lt == 12 ? 0 : (P->shp << 16)) | (lt << 8) | P->ordis;
+    const bool special = !c->bIgnoreNewSwitch &&
+                         (key == CS_KEY_SPHERE_NONE_ISO || key == CS_KEY_SPHERE_GAUSS_FCC_GAUSS ||
+                          key == CS_KEY_CYL_NONE_GAUSS || key == CS_KEY_CYL_NONE_ZDIR ||
+                          key == CS_KEY_CYL_GAUSS_BCT_ZDIR || key == CS_KEY_CUBE_NONE_ISO);
+    P->key = special ? key : CS_KEY_GENERIC;
+    P->cs = R.cs;
+    P->part = R.part;
+    P->cdim = c->cdim;
+    P->partdim = c->partdim;
+    P->orcase = (int)R.orcase;
+    P->lattice = c->lattice ? 1 : 0;
+    P->twin = c->twin ? 1 : 0;
+    P->debyescherrer = c->RadioButtonDebyeScherrer ? 1 : 0;
+    P->para = c->RadioButtonPara ? 1 : 0;
+    // geometry
+    P->use1d = c->use1d ? 1 : 0;
+    P->usebeamstop = c->useBeamStop ? 1 : 0;
+    P->zmax = c->zmax;
+    P->zzmin = c->zzmin;
+    P->zzmax = c->zzmax;
+    P->iimin = c->iimin;
+    P->iimax = c->iimax;
+    P->xmin = c->_xmin;
+    P->xmax = c->_xmax;
+    P->ymin = c->_ymin;
+    P->ymax = c->_ymax;
+    P->calc_quadrants = (int)c->calcQuadrants;
+    P->expand = c->bExpandImage ? 1 : 0;
+    P->qmax = c->qmax;
+    P->qmin = c->qmin;
+    P->pixnox = c->pixnox;
+    P->pixnoy = c->pixnoy;
+    P->pixx_m = c->pixx_m;
+    P->pixy_m = c->pixy_m;
+    P->beamx0 = c->beamX0;
+    P->beamy0 = c->beamY0;
+    P->det = c->det;
+    P->wave = c->wave;
+    // pixel manipulation
+    P->base = c->base;
+    P->izero = c->izero;
+    P->iso = c->iso;
+    P->ifluc = c->ifluc;
+    P->rfluc = c->rfluc;
+    // particle
+    P->radius = R.radius;
+    P->radiusi = R.radiusi;
+    P->sigma = R.sigma;
+    P->sigmal = R.sigmal;
+    P->length = R.length;
+    P->p1 = R.p1;
+    P->rho = R.rho;
+    P->alphash1 = R.alphash1;
+    P->alpha = R.alpha;
+    P->poltheta = R.polTheta;
+    P->polphi = R.polPhi;
+    P->dbeta = R.dbeta;
+    P->norm = R.norm;
+    P->por = R.por;
+    P->order = c->order;
+    const double lq[10] = {0, R.limq1, R.limq2, R.limq3, R.limq4, R.limq5, R.limq6, R.limq7, R.limq8, R.limq9};
+    const double lf[10] = {0, R.limq1f, R.limq2f, R.limq3f, R.limq4f, R.limq5f, R.limq6f, R.limq7f, R.limq8f, R.limq9f};
+    for (int i = 0; i < 10; i++) {
+        P->limq[i] = lq[i];
+        P->limqf[i] = lf[i];
+    }
+    P->cosphic = c->cosphic;
+    P->sinphic = c->sinphic;
+    P->cosphi = c->cosphi;
+    P->sinphi = c->sinphi;
+    P->costheta = c->costheta;
+    P->sintheta = c->sintheta;
+    // lattice
+    P->peakmax1 = c->peakmax1;
+    P->peakmax2 = c->peakmax2;
+    for (int i = 0; i < 4; i++) P->latpar[i] = c->latpar[i];
+    P->dwfactor = c->dwfactor;
+    P->uca = R.uca;
+    P->ucb = R.ucb;
+    P->domainsize = R.domainsize;
+    P->width_zuf = R.width_zuf;
+    P->reldis = c->reldis;
+    P->dist = c->dist;
+    P->phiwidth = c->phiwidth;
+    P->ceff = R.ceff;
+    // coefficient arrays
+    if (R.CR) {
+        const double *cp[9] = {R.CR->carr1p, R.CR->carr2p, R.CR->carr3p, R.CR->carr4p, R.CR->carr5p,
+                               R.CR->carr6p, R.CR->carr7p, R.CR->carr8p, R.CR->carr9p};
+        const double *cf[9] = {R.CR->carr1f, R.CR->carr2f, R.CR->carr3f, R.CR->carr4f, R.CR->carr5f,
+                               R.CR->carr6f, R.CR->carr7f, R.CR->carr8f, R.CR->carr9f};
+        for (int k = 0; k < 9; k++) {
+            std::memcpy(P->carrp[k], cp[k], sizeof(double) * CS_COEFF_LEN);
+            std::memcpy(P->carrf[k], cf[k], sizeof(double) * CS_COEFF_LEN);
+        }
+        std::memcpy(P->carr11pm, R.CR->carr11pm, sizeof(double) * CS_IMAX2D * CS_IMAX2D);
+    }
+    // reflection tables (same [2500][6] / [2500][17] layout as the reference's)
+    const int L = SasCalc_GENERIC_calculation::latparlen;
+    if (c->latpar1ptr) std::memcpy(P->latpar1, c->latpar1ptr, sizeof(int) * L * 6);
+    if (c->latpar2ptr) std::memcpy(P->latpar2, c->latpar2ptr, sizeof(int) * L * 6);
+    if (c->latpar3ptr) std::memcpy(P->latpar3, c->latpar3ptr, sizeof(float) * L * 17);
+    for (int i = 0; i < 4; i++) P->nofit_x0[i] = P->nofit_x1[i] = P->nofit_y0[i] = P->nofit_y1[i] = -1;
+    return (long)sizeof(cs_prepared);
 }
 
 // Per-pixel FQS values left by the last fit call (arrFitFqs, fitWidth*fitHeight).

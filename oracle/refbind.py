@@ -178,3 +178,27 @@ def condition(params, ign_new_switch=0, ign_cbs=0, nthreads=8, modes=PROBE_MODES
         d[~np.isfinite(d)] = np.inf
         cond = np.maximum(cond, d)
     return cond
+
+
+def prepared_block(params, ign_new_switch=0, ign_cbs=0):
+    """The reference's own host preparation of a parameter set, exported into
+    the prepared-block layout the CPU oracle evaluates (ref_prepare +
+    ref_export_prepared in oracle/ref_driver.cpp). Returns (bytes, error):
+    error is the reference's message when it rejects the set, else ""."""
+    lib = load()
+    if not hasattr(lib.ref_prepare, "_bound"):
+        lib.ref_prepare.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        lib.ref_export_prepared.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+        lib.ref_export_prepared.restype = ctypes.c_long
+        lib.ref_prepare._bound = True
+    r = RefCalc(params)
+    try:
+        if lib.ref_prepare(r.h, int(ign_new_switch), int(ign_cbs)) != 0:
+            return None, lib.ref_error(r.h).decode()
+        size = 1 << 20
+        buf = ctypes.create_string_buffer(size)
+        n = lib.ref_export_prepared(r.h, buf, size)
+        assert n > 0
+        return buf.raw[:n], ""
+    finally:
+        r.close()
