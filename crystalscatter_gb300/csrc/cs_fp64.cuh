@@ -245,6 +245,34 @@ __device__ __forceinline__ void polint5(const double ya[5], double &y, double &d
     }
 }
 
+// Length factor of the Schulz-averaged cylinder along its axis,
+//   L(a) = (1/(2z(z-1)a^2)) (1 - cos(m atan 2a) / (1+4a^2)^(m/2)),  m = z-1,
+// in the reference's closed form (formpq/formfq_partCylinder ordis 6,
+// Source/sc_lib_formpq_partCylinder.h:115-119; the integrand of trapzdchid
+// i1 = 1..4, Source/sc_calc_generic_gpu.cu:1590-2965). For small |m a| the
+// bracket cancels: it is ~2 m(m+1) a^2 while its terms carry FP64 rounding of
+// ~1e-16, so the reference's FP64 value is off by up to ~1e-16/(m a)^2
+// relative (O(1) on pixels on the cylinder axis, where a is eps-sized) and
+// moves by as much under one-ulp changes of cos/pow. Below |m a| = 0.05 the
+// closed form's exact value is taken from its power series instead: the
+// bracket is 1 - Re (1+2ia)^(-m) = -sum_{j>=1} C(m+2j-1, 2j) (-4a^2)^j, so
+//   L = 1 + sum_{j>=1} T_j,  T_j/T_(j-1) = -4a^2 (m+2j)(m+2j+1)/((2j+1)(2j+2)),
+// whose ratios there are below ~1e-3: a few terms reach the FP64 rounding of
+// the sum. Elsewhere the reference's own expression is evaluated (same
+// operations, same rounding).
+__device__ __forceinline__ bool len_factor_small(double a, double m) { return fabs(m * a) < 0.05 && fabs(a) < 0.05; }
+
+__device__ __forceinline__ double len_factor_series(double a, double m) {
+    const double x = -4.0 * a * a;
+    double term = 1.0, sum = 0.0;
+    for (int j = 1; j <= 40; j++) {
+        term = term * (x * ((m + 2 * j) * (m + 2 * j + 1)) / ((2 * j + 1) * (2 * j + 2)));
+        sum = sum + term;
+        if (fabs(term) <= 1e-18 * fabs(sum) || term == 0.0) break;
+    }
+    return 1.0 + sum;
+}
+
 // chi integrand of trapzdchid for the cylinder cases i1 = 1..4; any other i1
 // leaves the integrand 0 (the reference has no branch for orcGeneral = 0).
 struct ChiArgs {
@@ -268,6 +296,7 @@ __device__ __forceinline__ double chi_integrand(const ChiArgs &A, double cx, dou
     case 4: argx = (A.qx * sx * sd - A.qy * cx * sd + eps) * A.l / A.zp1; break;
     default: return 0.0;
     }
+    if (len_factor_small(argx, A.zm1)) return len_factor_series(argx, A.zm1);
     return (A.a1 / (argx * argx)) * (1 - cos(A.zm1 * atan(2.0 * argx)) / pow(1.0 + 4 * argx * argx, A.zm1h));
 }
 
@@ -584,6 +613,13 @@ __device__ __forceinline__ double len_factor_ref(double arglq, double zl) {
            (1 - cos((zl - 1) * atan(2.0 * arglq)) / pow(1.0 + 4 * arglq * arglq, (zl - 1) / 2.0));
 }
 
+// The same with its small-argument series where the closed form cancels
+// (see len_factor_small above): the closed form's exact value everywhere.
+__device__ __forceinline__ double len_factor(double arglq, double zl) {
+    if (len_factor_small(arglq, zl - 1)) return len_factor_series(arglq, zl - 1);
+    return len_factor_ref(arglq, zl);
+}
+
 template <bool WARP = false>
 __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, double q) {
     const cs_prepared &P = *C.P;
@@ -600,7 +636,7 @@ __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, d
             } else {
                 const double zl = zl_of();
                 const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-                pql = len_factor_ref(arglq, zl);
+                pql = len_factor(arglq, zl);
             }
         }
     }
@@ -674,7 +710,7 @@ __device__ inline double formfq_cylinder(const Ctx &C, double limql, double qxs,
                 pql = series_zdir(P.carrf[0], qxs, qys);
             } else {
                 const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-                pql = len_factor_ref(arglq, zl);
+                pql = len_factor(arglq, zl);
             }
         }
     }
@@ -789,6 +825,30 @@ __device__ inline void peak_sums(const cs_prepared &P, double qx, double qy, dou
 }
 
 // calc_partSphere_peakGauss_lattFCC_ordisGauss, Source/sc_gpu_pSph_pGau_lFCC_oGau.h:15-171
+// Lattice factors near q = 0. The reference forms
+//   szq    = 1 + (F/P) (r1 - 1) e1,   r1 = 2 pi I_aniso / V,  e1 = exp(-dw q^2),
+//   szqiso = 1 + (r2 - 1) e2,         r2 = 8 pi^3 I_iso / (4 pi V), e2 = exp(-ucb q^2),
+// which cancel as q -> 0 (F/P, e1, e2 -> 1, no reflection near): their exact
+// values are O(q^2), while the FP64 forms round to 0 or to noise of ~1e-16
+// (at the beam-centre pixel, q = 1e-9, the reference returns 0 where the
+// exact value is ~1e-18). Below q = 1e-6 the form factors are their one-term
+// series, P = 1 + cp q^2, F = 1 + cf q^2 (per factor; the stop rule ends each
+// series after that term), so the factors are formed from the difference
+//   1 - (F/P) e1 = ((P - F) + F (1 - e1)) / P,  1 - e1 = -expm1(-dw q^2),
+// with P - F from the series coefficients: the exact values to rounding.
+#define CS_SMALL_Q 1e-6
+
+__device__ __forceinline__ void lattice_factors_small_q(const cs_prepared &P, double q, double pq, double fq,
+                                                        double p_minus_f, double intensity, double radintensity,
+                                                        double &szq, double &szqiso) {
+    const double sphno_cubevol = P.latpar[1] * P.latpar[2];
+    const double r1 = 2 * M_PI * intensity / sphno_cubevol;
+    const double r2 = 8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol);
+    const double om1 = -expm1(-P.dwfactor * q * q), om2 = -expm1(-P.ucb * q * q);
+    szq = (p_minus_f + fq * om1) / pq + (fq / pq) * r1 * (1 - om1);
+    szqiso = om2 + r2 * (1 - om2);
+}
+
 __device__ inline double calc_sphere_fcc(const Ctx &C, double qx, double qy, double qz) {
     const cs_prepared &P = *C.P;
     const double q = sqrt(qx * qx + qy * qy + qz * qz) + CS_EPS9;
@@ -800,7 +860,15 @@ __device__ inline double calc_sphere_fcc(const Ctx &C, double qx, double qy, dou
     const double sphno_cubevol = P.latpar[1] * P.latpar[2];
     const double szqiso = (1 + (1) * (8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol) - 1) *
                                    exp(-P.ucb * q * q));
-    const double szq = (1 + (fq / pq) * (2 * M_PI * intensity / sphno_cubevol - 1) * exp(-P.dwfactor * q * q));
+    double szq = (1 + (fq / pq) * (2 * M_PI * intensity / sphno_cubevol - 1) * exp(-P.dwfactor * q * q));
+    if (q < CS_SMALL_Q && P.cs == 0) {
+        // homogeneous spheres: P and F are series in q^2 (carr4p, carr4f)
+        double szi;
+        const double q2 = q * q;
+        lattice_factors_small_q(P, q, pq, fq, (P.carrp[3][1] - P.carrf[3][1]) * q2 + (P.carrp[3][2] - P.carrf[3][2]) * q2 * q2,
+                                intensity, radintensity, szq, szi);
+        return P.base + P.izero * (szq * pq + P.iso * szi * pqiso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+    }
     return P.base + P.izero * (szq * pq + P.iso * szqiso * pqiso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
 }
 
@@ -870,7 +938,26 @@ __device__ inline double calc_cyl_bct_zdir(const Ctx &C, double qx, double qy, d
     const double sphno_cubevol = P.latpar[1] * P.latpar[2];
     const double szqiso = (1 + (1) * (8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol) - 1) *
                                    exp(-P.ucb * q * q));
-    const double szq = (1 + (fq / pq) * (2 * M_PI * intensity / (sphno_cubevol)-1) * exp(-P.dwfactor * q * q));
+    double szq = (1 + (fq / pq) * (2 * M_PI * intensity / (sphno_cubevol)-1) * exp(-P.dwfactor * q * q));
+    if (q < CS_SMALL_Q && P.cs == 0 && P.ordis == 6 && P.orcase != 4 && (P.length / P.radius) >= 2) {
+        // P = Pl Pr and F = Fl Fr, each factor its one-term series: the length
+        // series in s^2 (s = qxs + qys, carr1p/carr1f), the radial in q^2
+        // (carr4p/carr4f); P - F = (Pl - Fl) Pr + Fl (Pr - Fr)
+        double qxs = 0, qys = 0;
+        switch (P.orcase) {
+        case CS_ORC_GENERAL: qxs = qx * P.cosphi * P.sintheta; qys = qy * P.sinphi * P.sintheta; break;
+        case CS_ORC_XAXIS: qxs = qx; break;
+        case CS_ORC_YAXIS: qys = qy; break;
+        default: qxs = qx; qys = qy; break;
+        }
+        const double s2 = (qxs + qys) * (qxs + qys), q2 = q * q;
+        const double pl = 1 + P.carrp[0][1] * s2, fl = 1 + P.carrf[0][1] * s2;
+        const double pr = 1 + P.carrp[3][1] * q2;
+        const double pmf = (P.carrp[0][1] - P.carrf[0][1]) * s2 * pr + fl * (P.carrp[3][1] - P.carrf[3][1]) * q2;
+        double szi;
+        lattice_factors_small_q(P, q, pl * pr, fq, pmf, intensity, radintensity, szq, szi);
+        return P.base + P.izero * (szq * pq + P.iso * szi * pqiso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
+    }
     return P.base + P.izero * (szq * pq + P.iso * szqiso * pqiso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
 }
 

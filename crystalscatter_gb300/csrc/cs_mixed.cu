@@ -325,12 +325,10 @@ struct ChiArgsF {
     int i1;
 };
 
-// Where m*a is small (m = z-1) the reference's closed form of the length
-// factor, 1 - cos(m atan 2a)/(1+4a^2)^(m/2) in FP64, cancels: its bracket is
-// ~2 (m a)^2 while its rounding is a few 1e-16, a relative noise of up to
-// ~5e-16/(m a)^2 that the FP64 drop-in reproduces and this FP32 series form does
-// not. Below |m a| = 1e-4 (noise above ~5e-8) a node flags the pixel for the
-// FP64 redo; above it the two agree to FP32 accuracy.
+// Where m*a is small (m = z-1) the closed form of the length factor cancels;
+// both paths take its power series there (cs64::len_factor_small and
+// len_series_ok above), so the FP32 node value agrees with the FP64 one to
+// FP32 accuracy everywhere.
 __device__ __forceinline__ float chi_integrand_f(const ChiArgsF &A, float cx, float sx, float cd, float sd,
                                                  bool &guard) {
     const float eps = 1e-10f;
@@ -348,7 +346,6 @@ __device__ __forceinline__ float chi_integrand_f(const ChiArgsF &A, float cx, fl
     default: return 0.0f;
     }
     const float a = s * A.lz;
-    if (fabsf((A.z - 1.0f) * a) < 1e-4f) guard = true;
     return cyl_len_factor(a, A.z, A.a4);
 }
 
@@ -877,12 +874,11 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
         } else {
             const double zl = z_of(P.sigmal);
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-            if (LAT || fabs((zl - 1) * arglq) < 1e-3) {
-                // the reference's closed form cancels to rounding noise for
-                // small |m a| (see chi_integrand_f), and lattice pixels need the
-                // length factor beyond FP32 accuracy where the structure factor
-                // cancels: evaluated as the drop-in does (same value)
-                pql = cs64::len_factor_ref(arglq, zl);
+            if (LAT) {
+                // lattice pixels need the length factor beyond FP32 accuracy
+                // where the structure factor cancels: evaluated as the drop-in
+                // does (same value)
+                pql = cs64::len_factor(arglq, zl);
             } else {
                 float rel;
                 pql = cyl_len_factor_e<false>(arglq, zl, rel);
@@ -997,12 +993,11 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             pql = cs64::series_zdir(P.carrf[0], qxs, qys);
         } else {
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-            if (LAT || fabs((zl - 1) * arglq) < 1e-3) {
-                // the reference's closed form cancels to rounding noise for
-                // small |m a| (see chi_integrand_f), and lattice pixels need the
-                // length factor beyond FP32 accuracy where the structure factor
-                // cancels: evaluated as the drop-in does (same value)
-                pql = cs64::len_factor_ref(arglq, zl);
+            if (LAT) {
+                // lattice pixels need the length factor beyond FP32 accuracy
+                // where the structure factor cancels: evaluated as the drop-in
+                // does (same value)
+                pql = cs64::len_factor(arglq, zl);
             } else {
                 float rel;
                 pql = cyl_len_factor_e<false>(arglq, zl, rel);
@@ -1109,6 +1104,9 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
         if (!(ep <= 5e-6)) guard = true;
         return P.base + P.izero * (pq + P.iso * pq) + tailv;
     }
+    // lattice keys: near q = 0 the structure factor's exact value is formed
+    // from series differences by the FP64 function (cs64::lattice_factors_small_q)
+    if ((KEY == CS_KEY_SPHERE_GAUSS_FCC_GAUSS || KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR) && q < CS_SMALL_Q) guard = true;
     if (KEY == CS_KEY_SPHERE_GAUSS_FCC_GAUSS) {
         const double pq = sphere_pq_mixed<true>(P, q, guard, ep);
         const double fq = sphere_fq_mixed<true>(P, q, guard, ef);

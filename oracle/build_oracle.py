@@ -14,6 +14,8 @@ LIB = os.path.join(OUT, "liboracle_cs.so")
 PROBE = os.path.join(OUT, "liboracle_cs_probe.so")
 COUNT = os.path.join(OUT, "liboracle_cs_count.so")
 COUNT_SRC = os.path.join(HERE, "count_ops.cpp")
+QUAD = os.path.join(OUT, "liboracle_cs_quad.so")
+QUAD_SRC = os.path.join(HERE, "quad_oracle.cpp")
 HDR = os.path.join(HERE, "..", "crystalscatter_gb300", "csrc", "cs_prepared.h")
 
 
@@ -35,6 +37,12 @@ def build(force=False):
     if force or not os.path.exists(COUNT) or os.path.getmtime(COUNT) < max(newest, os.path.getmtime(COUNT_SRC)):
         subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w", COUNT_SRC, "-o",
                         COUNT, "-lpthread"], check=True)
+    # quadruple-precision build (quad_oracle.cpp includes cs_oracle.c unchanged)
+    if force or not os.path.exists(QUAD) or os.path.getmtime(QUAD) < max(newest, os.path.getmtime(QUAD_SRC)):
+        import platform
+        libs = [] if platform.machine() in ("aarch64", "arm64") else ["-lquadmath"]
+        subprocess.run(["g++", "-O2", "-std=gnu++17", "-fPIC", "-shared", "-ffp-contract=off", "-w", QUAD_SRC, "-o",
+                        QUAD, "-lpthread"] + libs, check=True)
     return LIB
 
 

@@ -154,3 +154,92 @@ def fit(params, target, bstop=0, border=0, nofit=()):
     nan = ctypes.c_long()
     chi2 = load().oracle_fit(ctypes.byref(P), target.ctypes.data, fqs.ctypes.data, ctypes.byref(cnt), ctypes.byref(nan))
     return chi2, cnt.value, nan.value, fqs
+
+
+# ------------------------------------------------------ quadruple precision
+
+QUAD = os.path.join(HERE, "_build", "liboracle_cs_quad.so")
+_quad = None
+
+
+def load_quad():
+    """The oracle evaluated in quadruple precision (oracle/quad_oracle.cpp)."""
+    global _quad
+    if _quad is None:
+        if not os.path.exists(QUAD):
+            from oracle import build_oracle
+            build_oracle.build()
+        lib = ctypes.CDLL(QUAD)
+        lib.quad_image.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        lib.quad_image.restype = ctypes.c_long
+        lib.quad_set_qmode.argtypes = [ctypes.c_int, ctypes.c_int]
+        _quad = lib
+    return _quad
+
+
+def quad_image(P, nthreads=None):
+    """The reference algorithm's value on every pixel of prepared block P
+    (ctypes struct or buffer), evaluated in quadruple precision and rounded to
+    double."""
+    lib = load_quad()
+    e = (ctypes.c_int * 9)()
+    load().oracle_extents(P if isinstance(P, ctypes.Array) else ctypes.byref(P), e)
+    out = np.zeros((e[3] - e[2], e[1] - e[0]), dtype=np.float64)
+    lib.quad_image(P if isinstance(P, ctypes.Array) else ctypes.byref(P), out.ctypes.data,
+                   int(nthreads or os.cpu_count() or 1))
+    return out
+
+
+# one-ulp input perturbations for the stability of the exact value: q moved by
+# 4 double ulps (all up, all down, mixed) and the series coefficients moved by
+# 2 ulps (all up, all down, alternating by order either way)
+QUAD_Q_MODES = (8, 15, 10, 13)
+QUAD_COEFF_MODES = (0, 1, 2, 3)
+
+
+def _perturb_coefficients(P, mode, steps=2):
+    import copy
+    Q = copy.deepcopy(P)
+    for arr in (Q.carrp, Q.carrf):
+        a = np.ctypeslib.as_array(arr)
+        n = np.arange(a.shape[1])[None, :]
+        if mode == 0:
+            up = np.ones(a.shape, dtype=bool)
+        elif mode == 1:
+            up = np.zeros(a.shape, dtype=bool)
+        else:
+            up = np.broadcast_to((n % 2) == (mode - 2), a.shape)
+        with np.errstate(over="ignore"):
+            for _ in range(steps):
+                a[...] = np.where(up, np.nextafter(a, np.inf), np.nextafter(a, -np.inf))
+    return Q
+
+
+def _spread(img, base, tau):
+    with np.errstate(invalid="ignore", over="ignore", divide="ignore"):
+        d = np.abs(img - base) / np.maximum(np.abs(base), tau)
+    same = (~np.isfinite(base)) & ((np.isnan(img) & np.isnan(base)) | (img == base))
+    d[same] = 0.0
+    d[~np.isfinite(d)] = np.inf
+    return d
+
+
+def quad_condition(P, nthreads=None, base=None):
+    """(exact value H, its spread): the largest relative change of the
+    quadruple-precision value under the input perturbations above (tau =
+    1e-30 max|H|). A pixel whose spread is large has no stable answer at
+    double-precision inputs: its coefficients or q alone decide the value."""
+    lib = load_quad()
+    H = quad_image(P, nthreads) if base is None else base
+    fin = np.isfinite(H)
+    tau = 1e-30 * (np.max(np.abs(H[fin])) if fin.any() else 1.0)
+    spread = np.zeros(H.shape)
+    try:
+        for m in QUAD_Q_MODES:
+            lib.quad_set_qmode(m, 4)
+            spread = np.maximum(spread, _spread(quad_image(P, nthreads), H, tau))
+    finally:
+        lib.quad_set_qmode(0, 0)
+    for m in QUAD_COEFF_MODES:
+        spread = np.maximum(spread, _spread(quad_image(_perturb_coefficients(P, m), nthreads), H, tau))
+    return H, spread

@@ -70,6 +70,13 @@ static double probe_(double r, int fn) {
 #define acos(x) probe_(acos(x), 8)
 #endif
 
+/* element type of the prepared block's arrays as seen by the functions below
+   (the block's own double; the high-precision build evaluates in another
+   type but reads the same block) */
+#ifndef CS_PDOUBLE_T
+#define CS_PDOUBLE_T double
+#endif
+
 /* sin, cos and exp of quadrature node positions (pixel-independent values;
    the operation-counting build evaluates them without counting, as the GPU
    paths read them from node tables) */
@@ -171,7 +178,7 @@ static void convert_idx2q(const cs_prepared *P, int ihex, int i, double *qx, dou
 
 /* ------------------------------------------------------------------ spheres */
 
-static double series_q(const double *c, double q, int nmax) {
+static double series_q(const CS_PDOUBLE_T *c, double q, int nmax) {
     double pqsum = 1.0, oldpqsum = 0.0, qq = 1.0;
     for (int nser = 1; nser <= nmax; nser++) {
         qq = qq * q * q;
@@ -509,7 +516,7 @@ static double qrombdeltac4(const cs_prepared *P, double sigma, double theta_deg,
 /* ----------------------------------------------------------------- cylinders */
 
 /* the ordis-0 double series; variant selects the carr11pm index/power order */
-static double cyl_double_series(const cs_prepared *P, double qxs, double qys, const double *carr1, int variant) {
+static double cyl_double_series(const cs_prepared *P, double qxs, double qys, const CS_PDOUBLE_T *carr1, int variant) {
     double pql = 1.0, oldpqsum = 0.0;
     double qxn[121], qyn[121];
     qxn[0] = 1.0;
@@ -823,9 +830,16 @@ void oracle_extents(const cs_prepared *P, int *e) {
     e[8] = P->key;
 }
 
+/* hook on the pixel's q vector (the high-precision build uses it to move q by
+   a few double ulps and measure how much the exact value depends on it) */
+#ifndef CS_ORACLE_Q_HOOK
+#define CS_ORACLE_Q_HOOK(qx, qy, qz)
+#endif
+
 double oracle_pixel(const cs_prepared *P, int ihex, int i) {
     double qx, qy, qz;
     convert_idx2q(P, ihex, i, &qx, &qy, &qz);
+    CS_ORACLE_Q_HOOK(qx, qy, qz);
     return oracle_pixel_q(P, qx, qy, qz);
 }
 

@@ -111,3 +111,66 @@ def compare_to_reference(got, ref, cond, mask=None, tol=1e-10, envelope=100.0):
         "max_rel_all": float(np.nanmax(np.where(np.isfinite(rel[mask]), rel[mask], 0))) if mask.any() else 0.0,
         "n_above_tol": int((mask & (rel > tol)).sum()),
     }
+
+
+HP_SPREAD_FACTOR = 10.0  # multiple of the exact value's own spread allowed where that spread exceeds tol
+
+
+def compare_with_exact(got, g, mask=None, tol=1e-10, envelope=100.0):
+    """Compares an image with a golden record g (the reference's image and
+    its one-ulp spread "cond"; where present the quadruple-precision value of
+    the reference's algorithm "hp" and that value's spread "hp_cond" under
+    4-ulp moves of q and 2-ulp moves of the series coefficients):
+
+    * reference stable (cond <= 1e-12): relative error vs the reference's
+      image <= tol;
+    * reference ill-conditioned, exact value known: relative error vs hp <=
+      max(tol, 10 hp_cond) -- tol wherever the exact value is stable at that
+      level; looser only where q or the coefficients alone move it more;
+    * reference ill-conditioned, no exact value (the generic pixel function,
+      which the oracle does not restate): vs the reference's image within
+      max(tol, envelope cond), counted apart.
+    Returns a dict of counts and maxima ("n_bad" must be 0)."""
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(g["image"], dtype=np.float64)
+    cond = np.asarray(g["cond"], dtype=np.float64)
+    if mask is None:
+        mask = np.ones(ref.shape, dtype=bool)
+    ill = cond > ILL
+    rel_r, _ = rel_error(got, ref)
+    allowed = np.full(ref.shape, tol)
+    rel = rel_r.copy()
+    has_hp = "hp" in g
+    if has_hp:
+        hp = np.asarray(g["hp"], dtype=np.float64)
+        hpc = np.asarray(g["hp_cond"], dtype=np.float64)
+        rel_h, _ = rel_error(got, hp)
+        rel[ill] = rel_h[ill]
+        allowed[ill] = np.maximum(tol, HP_SPREAD_FACTOR * hpc[ill])
+        loose = mask & ill & (allowed > tol)
+        envelope_px = np.zeros(ref.shape, dtype=bool)
+    else:
+        allowed[ill] = np.maximum(tol, envelope * cond[ill])
+        envelope_px = mask & ill
+        loose = envelope_px & (allowed > tol)
+    bad = mask & (rel > allowed)
+    worst = []
+    if bad.any():
+        idx = np.flatnonzero(bad.ravel())
+        order = np.argsort(-np.nan_to_num(rel.ravel()[idx], nan=np.inf))[:5]
+        for j in idx[order]:
+            worst.append((int(j), float(rel.ravel()[j]), float(allowed.ravel()[j]), float(got.ravel()[j]),
+                          float(ref.ravel()[j])))
+    well = mask & ~ill & np.isfinite(rel_r)
+    ill_fin = mask & ill & np.isfinite(rel)
+    return {
+        "worst_bad": worst,
+        "n": int(mask.sum()),
+        "n_ill": int((mask & ill).sum()),
+        "n_checked_vs_exact": int((mask & ill).sum()) if has_hp else 0,
+        "n_looser_than_tol": int(loose.sum()),
+        "n_envelope": int(envelope_px.sum()),
+        "n_bad": int(bad.sum()),
+        "max_rel_well": float(rel_r[well].max()) if well.any() else 0.0,
+        "max_rel_ill": float(rel[ill_fin].max()) if ill_fin.any() else 0.0,
+    }

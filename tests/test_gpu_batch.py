@@ -6,14 +6,14 @@ Every batch image must equal, bit for bit, the image the single-set call
 computes for the same parameter set in the same precision mode (the pixel
 arithmetic is the same code; only the scheduling differs), and the golden
 cases must meet the same bars as the single-set tests (1e-10 FP64, 1e-5
-mixed, widened to 100x the reference's own one-ulp spread where the
-reference is ill-conditioned)."""
+mixed; where the reference is ill-conditioned, against the quadruple-precision
+value of its algorithm, helpers.compare_with_exact)."""
 import numpy as np
 import pytest
 
 import crystalscatter_gb300 as cs
 from crystalscatter_gb300 import configs as C
-from helpers import compare_to_reference, golden, golden_cases, written_mask
+from helpers import compare_with_exact, golden, golden_cases, written_mask
 
 pytestmark = pytest.mark.gpu
 
@@ -71,7 +71,7 @@ def test_batch_equals_single_calls_and_reference(gbatch, mode):
         ref = single(case["params"], case["ign_cbs"], mode)
         assert same_bits(img, ref), n
         g = golden(n)
-        r = compare_to_reference(img, g["image"], g["cond"], mask=written_mask(case["params"], img.shape), tol=tol)
+        r = compare_with_exact(img, g, mask=written_mask(case["params"], img.shape), tol=tol)
         assert r["n_bad"] == 0, (n, r)
         assert r["max_rel_well"] <= tol, (n, r)
 

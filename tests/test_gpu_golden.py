@@ -1,16 +1,19 @@
 """FP64 GPU drop-in against the reference's own images (golden fixtures).
 
 Bar: per-pixel relative error <= 1e-10 on every pixel the reference computes
-stably. Where the reference's own result moves under one-ulp changes of the
-math library (the golden "cond" map; e.g. series/asymptote or Romberg stop
-decisions near their thresholds, and the catastrophically cancelling cylinder
-F(q) series of the BCT case), the GPU must stay within 100x that spread. The
-number of such ill-conditioned pixels is part of the report."""
+stably. Where the reference's own FP64 result moves under one-ulp changes of
+the math library (the golden "cond" map), its value is not a usable answer:
+there the GPU is compared with the reference algorithm's value evaluated in
+quadruple precision (the golden "hp" map, tests/golden/make_golden_hp.py),
+still to 1e-10 unless that exact value itself moves by more under few-ulp
+changes of q or of the series coefficients (then 10x that spread). Cases of
+the generic pixel function, which the CPU oracle does not restate, keep the
+reference's one-ulp envelope and are counted apart."""
 import numpy as np
 import pytest
 
 import crystalscatter_gb300 as cs
-from helpers import compare_to_reference, golden, golden_cases, written_mask
+from helpers import compare_with_exact, golden, golden_cases, written_mask
 
 CASES = golden_cases()["images"]
 TOL = 1e-10
@@ -35,7 +38,7 @@ def test_fp64_image_matches_reference(name):
     img, dims = run_case(case)
     assert dims == [int(v) for v in g["dims"]]
     m = written_mask(case["params"], img.shape)
-    r = compare_to_reference(img, g["image"], g["cond"], mask=m, tol=TOL)
+    r = compare_with_exact(img, g, mask=m, tol=TOL)
     print(name, r)
     assert r["n_bad"] == 0, r
     assert r["max_rel_well"] <= TOL, r
