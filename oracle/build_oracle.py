@@ -41,8 +41,12 @@ def build(force=False):
     if force or not os.path.exists(QUAD) or os.path.getmtime(QUAD) < max(newest, os.path.getmtime(QUAD_SRC)):
         import platform
         libs = [] if platform.machine() in ("aarch64", "arm64") else ["-lquadmath"]
-        subprocess.run(["g++", "-O2", "-std=gnu++17", "-fPIC", "-shared", "-ffp-contract=off", "-w", QUAD_SRC, "-o",
-                        QUAD, "-lpthread"] + libs, check=True)
+        # optional: only the golden-fixture generator needs it; a host whose
+        # compiler lacks binary128 support goes on without it
+        r = subprocess.run(["g++", "-O2", "-std=gnu++17", "-fPIC", "-shared", "-ffp-contract=off", "-w", QUAD_SRC,
+                            "-o", QUAD, "-lpthread"] + libs, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            print("quadruple-precision oracle not built on this host:\n" + r.stdout[-2000:], file=sys.stderr)
     return LIB
 
 

@@ -24,41 +24,33 @@
 typedef double pdouble_t;  // the prepared block's element type
 
 #if defined(__aarch64__)
-// long double is IEEE binary128 on AArch64 Linux: the C library's
-// long-double functions serve
+// long double is IEEE binary128 on AArch64 Linux: the standard library's
+// long-double overloads of the math functions serve as they are
 typedef long double Q;
-#define QF(f) f##l
 #else
 #include <quadmath.h>
 typedef __float128 Q;
-#define QF(f) f##q
-#endif
 
-inline Q sin(Q x) { return QF(sin)(x); }
-inline Q cos(Q x) { return QF(cos)(x); }
-inline Q tan(Q x) { return QF(tan)(x); }
-inline Q atan(Q x) { return QF(atan)(x); }
-inline Q acos(Q x) { return QF(acos)(x); }
-inline Q atan2(Q y, Q x) { return QF(atan2)(y, x); }
-inline Q atan2(Q y, double x) { return QF(atan2)(y, (Q)x); }
-inline Q atan2(double y, Q x) { return QF(atan2)((Q)y, x); }
-inline Q exp(Q x) { return QF(exp)(x); }
-inline Q log(Q x) { return QF(log)(x); }
-inline Q sqrt(Q x) { return QF(sqrt)(x); }
-inline Q fabs(Q x) { return QF(fabs)(x); }
-inline Q trunc(Q x) { return QF(trunc)(x); }
-inline Q pow(Q x, Q y) { return QF(pow)(x, y); }
-inline Q pow(Q x, double y) { return QF(pow)(x, (Q)y); }
-inline Q pow(double x, Q y) { return QF(pow)((Q)x, y); }
-inline Q pow(Q x, int y) { return QF(pow)(x, (Q)y); }
-inline Q pow(Q x, float y) { return QF(pow)(x, (Q)y); }
-inline Q pow(int x, Q y) { return QF(pow)((Q)x, y); }
-inline Q modf(Q x, Q *ip) { return QF(modf)(x, ip); }
-#if defined(__aarch64__)
-inline bool isfinite(Q x) { return std::isfinite(x); }
-inline bool isnan(Q x) { return std::isnan(x); }
-inline bool isinf(Q x) { return std::isinf(x); }
-#else
+inline Q sin(Q x) { return sinq(x); }
+inline Q cos(Q x) { return cosq(x); }
+inline Q tan(Q x) { return tanq(x); }
+inline Q atan(Q x) { return atanq(x); }
+inline Q acos(Q x) { return acosq(x); }
+inline Q atan2(Q y, Q x) { return atan2q(y, x); }
+inline Q atan2(Q y, double x) { return atan2q(y, (Q)x); }
+inline Q atan2(double y, Q x) { return atan2q((Q)y, x); }
+inline Q exp(Q x) { return expq(x); }
+inline Q log(Q x) { return logq(x); }
+inline Q sqrt(Q x) { return sqrtq(x); }
+inline Q fabs(Q x) { return fabsq(x); }
+inline Q trunc(Q x) { return truncq(x); }
+inline Q pow(Q x, Q y) { return powq(x, y); }
+inline Q pow(Q x, double y) { return powq(x, (Q)y); }
+inline Q pow(double x, Q y) { return powq((Q)x, y); }
+inline Q pow(Q x, int y) { return powq(x, (Q)y); }
+inline Q pow(Q x, float y) { return powq(x, (Q)y); }
+inline Q pow(int x, Q y) { return powq((Q)x, y); }
+inline Q modf(Q x, Q *ip) { return modfq(x, ip); }
 inline bool isfinite(Q x) { return finiteq(x); }
 inline bool isnan(Q x) { return isnanq(x); }
 inline bool isinf(Q x) { return isinfq(x); }
