@@ -620,6 +620,97 @@ __device__ __forceinline__ double len_factor(double arglq, double zl) {
     return len_factor_ref(arglq, zl);
 }
 
+// Isotropic orientation average of the cylinder's length factor
+// (formpq_partCylinder ordis 7, Source/sc_lib_formpq_partCylinder.h:29-90):
+// short cylinders (L/R < 2) take the exact average as a double series in q^2
+// (carr11pm, carr2p) or the Porod tail; longer ones its factorised form, a
+// series in q^2 (carr1p) or the closed form
+//   (pi/(2z)) / a - cos((z-1) atan 2a) / (2z(z-1) a^2 (1+4a^2)^((z-1)/2)).
+__device__ inline double cyl_len_iso(const cs_prepared &P, double q, double zl) {
+    if ((P.length / P.radius) < 2) {
+        if (q < (5 * P.limq[2])) {
+            double qqn[101];
+            qqn[0] = 1.0;
+            for (int nser = 1; nser <= 100; nser++) qqn[nser] = qqn[nser - 1] * q * q;
+            double pql = 0.0, oldpqsum = -10.0;
+            for (int nser = 0; nser <= 100; nser++) {
+                double binsum = 0.0;
+                for (int mser = 0; mser <= 100; mser++) binsum += P.carr11pm[nser][mser] * qqn[mser];
+                pql += P.carrp[1][nser] * qqn[nser] * binsum;
+                const double delser = fabs((pql - oldpqsum) / pql);
+                if (delser < 0.0001) break;
+                oldpqsum = pql;
+            }
+            return pql;
+        }
+        return P.por / pow(q, 4);
+    }
+    if (q < (0.6 * P.limq[1])) return series_q(P.carrp[0], q, 120);
+    const double arglq = q * P.length / (zl + 1);
+    double pql = (M_PI / (2.0 * zl)) * (1 / arglq);
+    pql = pql - (1 / (2.0 * zl * (zl - 1) * arglq * arglq)) * cos((zl - 1) * atan(2.0 * arglq)) /
+                    pow(1.0 + 4 * arglq * arglq, (zl - 1) / 2.0);
+    return pql;
+}
+
+// The Schulz cylinder cross-section's closed form shared by the terms below:
+// (4/pi)(T1 - T2 - (9/8) T3) at argument x (Source/sc_lib_formpq_partCylinder.h:272-275)
+__device__ __forceinline__ double cyl_cross_closed(double x, double zr) {
+    const double pqr1 = (1 / (zr * (zr - 1) * (zr - 2))) * pow(x, -3);
+    const double pqr2 = (1 / (zr * (zr - 1) * (zr - 2))) * pow(x, -3) * sin((zr - 2) * atan(2.0 * x)) /
+                        pow(1.0 + 4 * x * x, (zr - 2) / 2.0);
+    const double pqr3 = (1 / (zr * (zr - 1) * (zr - 2) * (zr - 3))) * pow(x, -4) * cos((zr - 3) * atan(2.0 * x)) /
+                        pow(1.0 + 4 * x * x, (zr - 3) / 2.0);
+    return (4 / M_PI) * (pqr1 - pqr2 - (9 / 8.0) * pqr3);
+}
+
+// Cross-section of the homogeneous core/shell cylinder, F121 + F122 + F123
+// (Source/sc_lib_formpq_partCylinder.h:284-393): core, cross and shell
+// terms, each a series (carr4p/5p/6p) below its switch point or its closed form.
+__device__ inline double cyl_cross_coreshell(const cs_prepared &P, double q, double zr) {
+    const double radiusm = P.radius / P.p1;
+    const double zz = zr;
+    const double ccc1 = sqr(1 - P.rho) * pow(P.p1, 4);
+    const double ccc2 = 2 * P.rho * (1 - P.rho) * pow(P.p1, 2);
+    const double ccc3 = P.rho * P.rho;
+    const double vv3 = sqr((1 - P.rho) * pow(P.p1, 2) + P.rho);
+    const double argq = q * radiusm / (zz + 1);
+    const double argpq = q * P.radius / (zz + 1);
+    double F121, F122, F123;
+    if (q < (0.7 * P.limq[4]))
+        F121 = ccc1 * series_q(P.carrp[3], q, 120) / vv3;
+    else
+        F121 = ccc1 * cyl_cross_closed(argpq, zr) / vv3;
+    if (q < (1.5 * P.limq[5])) {
+        F122 = ccc2 * series_q(P.carrp[4], q, 120) / vv3;
+    } else {
+        const double argbm = (zr - 2) * atan(argpq - argq);
+        const double nenbm = pow(1.0 + sqr(argpq - argq), (zr - 2) / 2.0);
+        const double argbp = (zr - 2) * atan(argpq + argq);
+        const double nenbp = pow(1.0 + sqr(argpq + argq), (zr - 2) / 2.0);
+        const double argem = (zr - 3) * atan(argpq - argq);
+        const double nenem = pow(1.0 + sqr(argpq - argq), (zr - 3) / 2.0);
+        const double argep = (zr - 3) * atan(argpq + argq);
+        const double nenep = pow(1.0 + sqr(argpq + argq), (zr - 3) / 2.0);
+        const double arggm = (zr - 4) * atan(argpq - argq);
+        const double nengm = pow(1.0 + sqr(argpq - argq), (zr - 4) / 2.0);
+        const double arggp = (zr - 4) * atan(argpq + argq);
+        const double nengp = pow(1.0 + sqr(argpq + argq), (zr - 4) / 2.0);
+        const double pqr1 = (1 / (zr * (zr - 1) * (zr - 2))) * pow(argq, -3) * (cos(argbm) / nenbm - sin(argbp) / nenbp);
+        const double pqr2 = (1 / (zr * (zr - 1) * (zr - 2) * (zr - 3))) * pow(argq, -4) *
+                            ((1 - 1 / P.p1) * sin(argem) / nenem - (1 + 1 / P.p1) * cos(argep) / nenep);
+        const double pqr3 = (1 / (zr * (zr - 1) * (zr - 2) * (zr - 3) * (zr - 4))) * pow(argq, -5) * (1 / P.p1) *
+                            (cos(arggm) / nengm - sin(arggp) / nengp);
+        const double pqr = (4 / M_PI) * pow(P.p1, -3 / 2.0) * (pqr1 + (9 / 16.0) * pqr2 + (9 / 16.0) * (9 / 16.0) * pqr3);
+        F122 = ccc2 * pqr / vv3;
+    }
+    if (q < (0.6 * P.limq[6]))
+        F123 = ccc3 * series_q(P.carrp[5], q, 120) / vv3;
+    else
+        F123 = ccc3 * cyl_cross_closed(argq, zr) / vv3;
+    return F121 + F122 + F123;
+}
+
 template <bool WARP = false>
 __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, double q) {
     const cs_prepared &P = *C.P;
@@ -627,6 +718,7 @@ __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, d
     // Schulz exponents, formed on the branches that use them
     auto zl_of = [&P]() { return P.sigmal == 1.0 ? CS_EPS9 : (1 - sqr(P.sigmal)) / sqr(P.sigmal); };
     auto zr_of = [&P]() { return P.sigma == 1.0 ? CS_EPS9 : (1 - sqr(P.sigma)) / (sqr(P.sigma)); };
+    if (P.ordis == 7) pql = cyl_len_iso(P, q, zl_of());
     if (P.ordis == 6) {
         if (P.orcase == 4)
             pql = 1.0;
@@ -694,6 +786,7 @@ __device__ inline double formpq_cylinder(const Ctx &C, double qxs, double qys, d
         }
         return pql * pqr;
     }
+    if (P.cs == 1) return pql * cyl_cross_coreshell(P, q, zr_of());
     return 0.0;
 }
 
@@ -702,6 +795,17 @@ __device__ inline double formfq_cylinder(const Ctx &C, double limql, double qxs,
     const double zl = (1 - sqr(P.sigmal)) / sqr(P.sigmal);
     const double zr = (1 - sqr(P.sigma)) / sqr(P.sigma);
     double pql = 0, pqr = 0;
+    if (P.ordis == 7) {
+        // isotropic (Source/sc_lib_formfq_partCylinder.h:27-48)
+        if (q < (0.6 * P.limqf[1])) {
+            pql = series_q(P.carrf[0], q, 120);
+        } else {
+            const double arglq = q * P.length / (zl + 1);
+            pql = (M_PI / (2.0 * zl)) * (1 / arglq);
+            pql = pql - (1 / (2.0 * zl * (zl - 1) * arglq * arglq)) * cos((zl - 1) * atan(2.0 * arglq)) /
+                            pow(1.0 + 4 * arglq * arglq, (zl - 1) / 2.0);
+        }
+    }
     if (P.ordis == 6) {
         if (P.orcase == 4)
             pql = 1.0;
@@ -749,6 +853,50 @@ __device__ inline double formfq_cylinder(const Ctx &C, double limql, double qxs,
             pqr = pqr3 * pqr3;
         }
         return pql * pqr;
+    }
+    if (P.cs == 1) {
+        // homogeneous core/shell cylinder, Source/sc_lib_formfq_partCylinder.h:211-302;
+        // the amplitude closed form A(x) = (2/sqrt pi)(T1 + (9/16) T2) with the
+        // prepared Gamma ratios (as for cs 0)
+        const double radiusm = P.radius / P.p1;
+        const double ccc1 = sqr(1 - P.rho) * pow(P.p1, 4);
+        const double ccc2 = 2 * P.rho * (1 - P.rho) * pow(P.p1, 2);
+        const double ccc3 = sqr(P.rho);
+        const double vv3 = sqr((1 - P.rho) * pow(P.p1, 2) + P.rho);
+        const double zz = zr;
+        const double argq = q * radiusm / (zz + 1);
+        const double argpq = q * P.radius / (zz + 1);
+        // T1, T2 of the amplitude at x, with the power's base 1 + x y (y = x
+        // except where the reference multiplies argpq by argq, kept)
+        auto t1 = [&](double x, double y) {
+            return P.gamma_ratio[0] * pow(x, -3 / 2.0) * (sin((zr - 1 / 2.0) * atan(x)) - cos((zr - 1 / 2.0) * atan(x))) /
+                   pow(1.0 + x * y, (zr - 1 / 2.0) / 2.0);
+        };
+        auto t2 = [&](double x, double y) {
+            return P.gamma_ratio[1] * pow(x, -5 / 2.0) * (sin((zr - 3 / 2.0) * atan(x)) + cos((zr - 3 / 2.0) * atan(x))) /
+                   pow(1.0 + x * y, (zr - 3 / 2.0) / 2.0);
+        };
+        double F121, F122, F123;
+        if (q < (0.7 * P.limqf[4])) {
+            F121 = ccc1 * series_q(P.carrf[3], q, 120) / vv3;
+        } else {
+            const double a = (2 / sqrt(M_PI)) * (t1(argpq, argpq) + (9 / 16.0) * t2(argpq, argpq));
+            F121 = ccc1 * a * a / vv3;
+        }
+        if (q < (0.3 * P.limqf[5])) {
+            F122 = ccc2 * series_q(P.carrf[4], q, 120) / vv3;
+        } else {
+            const double pqr = (4 / M_PI) * (t1(argpq, argq) + (9 / 16.0) * t2(argpq, argq)) *
+                               (t1(argq, argq) + (9 / 16.0) * t2(argq, argq));
+            F122 = ccc2 * pqr / vv3;
+        }
+        if (q < (0.6 * P.limqf[6])) {
+            F123 = ccc3 * series_q(P.carrf[5], q, 120) / vv3;
+        } else {
+            const double a = (2 / sqrt(M_PI)) * (t1(argq, argq) + (9 / 16.0) * t2(argq, argq));
+            F123 = ccc3 * a * a / vv3;
+        }
+        return pql * (F121 + F122 + F123);
     }
     return 0.0;
 }
@@ -1193,7 +1341,10 @@ static __device__ __noinline__ double calc_generic(const Ctx &C, double qx, doub
         if (P.lattice) fq = formfq_sphere(P, q);
         pqiso = pq;
     } else if (P.particle == 1) {  // cylinders, :64-165
-        if (P.ordis == 6) {
+        if (P.ordis == 7) {  // isotropic, :67-74
+            pq = formpq_cylinder(C, qx, qy, q);
+            if (P.lattice) fq = formfq_cylinder(C, q, qx, qy, q);
+        } else if (P.ordis == 6) {
             switch (P.orcase) {
             case CS_ORC_GENERAL:
                 pq = formpq_cylinder(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q);

@@ -562,6 +562,194 @@ bool Prep::coefficients() {
         } else {
             supported = false;
         }
+    } else if ((P.ordis == 7) && (cdim != 3)) {
+        // isotropic case for cylinders and disks, :3578-4122 (homogeneous and
+        // core/shell; operand types as the reference declares them: the
+        // local z12v and the recurrence factors in long double)
+        P.norm = 1;
+        P.order = 0;
+        if (P.cs == 0 && (cdim == 1 || cdim == 2)) {
+            long double z12v[kNmax + 1];
+            z12v[0] = 1.0;
+            double xrn[kNmax + 1];
+            xrn[0] = 1;
+            const double xrn_n0 = 1.0;
+            long double xln_n = 1.0;
+            if ((P.length / P.radius) < 2.0) {
+                // small axial ratios (the double sum of the exact average), :3592-3626
+                const double area = 2 * M_PI * sqr(P.radius) + 2 * M_PI * P.radius * (2. * P.length);
+                const double vol = M_PI * sqr(P.radius) * (2. * P.length);
+                P.por = 2 * M_PI * std::pow(z + 1, 4) * area / (z * (z - 1) * (z - 2) * (z - 3) * vol * vol);
+                for (int n = 1; n <= nmax; n++) {
+                    z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
+                    z12vl[n] = z12vl[n - 1] * ((zl + 1) - 2 + 2 * n) * ((zl + 1) - 1 + 2 * n);
+                    fkv[n] = fkv[n - 1] * n;
+                    gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
+                    xln_n = -xln_n * xl2z;
+                    // the reference's running xrn_n is never advanced here:
+                    // every xrn[n] is -xr2z (reproduced)
+                    xrn[n] = -xrn_n0 * xr2z;
+                }
+                // xln_n keeps its n = nmax value in this loop (reproduced)
+                for (int n = 0; n <= nmax; n++) {
+                    const double binsum = 0.0;
+                    P.carr11pm[n][0] = std::sqrt(M_PI) / gam3[n];
+                    double a1 = std::sqrt(M_PI) / (2.0 * gam3[n]);
+                    for (int m = 1; m <= nmax; m++) {
+                        a1 = a1 * (m + 1 / 2.0) / (n + m + 1 / 2.0);
+                        P.carr11pm[n][m] =
+                            std::pow(4.0, m + 1) * a1 * z12v[m] * xrn[m] / ((m + 2) * (m + 1) * fkv[m] * (m + 1) * fkv[m]);
+                    }
+                    carrp[1][n] = std::pow(4.0, n - 1) * z12vl[n] * xln_n / ((n + 1 / 2.0) * (n + 1) * fkv[n]);
+                    carrp[2][n] = std::pow(4.0, n) * binsum / gam3[n];
+                }
+            } else {
+                // large axial ratios (factorisation), :3628-3706
+                double xrn_n = 1.0;
+                for (int n = 1; n <= nmax; n++) {
+                    z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
+                    z12vl[n] = z12vl[n - 1] * ((zl + 1) - 2 + 2 * n) * ((zl + 1) - 1 + 2 * n);
+                    fkv[n] = fkv[n - 1] * n;
+                    fk2v[n] = fk2v[n - 1] * (2 * n - 1) * (2 * n);
+                    gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
+                    xln_n = -xln_n * xl2z;
+                    xrn_n = -xrn_n * xr2z;
+                    if (cdim == 1) {
+                        carr1p[n] = std::sqrt(M_PI) * std::pow(4.0, n) * z12vl[n] * xln_n /
+                                    (2.0 * (2 * n + 1) * (n + 1) * gam3[n] * fkv[n]);
+                        carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
+                                    ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n] * fkv[n]);
+                        double binsum = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            binsum += z12vl[m] * z12vl[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                        carr1f[n] = M_PI * xln_n * binsum / (4.0 * (2 * n + 1));
+                        binsum = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            binsum += z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                        carr4f[n] = xrn_n * binsum;
+                    }
+                    if (cdim == 2) {
+                        carr1p[n] = 2 * std::pow(4.0, n) * z12vl[n] * xln_n / ((n + 2) * (n + 1) * (n + 1) * fkv[n] * fkv[n]);
+                        carr4p[n] = std::pow(4.0, n) * std::sqrt(M_PI) * z12v[n] * xrn_n / (2.0 * (n + 1) * gam3[n] * fkv[n]);
+                        double binsum = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            binsum += z12vl[m] * z12vl[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                        carr1f[n] = std::sqrt(M_PI) * fkv[n] * xln_n * binsum / (2.0 * gam3[n]);
+                        binsum = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            binsum += z12v[m] * z12v[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                        carr4f[n] = M_PI * xrn_n * binsum / 4.0;
+                    }
+                    if (std::fabs(carr1p[n]) < kMin) {
+                        if (n < n1) n1 = n;
+                    }
+                    if (std::fabs(carrp[1][n]) < kMin) {
+                        if (n < n2) n2 = n;
+                    }
+                    if (std::fabs(carrp[2][n]) < kMin) {
+                        if (n < n3) n3 = n;
+                    }
+                    if (std::fabs(carr1f[n]) < kMin) {
+                        if (n < n1f) n1f = n;
+                    }
+                    if (std::fabs(carr4p[n]) < kMin) {
+                        if (n < n4) n4 = n;
+                    }
+                    if (std::fabs(carr4f[n]) < kMin) {
+                        if (n < n4f) n4f = n;
+                    }
+                }
+            }
+            done = true;
+        } else if (P.cs == 1 && (cdim == 1 || cdim == 2)) {
+            // core/shell, :3709-3828
+            long double xrmn_n = 1.0, xrn_n = 1.0, xln_n = 1.0;
+            long double z12v[kNmax + 1];
+            z12v[0] = 1.0;
+            for (int n = 1; n <= nmax; n++) {
+                z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
+                z12vl[n] = z12vl[n - 1] * ((zl + 1) - 2 + 2 * n) * ((zl + 1) - 1 + 2 * n);
+                fkv[n] = fkv[n - 1] * n;
+                fk2v[n] = fk2v[n - 1] * (2 * n - 1) * (2 * n);
+                gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
+                xln_n = -xln_n * xl2z;
+                xrn_n = -xrn_n * xr2z;
+                xrmn_n = -xrmn_n * xrm2z;
+                pn[n] = pn[n - 1] * p * p;
+                if (cdim == 1) {
+                    carr1p[n] = std::sqrt(M_PI) * std::pow(4.0, n) * z12vl[n] * xln_n /
+                                (2.0 * (2 * n + 1) * (n + 1) * gam3[n] * fkv[n]);
+                    carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
+                                ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n] * fkv[n]);
+                    double sump = 0.0;
+                    for (int m = 0; m <= n; m++) sump += pn[m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                    carr5p[n] = z12v[n] * xrmn_n * sump;
+                    carr6p[n] = carr4p[n] / pn[n];
+                    double binsum = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        binsum += z12vl[m] * z12vl[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                    carr1f[n] = M_PI * xln_n * binsum / (4.0 * (2 * n + 1));
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        sump += z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                    carr4f[n] = xrn_n * sump;
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        sump += z12v[m] * z12v[n - m] * pn[m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                    carr5f[n] = xrmn_n * sump;
+                    carr6f[n] = carr4f[n] / pn[n];
+                } else {
+                    carr1p[n] = 2 * std::pow(4.0, n) * z12vl[n] * xln_n / ((n + 2) * (n + 1) * (n + 1) * fkv[n] * fkv[n]);
+                    carr4p[n] = std::pow(4.0, n) * std::sqrt(M_PI) * z12v[n] * xrn_n / (2.0 * (n + 1) * gam3[n] * fkv[n]);
+                    double sump = 0.0;
+                    for (int m = 0; m <= n; m++) sump += pn[m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                    carr5p[n] = M_PI * z12v[n] * xrmn_n * sump / 4.0;
+                    carr6p[n] = carr4p[n] / pn[n];
+                    double binsum = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        binsum += z12vl[m] * z12vl[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                    carr1f[n] = std::sqrt(M_PI) * fkv[n] * xln_n * binsum / (2.0 * gam3[n]);
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++) sump += z12v[m] * z12v[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                    carr4f[n] = M_PI * xrn_n * sump / 4.0;
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        sump += pn[m] * z12v[m] * z12v[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                    carr5f[n] = M_PI * xrmn_n * sump / 4.0;
+                    carr6f[n] = carr4f[n] / pn[n];
+                }
+                if (std::fabs(carr1p[n]) < kMin) {
+                    if (n < n1) n1 = n;
+                }
+                if (std::fabs(carrp[2][n]) < kMin) {
+                    if (n < n3) n3 = n;
+                }
+                if (std::fabs(carr4p[n]) < kMin) {
+                    if (n < n4) n4 = n;
+                }
+                if (std::fabs(carr5p[n]) < kMin) {
+                    if (n < n5) n5 = n;
+                }
+                if (std::fabs(carr6p[n]) < kMin) {
+                    if (n < n6) n6 = n;
+                }
+                if (std::fabs(carr1f[n]) < kMin) {
+                    if (n < n1f) n1f = n;
+                }
+                if (std::fabs(carr4f[n]) < kMin) {
+                    if (n < n4f) n4f = n;
+                }
+                if (std::fabs(carr5f[n]) < kMin) {
+                    if (n < n5f) n5f = n;
+                }
+                if (std::fabs(carr6f[n]) < kMin) {
+                    if (n < n6f) n6f = n;
+                }
+            }
+            done = true;
+        } else {
+            supported = false;
+        }
     } else if ((P.ordis == 6) && (cdim != 3)) {
         // perfect orientation for cylinders and disks, :4124-4644
         P.norm = 1;
@@ -1954,11 +2142,13 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
                           P.key == CS_KEY_CYL_GAUSS_BCT_ZDIR || P.key == CS_KEY_CUBE_NONE_ISO);
     if (!special) {
         // the generic pixel function covers the particles prepared above:
-        // spheres, cylinders (z-direction, Gaussian orientation), homogeneous
+        // spheres, cylinders (z-direction, Gaussian orientation; isotropic,
+        // homogeneous or core/shell), homogeneous
         // isotropic cubes, z-direction disks along an axis without a lattice,
         // isotropic or z-direction vesicles, and homogeneous isotropic
         // ellipsoids
         const bool ok = P.particle == 0 || (P.particle == 1 && (P.ordis == 6 || P.ordis == 0)) ||
+                        (P.particle == 1 && P.ordis == 7 && (P.cs == 0 || P.cs == 1)) ||
                         (P.particle == 4 && P.ordis == 7 && P.cs == 0) ||
                         (P.particle == 2 && P.ordis == 6 && P.cs == 0 && !P.lattice && P.orcase != CS_ORC_GENERAL) ||
                         (P.particle == 3 && (P.ordis == 7 || P.ordis == 6)) ||

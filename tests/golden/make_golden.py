@@ -93,6 +93,15 @@ def image_cases():
     cases["vesicle_iso_g32"] = dict(ves, iso=0.2)
     cases["vesicle_zdir_g32"] = dict(ves, Ordis=6)
     cases["vesicle_fcc_g24"] = dict(sph, ComboBoxParticle=3, Ordis=7, Length=12.0, SigmaL=0.15)
+    # isotropic cylinders (exact average for short ones, factorised for long
+    # ones), homogeneous and core/shell, alone and on a lattice
+    cyl_iso = dict(C.scaled(C.CYL_GAUSS, 32), Ordis=7)
+    cases["cyl_iso_g32"] = dict(cyl_iso)
+    cases["cyl_iso_short_g24"] = dict(C.scaled(C.CYL_GAUSS, 24), Ordis=7, EditRadius=10.0, Length=15.0)
+    cases["cyl_iso_cs_g32"] = dict(cyl_iso, ComboBoxInterior=1, EditRadiusi=7.0, EditRho=0.3)
+    cases["cyl_iso_fcc_g24"] = dict(sph, ComboBoxParticle=1, Ordis=7, EditRadius=5.0, Length=30.0, SigmaL=0.1)
+    cases["cyl_iso_cs_fcc_g24"] = dict(sph, ComboBoxParticle=1, Ordis=7, EditRadius=5.0, Length=30.0, SigmaL=0.1,
+                                       ComboBoxInterior=1, EditRadiusi=7.0, EditRho=0.3)
     ell = dict(C.scaled(C.SPHERE, 32), ComboBoxParticle=5, Ordis=7)
     cases["ellipsoid_prolate_g32"] = dict(ell, Length=16.0)
     cases["ellipsoid_oblate_g32"] = dict(ell, Length=6.0, iso=0.1)
@@ -124,8 +133,15 @@ def rejected_cases():
 def main():
     if not refbind.available():
         sys.exit("oracle/_ref/libscref.so not built (oracle/build_ref.sh)")
+    # --only a,b: (re)generate just these image cases and merge them into
+    # cases.json; the fit and rejection fixtures are left as they are
+    only = None
+    if "--only" in sys.argv:
+        only = set(sys.argv[sys.argv.index("--only") + 1].split(","))
     out = {}
     for name, p in image_cases().items():
+        if only is not None and name not in only:
+            continue
         r = refbind.RefCalc(p)
         ign = ign_cbs_for(p)
         ins = 1 if name in IGN_NEW_SWITCH else 0
@@ -165,6 +181,13 @@ def main():
         print(name, img.shape, "nonfinite", out[name]["nonfinite"], "zeros", out[name]["zeros"],
               "ill-conditioned", out[name]["ill_conditioned"])
         r.close()
+    if only is not None:
+        with open(os.path.join(HERE, "cases.json")) as f:
+            allc = json.load(f)
+        allc["images"].update(out)
+        with open(os.path.join(HERE, "cases.json"), "w") as f:
+            json.dump(allc, f, indent=1, sort_keys=True)
+        return
 
     # fit cases: target = reference image * deterministic multiplicative noise
     fits = {}
