@@ -373,6 +373,7 @@ def sweep_accuracy_vs_cpu(b, out_host_view, names, rows_per_set=8):
     from oracle import ref_prepared as R
     nt = cpu_threads()
     gi, ri, ci = [], [], []
+    worst = None  # largest error where the reference is stable to 1e-6: (err, set, ihex, i, got, ref, cond)
     for name in names:
         k = int(name[len("bct_set"):])
         blk = R.load(name)
@@ -382,10 +383,19 @@ def sweep_accuracy_vs_cpu(b, out_host_view, names, rows_per_set=8):
         off, x0, x1, y0, y1 = b.layout(k)
         g = out_host_view(off, (x1 - x0) * (y1 - y0)).reshape(y1 - y0, x1 - x0)
         cols = np.asarray(rows) - blk.xmin
-        gi.append(g[:, cols].ravel())
-        ri.append(o[:, cols].ravel())
-        ci.append(cond[:, cols].ravel())
+        gs, rs, cs_ = g[:, cols], o[:, cols], cond[:, cols]
+        with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
+            e = np.abs(gs - rs) / np.maximum(np.abs(rs), 1e-300)
+        e = np.where((cs_ <= 1e-6) & np.isfinite(e), e, 0.0)
+        j = np.unravel_index(np.argmax(e), e.shape)
+        if worst is None or e[j] > worst[0]:
+            worst = (float(e[j]), k, int(rows[j[1]]), int(j[0] + blk.ymin), float(gs[j]), float(rs[j]), float(cs_[j]))
+        gi.append(gs.ravel())
+        ri.append(rs.ravel())
+        ci.append(cs_.ravel())
     st = rel_stats(np.concatenate(gi), np.concatenate(ri), np.concatenate(ci))
+    if worst is not None:
+        st["worst_where_cond_le_1e-6"] = dict(zip(("rel", "set", "ihex", "i", "gpu", "cpu", "cond"), worst))
     st["sample"] = f"{len(names)} reference-prepared sets (k = 0, 64, ..., 4032), {rows_per_set} ihex rows each"
     return st
 

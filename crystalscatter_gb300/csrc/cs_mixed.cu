@@ -206,22 +206,6 @@ __device__ float cyl_pqr_asym(double argpq_d, double zr_d, float &rel) {
     return v;
 }
 
-// The same in FP64 for lattice pixels (there the FP32 form's ~1e-6 is
-// amplified where the structure factor cancels): one atan, one log1p, two
-// exps, a sine and a cosine. Its own error is that of a few FP64 roundings per
-// term, relative to the sum.
-__device__ double cyl_pqr_asym_d(double argpq, double zr, float &rel) {
-    const double t = atan(2.0 * argpq), L = log1p(4.0 * argpq * argpq);
-    const double a3 = argpq * argpq * argpq;
-    const double pqr1 = (1.0 / (zr * (zr - 1) * (zr - 2))) / a3;
-    const double pqr2 = pqr1 * sin((zr - 2) * t) / exp((zr - 2) / 2.0 * L);
-    const double b3 = (1.0 / (zr * (zr - 1) * (zr - 2) * (zr - 3))) / (a3 * argpq);
-    const double pqr3 = b3 * cos((zr - 3) * t) / exp((zr - 3) / 2.0 * L);
-    const double v = (4.0 / M_PI) * (pqr1 - pqr2 - (9.0 / 8.0) * pqr3);
-    rel = (float)((fabs(pqr1) + fabs(pqr2) + fabs(pqr3)) * 1e-13 / fabs(v) + 1e-15);
-    return v;
-}
-
 // cylinder cross-section F(q), q >= limq4f (Source/sc_lib_formfq_partCylinder.h)
 // amplitude squared; gamma ratios from the preparation
 template <bool ACC>
@@ -874,17 +858,15 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
         } else {
             const double zl = z_of(P.sigmal);
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-            if (LAT) {
-                // lattice pixels need the length factor beyond FP32 accuracy
-                // where the structure factor cancels: evaluated as the drop-in
-                // does (same value)
-                pql = cs64::len_factor(arglq, zl);
-            } else {
-                float rel;
-                pql = cyl_len_factor_e<false>(arglq, zl, rel);
-                if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
-                el = rel;
-            }
+            // FP32 closed form (its small-argument series where it cancels),
+            // refined with FP64 arguments when its own estimate exceeds the
+            // switch; lattice pixels carry the estimate into the structure
+            // factor's error bound (lattice_combine), which sends the pixels
+            // where the structure factor amplifies it to the FP64 redo
+            float rel;
+            pql = cyl_len_factor_e<false>(arglq, zl, rel);
+            if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
+            el = rel;
         }
     } else if (P.ordis == 0) {
         const double thr = 0.4 * P.limq[1];
@@ -957,13 +939,9 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             float rel;
             const double zr = z_of(P.sigma);
             const double argpq = q * P.radius / (zr + 1);
-            if (LAT) {
-                pqr = cyl_pqr_asym_d(argpq, zr, rel);
-            } else {
-                pqr = cyl_pqr_asym<false>(argpq, zr, rel);
-                // (a zero length factor makes the product zero: no need to refine)
-                if (!(rel <= acc_switch<LAT>()) && !zero_len) pqr = cyl_pqr_asym<true>(argpq, zr, rel);
-            }
+            pqr = cyl_pqr_asym<false>(argpq, zr, rel);
+            // (a zero length factor makes the product zero: no need to refine)
+            if (!(rel <= acc_switch<LAT>()) && !zero_len) pqr = cyl_pqr_asym<true>(argpq, zr, rel);
             // a finite factor of a zero product carries no error into it
             er = (zero_len && isfinite(pqr)) ? 0.0f : rel;
         }
@@ -993,17 +971,15 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             pql = cs64::series_zdir(P.carrf[0], qxs, qys);
         } else {
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
-            if (LAT) {
-                // lattice pixels need the length factor beyond FP32 accuracy
-                // where the structure factor cancels: evaluated as the drop-in
-                // does (same value)
-                pql = cs64::len_factor(arglq, zl);
-            } else {
-                float rel;
-                pql = cyl_len_factor_e<false>(arglq, zl, rel);
-                if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
-                el = rel;
-            }
+            // FP32 closed form (its small-argument series where it cancels),
+            // refined with FP64 arguments when its own estimate exceeds the
+            // switch; lattice pixels carry the estimate into the structure
+            // factor's error bound (lattice_combine), which sends the pixels
+            // where the structure factor amplifies it to the FP64 redo
+            float rel;
+            pql = cyl_len_factor_e<false>(arglq, zl, rel);
+            if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
+            el = rel;
         }
     } else if (P.ordis == 0) {
         const double thr = 0.2 * P.limqf[1];
