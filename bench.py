@@ -441,6 +441,27 @@ def sweep(cs, torch, C, args, world, peaks, work, clocks_start):
     clk = clocks.stop()
     t_kernel = sum(times)
     redo, cap = b.redo_pixels(sp)
+
+    def timed(fn):
+        fn()
+        s.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        fn()
+        e.record(s)
+        e.synchronize()
+        return a.elapsed_time(e) / 1e3
+
+    # the autotuned schedule against the fixed one (block tiles of 256 pixels
+    # at the occupancy limit), one persistent launch each
+    row["schedule"] = b.schedule(0)
+    t_tuned = timed(lambda: b.launch(out.data_ptr(), total, sp, cs.CS_MODE_MIXED, cs.CS_SCHED_PERSISTENT))
+    b.set_schedule(0, 0)
+    t_fixed = timed(lambda: b.launch(out.data_ptr(), total, sp, cs.CS_MODE_MIXED, cs.CS_SCHED_PERSISTENT))
+    b.set_schedule(-1, 0)
+    row["schedule_comparison"] = {"tuned_s": t_tuned, "fixed_block_tile_256_s": t_fixed,
+                                  "speedup_tuned_over_fixed": t_fixed / t_tuned}
     # the dominant kernel alone: CUDA events around it on its stream
     prof = [b.profile(out.data_ptr(), total, sp, cs.CS_MODE_MIXED) for _ in range(2)]
     main_ms = min(p[0] for p in prof)
@@ -451,21 +472,9 @@ def sweep(cs, torch, C, args, world, peaks, work, clocks_start):
     # FP64 drop-in: one plain launch per set (the drop-in's own call pattern)
     if not args.no_fp64:
         ref = torch.empty_like(out)
-
-        def timed(fn):
-            fn()
-            s.synchronize()
-            a = torch.cuda.Event(enable_timing=True)
-            e = torch.cuda.Event(enable_timing=True)
-            a.record(s)
-            fn()
-            e.record(s)
-            e.synchronize()
-            return a.elapsed_time(e) / 1e3
-
         t_fplain = timed(lambda: b.launch(ref.data_ptr(), total, sp, cs.CS_MODE_FP64, cs.CS_SCHED_PLAIN))
         t_mplain = timed(lambda: b.launch(out.data_ptr(), total, sp, cs.CS_MODE_MIXED, cs.CS_SCHED_PLAIN))
-        b.replay(sp)
+        b.launch(out.data_ptr(), total, sp, cs.CS_MODE_MIXED, cs.CS_SCHED_PERSISTENT)
         s.synchronize()
         row.update({"fp64_plain_launches_s": t_fplain, "fp64_plain_launches_pixels_per_s": npix / t_fplain,
                     "mixed_plain_launches_s": t_mplain,

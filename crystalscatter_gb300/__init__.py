@@ -154,6 +154,9 @@ def _sig(lib):
     lib.cs_batch_prepare.argtypes = [B, P(CsParams), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     lib.cs_batch_info.argtypes = [B, P(ctypes.c_size_t), P(ctypes.c_long), P(ctypes.c_int)]
     lib.cs_batch_upload_bytes.argtypes = [B, P(ctypes.c_size_t)]
+    lib.cs_batch_set_schedule.argtypes = [B, ctypes.c_int, ctypes.c_int]
+    lib.cs_batch_schedule.argtypes = [B, ctypes.c_int, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int),
+                                      P(ctypes.c_double), P(ctypes.c_int)]
     lib.cs_batch_layout.argtypes = [B, ctypes.c_int, P(ctypes.c_size_t)] + [P(ctypes.c_int)] * 4
     lib.cs_batch_launch.argtypes = [B, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
     lib.cs_batch_profile.argtypes = [B, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_int,
@@ -467,6 +470,21 @@ class SasCalcBatch:
         d, p, g = ctypes.c_size_t(), ctypes.c_long(), ctypes.c_int()
         self._check(self._lib.cs_batch_info(self._b, ctypes.byref(d), ctypes.byref(p), ctypes.byref(g)))
         return d.value, p.value, g.value
+
+    def set_schedule(self, chunk=-1, blocks_per_sm=0):
+        """Force the mixed persistent kernel's work unit (0 = block tiles,
+        32..256 = warp chunk) and resident blocks per SM; chunk -1 = autotune."""
+        self._check(self._lib.cs_batch_set_schedule(self._b, int(chunk), int(blocks_per_sm)))
+
+    def schedule(self, group=0):
+        """The schedule in use for a key group: dict(key, chunk, blocks_per_sm,
+        ns_per_pixel, tuned)."""
+        k, c, b, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        ns = ctypes.c_double()
+        self._check(self._lib.cs_batch_schedule(self._b, int(group), ctypes.byref(k), ctypes.byref(c), ctypes.byref(b),
+                                                ctypes.byref(ns), ctypes.byref(t)))
+        return {"key": hex(k.value), "chunk": c.value, "blocks_per_sm": b.value, "ns_per_pixel": ns.value,
+                "tuned": bool(t.value)}
 
     def upload_bytes(self):
         """host-to-device bytes of the last prepare"""

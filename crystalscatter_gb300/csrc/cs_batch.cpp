@@ -23,6 +23,8 @@
 #include <cstdint>
 #include <cstring>
 #include <string>
+#include <map>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -104,6 +106,19 @@ struct cs_batch {
     size_t h_fit_cap = 0;
     cudaGraphExec_t fit_exec = nullptr;
     std::vector<long long> fit_graph_sig;
+
+    // schedule of the mixed persistent kernel per group: work unit (0 = block
+    // tiles, 32..CS_BATCH_TILE = pixels per warp chunk) and resident blocks
+    // per SM; chosen by the autotuner at the first mixed persistent run of a
+    // key on a device (cached), or forced by cs_batch_set_schedule
+    struct Sched {
+        int chunk = -1;
+        int bps = 0;
+        double ns_per_px = 0;
+        int tuned = 0;
+    };
+    std::vector<Sched> sched;
+    int force_chunk = -1, force_bps = 0;
 
     double t_prep = 0;
     bool prepared = false;
@@ -197,6 +212,101 @@ int ensure_redo(cs_batch *b) {
     return CS_OK;
 }
 
+// ---- autotuner of the mixed persistent kernels ----------------------------
+// Candidates per dispatch key: block tiles (the barrier-synchronised form) or
+// warp chunks of 32, 64, 128 or 256 pixels, at the occupancy limit of
+// resident blocks per SM or half of it. Each candidate computes the same
+// prefix of the group's pixels (1/32 of them, at least 8 tiles per resident
+// block) with the main kernel alone, timed with CUDA events; the fastest per
+// pixel wins and is cached per (device, key) for the process.
+std::mutex g_tune_mutex;
+std::map<std::pair<int, int>, cs_batch::Sched> g_tune_cache;
+
+int tune_group(cs_batch *b, size_t gi, double *d_out, cudaStream_t s, cs_batch::Sched &out) {
+    const cs::BatchGroup &g = b->groups[gi];
+    const int occ = std::max(cs::batch_blocks_per_sm_mixed(g.key), 1);
+    const long gpx = g.tiles * (long)CS_BATCH_TILE;
+    long sample = std::max(gpx / 32, (long)b->sm_count * occ * CS_BATCH_TILE * 8);
+    sample = std::min(sample, gpx);
+    std::vector<std::pair<int, int>> cand;
+    for (int chunk : {0, 32, 64, 128, 256}) {
+        cand.push_back({chunk, occ});
+        if (occ > 1) cand.push_back({chunk, occ / 2});
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return cuda_fail(b, e, "cudaEventCreate");
+    }
+    int rc = CS_OK;
+    double best = 1e300;
+    for (size_t c = 0; c <= cand.size() && rc == CS_OK; c++) {
+        // entry 0 runs twice: the first pass warms up (clocks, caches) untimed
+        const auto [chunk, bps] = cand[c == 0 ? 0 : c - 1];
+        const long limit = sample / (chunk ? chunk : CS_BATCH_TILE);
+        if ((e = cudaMemsetAsync(b->d_counters + gi, 0, sizeof(unsigned long long), s)) != cudaSuccess ||
+            (e = cudaMemsetAsync(b->redo.d_count + gi, 0, sizeof(int), s)) != cudaSuccess) {
+            rc = cuda_fail(b, e, "cudaMemsetAsync(tuning)");
+            break;
+        }
+        cudaEventRecord(e0, s);
+        rc = cs::launch_batch_mixed(b->dsets, g, (int)gi, b->d_counters + gi, b->d_chi, d_out, b->redo,
+                                    b->sm_count * bps, s, nullptr, chunk, limit, false);
+        if (rc == CS_ERR_CUDA) rc = cuda_fail(b, cs::last_launch_error(), "tuning launch");
+        cudaEventRecord(e1, s);
+        if (rc == CS_OK && (e = cudaEventSynchronize(e1)) != cudaSuccess) rc = cuda_fail(b, e, "tuning run");
+        if (rc != CS_OK || c == 0) continue;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        const double ns = ms * 1e6 / (double)sample;
+        if (ns < best) {
+            best = ns;
+            out.chunk = chunk;
+            out.bps = bps;
+            out.ns_per_px = ns;
+            out.tuned = 1;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+// Schedules of every group for a mixed persistent run (before any capture).
+int ensure_schedule(cs_batch *b, double *d_out, cudaStream_t s) {
+    if (b->sched.size() != b->groups.size()) b->sched.assign(b->groups.size(), cs_batch::Sched{});
+    for (size_t gi = 0; gi < b->groups.size(); gi++) {
+        cs_batch::Sched &sc = b->sched[gi];
+        if (sc.chunk >= 0) continue;
+        const int key = b->groups[gi].key;
+        if (!cs::mixed_key(key)) continue;
+        const int occ = std::max(cs::batch_blocks_per_sm_mixed(key), 1);
+        if (b->force_chunk >= 0) {
+            sc.chunk = b->force_chunk;
+            sc.bps = b->force_bps > 0 ? std::min(b->force_bps, occ) : occ;
+            sc.tuned = 0;
+            continue;
+        }
+        const std::pair<int, int> ck{b->device, key};
+        {
+            std::lock_guard<std::mutex> lock(g_tune_mutex);
+            auto it = g_tune_cache.find(ck);
+            if (it != g_tune_cache.end()) {
+                sc = it->second;
+                continue;
+            }
+        }
+        int rc = ensure_redo(b);
+        if (rc) return rc;
+        if ((rc = tune_group(b, gi, d_out, s, sc))) return rc;
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache[ck] = sc;
+    }
+    return CS_OK;
+}
+
 // Enqueue one evaluation of all sets on stream s. marks (persistent schedule
 // only): three events per group, recorded before the group's main kernel,
 // between it and its redo kernel, and after the redo.
@@ -221,13 +331,20 @@ int enqueue(cs_batch *b, double *d_out, cudaStream_t s, int mode, int schedule, 
         for (size_t gi = 0; gi < b->groups.size(); gi++) {
             const cs::BatchGroup &g = b->groups[gi];
             const bool mixed = mode == CS_MODE_MIXED && cs::mixed_key(g.key);
-            const int per_sm = mixed ? cs::batch_blocks_per_sm_mixed(g.key) : cs::batch_blocks_per_sm_fp64(g.key);
+            int per_sm = mixed ? cs::batch_blocks_per_sm_mixed(g.key) : cs::batch_blocks_per_sm_fp64(g.key);
+            // the mixed kernel's schedule (autotuned, or warp chunks of 32 at
+            // the occupancy limit when no run has tuned it yet)
+            int chunk = 32;
+            if (mixed && gi < b->sched.size() && b->sched[gi].chunk >= 0) {
+                chunk = b->sched[gi].chunk;
+                per_sm = b->sched[gi].bps;
+            }
             long grid = (long)b->sm_count * std::max(per_sm, 1);
             grid = std::min(grid, std::max(g.tiles, 1L));
             if (marks) cudaEventRecord(marks[3 * gi], s);
             int rc = mixed
                          ? cs::launch_batch_mixed(b->dsets, g, (int)gi, b->d_counters + gi, b->d_chi, d_out, b->redo,
-                                                  (int)grid, s, marks ? marks[3 * gi + 1] : nullptr)
+                                                  (int)grid, s, marks ? marks[3 * gi + 1] : nullptr, chunk)
                          : cs::launch_batch_fp64(b->dsets, g, b->d_counters + gi, b->d_chi, d_out, (int)grid, s);
             if (marks) {
                 if (!mixed) cudaEventRecord(marks[3 * gi + 1], s);
@@ -460,6 +577,7 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
     if (nd) dt.resize(nd * CS_NODE_COUNT);
     b->hsets.assign(nsets, cs::BatchSetDev{});
     b->groups.clear();
+    b->sched.clear();
     size_t di = 0;
     for (int j = 0; j < nsets; j++) {
         const int k = b->order[j];
@@ -540,6 +658,31 @@ int cs_batch_info(cs_batch *b, size_t *total_doubles, long *total_pixels, int *n
     return CS_OK;
 }
 
+int cs_batch_set_schedule(cs_batch *b, int chunk, int blocks_per_sm) {
+    if (!b) return CS_ERR_PARAM;
+    if (chunk != -1 && chunk != 0 && (chunk < 32 || chunk > CS_BATCH_TILE || chunk % 32 || CS_BATCH_TILE % chunk))
+        return fail(b, CS_ERR_PARAM, "chunk must be -1 (autotune), 0 (block tiles) or 32..256 pixels dividing 256");
+    if (blocks_per_sm < 0) return fail(b, CS_ERR_PARAM, "blocks_per_sm must be >= 0");
+    b->force_chunk = chunk;
+    b->force_bps = blocks_per_sm;
+    b->sched.clear();
+    drop_graph(b);
+    return CS_OK;
+}
+
+int cs_batch_schedule(cs_batch *b, int group, int *key, int *chunk, int *blocks_per_sm, double *ns_per_pixel,
+                      int *tuned) {
+    if (!b) return CS_ERR_PARAM;
+    if (group < 0 || (size_t)group >= b->groups.size()) return fail(b, CS_ERR_PARAM, "group index out of range");
+    const cs_batch::Sched sc = (size_t)group < b->sched.size() ? b->sched[group] : cs_batch::Sched{};
+    if (key) *key = b->groups[group].key;
+    if (chunk) *chunk = sc.chunk;
+    if (blocks_per_sm) *blocks_per_sm = sc.bps;
+    if (ns_per_pixel) *ns_per_pixel = sc.ns_per_px;
+    if (tuned) *tuned = sc.tuned;
+    return CS_OK;
+}
+
 int cs_batch_upload_bytes(cs_batch *b, size_t *bytes) {
     if (!b || !bytes) return CS_ERR_PARAM;
     if (!b->prepared) return fail(b, CS_ERR_STATE, "no prepared batch");
@@ -573,6 +716,7 @@ int cs_batch_launch(cs_batch *b, double *d_out, size_t n_doubles, void *stream, 
     if (rc) return rc;
     // the uploads of cs_batch_prepare have completed, so any stream may run the batch
     cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    if (mode == CS_MODE_MIXED && schedule == CS_SCHED_PERSISTENT && (rc = ensure_schedule(b, d_out, s))) return rc;
     return enqueue(b, d_out, s, mode, schedule);
 }
 
@@ -582,6 +726,7 @@ int cs_batch_profile(cs_batch *b, double *d_out, size_t n_doubles, void *stream,
     int rc = check_run_args(b, d_out, n_doubles, mode);
     if (rc) return rc;
     cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    if (mode == CS_MODE_MIXED && (rc = ensure_schedule(b, d_out, s))) return rc;
     const size_t ng = b->groups.size();
     std::vector<cudaEvent_t> ev(3 * ng, nullptr);
     cudaError_t e = cudaSuccess;
@@ -612,7 +757,9 @@ int cs_batch_capture(cs_batch *b, double *d_out, size_t n_doubles, int mode, int
     if (rc) return rc;
     drop_graph(b);
     // allocations happen before the capture (they are not capturable)
-    if (schedule == CS_SCHED_PERSISTENT && mode == CS_MODE_MIXED && (rc = ensure_redo(b))) return rc;
+    if (schedule == CS_SCHED_PERSISTENT && mode == CS_MODE_MIXED &&
+        ((rc = ensure_redo(b)) || (rc = ensure_schedule(b, d_out, b->stream))))
+        return rc;
     if (schedule == CS_SCHED_PLAIN && mode == CS_MODE_MIXED) {
         // size the plain redo scratch by a dry pass over the sets
         long most = 0;
@@ -842,7 +989,8 @@ int cs_batch_run_host(cs_batch *b, int mode, double *out, size_t n_doubles) {
     cudaError_t e = cudaMallocAsync(&d_out, sizeof(double) * b->total_doubles, b->stream);
     if (e != cudaSuccess) return cuda_fail(b, e, "cudaMallocAsync(batch images)");
     int rc = CS_OK;
-    for (int attempt = 0; attempt < 3; attempt++) {
+    if (mode == CS_MODE_MIXED) rc = ensure_schedule(b, d_out, b->stream);
+    for (int attempt = 0; attempt < 3 && rc == CS_OK; attempt++) {
         rc = enqueue(b, d_out, b->stream, mode, CS_SCHED_PERSISTENT);
         if (rc || mode != CS_MODE_MIXED) break;
         long n = 0;

@@ -46,6 +46,51 @@ __device__ __forceinline__ bool batch_next_tile(const BatchSetDev *__restrict__ 
     return tile < tiles;
 }
 
+// Warp-level form of the queue: lane 0 of a warp takes the next chunk of
+// `chunk` pixels (a multiple of 32 dividing CS_BATCH_TILE; the counter counts
+// chunks) and finds its set as above; no barrier, so a warp that finishes
+// early takes the next chunk at once instead of waiting for the slowest warp
+// of its block. Returns false when the group's chunks (tiles * TILE/chunk)
+// or the first `limit` of them are taken. pix0: first pixel of the chunk in
+// the set's calculated region.
+__device__ __forceinline__ bool batch_next_chunk(const BatchSetDev *__restrict__ sets, int set_begin, int set_end,
+                                                 long tiles, int chunk, long limit, unsigned long long *counter,
+                                                 int &cur, long &pix0, int &set) {
+    const int lane = threadIdx.x & 31;
+    const long per_tile = CS_BATCH_TILE / chunk;
+    long nchunks = tiles * per_tile;
+    if (limit > 0 && limit < nchunks) nchunks = limit;
+    long c = 0;
+    if (lane == 0) {
+        c = (long)atomicAdd(counter, 1ull);
+        if (c < nchunks) {
+            const long t = c / per_tile;
+            auto inside = [&](int k) {
+                return t >= sets[k].tile_begin && (k + 1 == set_end || t < sets[k + 1].tile_begin);
+            };
+            if (!inside(cur)) {
+                if (cur + 1 < set_end && inside(cur + 1)) {
+                    cur = cur + 1;
+                } else {
+                    int lo = set_begin, hi = set_end - 1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (sets[mid].tile_begin <= t) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    cur = lo;
+                }
+            }
+        }
+    }
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= nchunks) return false;
+    set = __shfl_sync(0xffffffffu, cur, 0);
+    const long t = c / per_tile;
+    pix0 = (t - sets[set].tile_begin) * CS_BATCH_TILE + (c % per_tile) * chunk;
+    return true;
+}
+
 }  // namespace cs
 
 #endif

@@ -65,9 +65,12 @@ struct BatchRedo {
 // Persistent mixed-precision launch over one group followed by the FP64 redo
 // of its guarded pixels. counter must be zero when the launch starts.
 // `mid`, when given, is recorded on s between the two (kernel timing).
+// chunk: the work unit (0 = block tiles of CS_BATCH_TILE pixels with
+// barriers; 32..CS_BATCH_TILE = that many pixels per warp, no barrier);
+// limit > 0: stop after that many units; redo = false: the main kernel only.
 int launch_batch_mixed(const BatchSetDev *d_sets, const BatchGroup &g, int group_index, unsigned long long *d_counter,
                        const cs_chi_node *d_chi, double *d_out, const BatchRedo &R, int grid, cudaStream_t s,
-                       cudaEvent_t mid = nullptr);
+                       cudaEvent_t mid = nullptr, int chunk = 0, long limit = 0, bool redo = true);
 // Persistent FP64 launch over one group (the drop-in arithmetic).
 int launch_batch_fp64(const BatchSetDev *d_sets, const BatchGroup &g, unsigned long long *d_counter,
                       const cs_chi_node *d_chi, double *d_out, int grid, cudaStream_t s);

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "cs_fp64.cuh"
@@ -203,6 +204,35 @@ __device__ float cyl_pqr_asym(double argpq_d, double zr_d, float &rel) {
     const float E = 3e-7f * fabsf(pqr1) + fabsf(pqr1) * (g2 + fabsf(S2) * e2) / P2 + 3e-7f * fabsf(pqr2) +
                     1.125f * (fabsf(b3) * (g3 + fabsf(C3) * e3) / P3 + 3e-7f * fabsf(pqr3));
     rel = (4.0f / (float)M_PI) * E / fabsf(v) + 3e-7f;
+    return v;
+}
+
+// The same in FP64, for the second pass of lattice pixels whose structure
+// factor amplifies the FP32 form's error (calc_mixed): one atan, one log1p,
+// two exps, a sine and a cosine; its own error is that of a few FP64
+// roundings per term, relative to the sum.
+__device__ double cyl_pqr_asym_d(double argpq, double zr, float &rel) {
+    const double t = atan(2.0 * argpq), L = log1p(4.0 * argpq * argpq);
+    const double a3 = argpq * argpq * argpq;
+    const double pqr1 = (1.0 / (zr * (zr - 1) * (zr - 2))) / a3;
+    const double pqr2 = pqr1 * sin((zr - 2) * t) / exp((zr - 2) / 2.0 * L);
+    const double b3 = (1.0 / (zr * (zr - 1) * (zr - 2) * (zr - 3))) / (a3 * argpq);
+    const double pqr3 = b3 * cos((zr - 3) * t) / exp((zr - 3) / 2.0 * L);
+    const double v = (4.0 / M_PI) * (pqr1 - pqr2 - (9.0 / 8.0) * pqr3);
+    rel = (float)((fabs(pqr1) + fabs(pqr2) + fabs(pqr3)) * 1e-13 / fabs(v) + 1e-15);
+    return v;
+}
+
+// FP64 amplitude of the cylinder cross-section F(q) asymptote (the drop-in's
+// expression with the prepared Gamma ratios), for the same second pass
+__device__ double cyl_fqr_asym_d(double a, double zr, double g0, double g1, float &rel) {
+    const double t = atan(a);
+    const double p1 = g0 * pow(a, -3 / 2.0) * (sin((zr - 1 / 2.0) * t) - cos((zr - 1 / 2.0) * t)) /
+                      pow(1.0 + a * a, (zr - 1 / 2.0) / 2.0);
+    const double p2 = g1 * pow(a, -5 / 2.0) * (sin((zr - 3 / 2.0) * t) + cos((zr - 3 / 2.0) * t)) /
+                      pow(1.0 + a * a, (zr - 3 / 2.0) / 2.0);
+    const double v = (2 / sqrt(M_PI)) * (p1 + (9 / 16.0) * p2);
+    rel = (float)(2.0 * (fabs(p1) + fabs(p2)) * 1e-13 / fabs(v) + 1e-15);
     return v;
 }
 
@@ -838,7 +868,8 @@ __device__ double sphere_fq_mixed(const cs_prepared &P, double q, bool &guard, d
 }
 
 // formpq_partCylinder, ordis 0 and 6, cs 0 (mixed)
-template <bool LAT, bool WARP = false>
+// F64: the closed forms in FP64 (the second pass of lattice pixels).
+template <bool LAT, bool WARP = false, bool F64 = false>
 __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, bool &guard, double &err) {
     const cs_prepared &P = *C.P;
     if (P.cs != 0) {
@@ -861,12 +892,16 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             // FP32 closed form (its small-argument series where it cancels),
             // refined with FP64 arguments when its own estimate exceeds the
             // switch; lattice pixels carry the estimate into the structure
-            // factor's error bound (lattice_combine), which sends the pixels
-            // where the structure factor amplifies it to the FP64 redo
-            float rel;
-            pql = cyl_len_factor_e<false>(arglq, zl, rel);
-            if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
-            el = rel;
+            // factor's error bound (lattice_combine), and a second pass takes
+            // the FP64 form where the structure factor amplifies it
+            if (F64) {
+                pql = cs64::len_factor(arglq, zl);
+            } else {
+                float rel;
+                pql = cyl_len_factor_e<false>(arglq, zl, rel);
+                if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
+                el = rel;
+            }
         }
     } else if (P.ordis == 0) {
         const double thr = 0.4 * P.limq[1];
@@ -939,9 +974,13 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             float rel;
             const double zr = z_of(P.sigma);
             const double argpq = q * P.radius / (zr + 1);
-            pqr = cyl_pqr_asym<false>(argpq, zr, rel);
-            // (a zero length factor makes the product zero: no need to refine)
-            if (!(rel <= acc_switch<LAT>()) && !zero_len) pqr = cyl_pqr_asym<true>(argpq, zr, rel);
+            if (F64) {
+                pqr = cyl_pqr_asym_d(argpq, zr, rel);
+            } else {
+                pqr = cyl_pqr_asym<false>(argpq, zr, rel);
+                // (a zero length factor makes the product zero: no need to refine)
+                if (!(rel <= acc_switch<LAT>()) && !zero_len) pqr = cyl_pqr_asym<true>(argpq, zr, rel);
+            }
             // a finite factor of a zero product carries no error into it
             er = (zero_len && isfinite(pqr)) ? 0.0f : rel;
         }
@@ -952,7 +991,7 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
 
 
 // formfq_partCylinder, ordis 0 and 6, cs 0 (mixed)
-template <bool LAT>
+template <bool LAT, bool F64 = false>
 __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qys, double q, bool &guard,
                              double &err) {
     const cs_prepared &P = *C.P;
@@ -974,12 +1013,16 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             // FP32 closed form (its small-argument series where it cancels),
             // refined with FP64 arguments when its own estimate exceeds the
             // switch; lattice pixels carry the estimate into the structure
-            // factor's error bound (lattice_combine), which sends the pixels
-            // where the structure factor amplifies it to the FP64 redo
-            float rel;
-            pql = cyl_len_factor_e<false>(arglq, zl, rel);
-            if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
-            el = rel;
+            // factor's error bound (lattice_combine), and a second pass takes
+            // the FP64 form where the structure factor amplifies it
+            if (F64) {
+                pql = cs64::len_factor(arglq, zl);
+            } else {
+                float rel;
+                pql = cyl_len_factor_e<false>(arglq, zl, rel);
+                if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
+                el = rel;
+            }
         }
     } else if (P.ordis == 0) {
         const double thr = 0.2 * P.limqf[1];
@@ -1023,9 +1066,14 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
     } else {
         const double a = q * P.radius / (zr + 1);
         float rel;
-        float amp = cyl_fqr_asym<false>(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
-        if (!(rel <= acc_switch<LAT>())) amp = cyl_fqr_asym<true>(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
-        pqr = (double)amp * (double)amp;
+        double amp;
+        if (F64) {
+            amp = cyl_fqr_asym_d(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
+        } else {
+            amp = cyl_fqr_asym<false>(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
+            if (!(rel <= acc_switch<LAT>())) amp = cyl_fqr_asym<true>(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
+        }
+        pqr = amp * amp;
         er = rel;
     }
     err = el + er;
@@ -1111,30 +1159,46 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
         return P.base + P.izero * (pq + P.iso) + tailv;
     }
     if (KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR) {
+        // form factors of the orientation case (first pass: FP32 closed forms)
+        auto forms = [&](auto f64tag, double &pq, double &fq) {
+            constexpr bool F = decltype(f64tag)::value;
+            switch (P.orcase) {
+            case CS_ORC_GENERAL:
+                pq = cyl_pq_mixed<true, false, F>(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard, ep);
+                fq = cyl_fq_mixed<true, F>(C, sqrt(P.cosphi * qx * qx + P.sinphi * qy * qy + CS_EPS9),
+                                           qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard, ef);
+                break;
+            case CS_ORC_XAXIS:
+                pq = cyl_pq_mixed<true, false, F>(C, qx, 0, q, guard, ep);
+                fq = cyl_fq_mixed<true, F>(C, fabs(qx), qx, 0, q, guard, ef);
+                break;
+            case CS_ORC_YAXIS:
+                pq = cyl_pq_mixed<true, false, F>(C, 0, qy, q, guard, ep);
+                fq = cyl_fq_mixed<true, F>(C, fabs(qy), 0, qy, q, guard, ef);
+                break;
+            default:
+                pq = cyl_pq_mixed<true, false, F>(C, qx, qy, q, guard, ep);
+                fq = cyl_fq_mixed<true, F>(C, q, qx, qy, q, guard, ef);
+                break;
+            }
+        };
         double pq = 0, fq = 0;
-        switch (P.orcase) {
-        case CS_ORC_GENERAL:
-            pq = cyl_pq_mixed<true>(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard, ep);
-            fq = cyl_fq_mixed<true>(C, sqrt(P.cosphi * qx * qx + P.sinphi * qy * qy + CS_EPS9), qx * P.cosphi * P.sintheta,
-                              qy * P.sinphi * P.sintheta, q, guard, ef);
-            break;
-        case CS_ORC_XAXIS:
-            pq = cyl_pq_mixed<true>(C, qx, 0, q, guard, ep);
-            fq = cyl_fq_mixed<true>(C, fabs(qx), qx, 0, q, guard, ef);
-            break;
-        case CS_ORC_YAXIS:
-            pq = cyl_pq_mixed<true>(C, 0, qy, q, guard, ep);
-            fq = cyl_fq_mixed<true>(C, fabs(qy), 0, qy, q, guard, ef);
-            break;
-        default:
-            pq = cyl_pq_mixed<true>(C, qx, qy, q, guard, ep);
-            fq = cyl_fq_mixed<true>(C, q, qx, qy, q, guard, ef);
-            break;
-        }
+        forms(std::false_type{}, pq, fq);
         double radint, intens, erad, eint;
         peak_sums_f(P, T, qx, qy, qz, q, radint, intens, erad, eint, guard);
         // the reference's BCT function multiplies szqiso by 1 instead of pq
-        return lattice_combine(P, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, guard);
+        bool g2 = false;
+        double v = lattice_combine(P, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, g2);
+        if (g2 && (ep > 1e-12 || ef > 1e-12)) {
+            // the structure factor amplifies the FP32 closed forms' error
+            // beyond the bound: second pass with their FP64 forms (the series
+            // branches are FP64 already and give the same values again)
+            forms(std::true_type{}, pq, fq);
+            g2 = false;
+            v = lattice_combine(P, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, g2);
+        }
+        guard = guard || g2;
+        return v;
     }
     guard = true;
     return 0.0;
@@ -1175,37 +1239,57 @@ __global__ void __launch_bounds__(256) k_image_mixed(Ctx C, PeakTab T, double *_
 }
 
 
-// Persistent mixed-precision kernel over one group of a batch: tiles from the
-// group's counter, pixel arithmetic as k_image_mixed, guarded pixels appended
-// to the group's redo list as (set, pixel).
+// Persistent mixed-precision kernel over one group of a batch, pixel
+// arithmetic as k_image_mixed, guarded pixels appended to the group's redo
+// list as (set, pixel). Work comes from the group's counter either as whole
+// block tiles (chunk = 0: CS_BATCH_TILE pixels per block, thread 0 takes the
+// tile, two barriers per tile) or as warp chunks (chunk = 32..CS_BATCH_TILE
+// pixels per warp, no barrier); `limit` > 0 stops after that many chunks
+// (the autotuner's timed samples).
+template <int KEY>
+__device__ __forceinline__ void batch_mixed_pixel(const cs::BatchSetDev *__restrict__ sets, int k, long t,
+                                                  const cs_chi_node *__restrict__ chi, double *__restrict__ out,
+                                                  int *__restrict__ redo_count, int2 *__restrict__ redo_list,
+                                                  long redo_cap) {
+    const cs::BatchSetDev &S = sets[k];
+    if (t >= S.npix) return;
+    const cs_prepared &P = *S.prep;
+    const Ctx C{S.prep, chi, S.delta};
+    const int ihex = P.zzmin + (int)(t % S.nx);
+    const int i = P.iimin + (int)(t / S.nx);
+    double qx, qy, qz;
+    q_of_pixel<KEY>(P, q_geom(P), ihex, i, qx, qy, qz);
+    bool guard = false;
+    const double v = calc_mixed<KEY>(C, S.peaks, qx, qy, qz, guard);
+    out[S.out_offset + (long)(ihex - P.xmin) + (long)(P.xmax - P.xmin) * (long)(i - P.ymin)] = v;
+    if (guard) {
+        const int pos = atomicAdd(redo_count, 1);
+        if (pos < redo_cap) redo_list[pos] = make_int2(k, (int)t);
+    }
+}
+
 template <int KEY>
 __global__ void __launch_bounds__(CS_BATCH_TILE) k_batch_mixed(const cs::BatchSetDev *__restrict__ sets,
-                                                               int set_begin, int set_end, long tiles,
-                                                               unsigned long long *__restrict__ counter,
+                                                               int set_begin, int set_end, long tiles, int chunk,
+                                                               long limit, unsigned long long *__restrict__ counter,
                                                                const cs_chi_node *__restrict__ chi,
                                                                double *__restrict__ out, int *__restrict__ redo_count,
                                                                int2 *__restrict__ redo_list, long redo_cap) {
     int cur = set_begin;
-    long tile;
     int k;
-    while (cs::batch_next_tile(sets, set_begin, set_end, tiles, counter, cur, tile, k)) {
-        const cs::BatchSetDev &S = sets[k];
-        const long t = (tile - S.tile_begin) * CS_BATCH_TILE + threadIdx.x;
-        if (t >= S.npix) continue;
-        const cs_prepared &P = *S.prep;
-        const Ctx C{S.prep, chi, S.delta};
-        const int ihex = P.zzmin + (int)(t % S.nx);
-        const int i = P.iimin + (int)(t / S.nx);
-        double qx, qy, qz;
-        q_of_pixel<KEY>(P, q_geom(P), ihex, i, qx, qy, qz);
-        bool guard = false;
-        const double v = calc_mixed<KEY>(C, S.peaks, qx, qy, qz, guard);
-        out[S.out_offset + (long)(ihex - P.xmin) + (long)(P.xmax - P.xmin) * (long)(i - P.ymin)] = v;
-        if (guard) {
-            const int pos = atomicAdd(redo_count, 1);
-            if (pos < redo_cap) redo_list[pos] = make_int2(k, (int)t);
-        }
+    if (chunk == 0) {
+        long tile;
+        const long lim = limit > 0 && limit < tiles ? limit : tiles;
+        while (cs::batch_next_tile(sets, set_begin, set_end, lim, counter, cur, tile, k))
+            batch_mixed_pixel<KEY>(sets, k, (tile - sets[k].tile_begin) * CS_BATCH_TILE + threadIdx.x, chi, out,
+                                   redo_count, redo_list, redo_cap);
+        return;
     }
+    const int lane = threadIdx.x & 31;
+    long pix0;
+    while (cs::batch_next_chunk(sets, set_begin, set_end, tiles, chunk, limit, counter, cur, pix0, k))
+        for (int o = 0; o < chunk; o += 32)
+            batch_mixed_pixel<KEY>(sets, k, pix0 + o + lane, chi, out, redo_count, redo_list, redo_cap);
 }
 
 // Redo of the guarded pixels of the orientation-averaged cylinder, one pixel
@@ -1373,15 +1457,15 @@ int launch_image_mixed(const DevSet &D, const csm::PeakTab &T, const cs_prepared
 
 int launch_batch_mixed(const BatchSetDev *d_sets, const BatchGroup &g, int group_index, unsigned long long *d_counter,
                        const cs_chi_node *d_chi, double *d_out, const BatchRedo &R, int grid, cudaStream_t s,
-                       cudaEvent_t mid) {
+                       cudaEvent_t mid, int chunk, long limit, bool redo) {
     if (g.tiles <= 0) return CS_OK;
     int *cnt = R.d_count + group_index;
     int2 *list = R.d_list + (size_t)group_index * (size_t)R.cap;
     switch (g.key) {
-#define CS_CASE(K)                                                                                               \
-    case K:                                                                                                      \
-        csm::k_batch_mixed<K><<<grid, CS_BATCH_TILE, 0, s>>>(d_sets, g.set_begin, g.set_end, g.tiles, d_counter, \
-                                                              d_chi, d_out, cnt, list, R.cap);                   \
+#define CS_CASE(K)                                                                                                \
+    case K:                                                                                                       \
+        csm::k_batch_mixed<K><<<grid, CS_BATCH_TILE, 0, s>>>(d_sets, g.set_begin, g.set_end, g.tiles, chunk,       \
+                                                              limit, d_counter, d_chi, d_out, cnt, list, R.cap);  \
         break;
         CS_FOR_EACH_KEY(CS_CASE)
 #undef CS_CASE
@@ -1389,6 +1473,7 @@ int launch_batch_mixed(const BatchSetDev *d_sets, const BatchGroup &g, int group
     }
     if (launch_status() != CS_OK) return CS_ERR_CUDA;
     if (mid) cudaEventRecord(mid, s);
+    if (!redo) return CS_OK;
     if (g.key == CS_KEY_CYL_NONE_GAUSS) {
         csm::k_batch_redo_cyl_warp<<<sm_count_m() * 4, 128, 0, s>>>(d_sets, d_chi, d_out, cnt, list, R.cap);
         return launch_status();

@@ -232,6 +232,22 @@ int cs_batch_info(cs_batch *b, size_t *total_doubles, long *total_pixels, int *n
 /* Host-to-device bytes that the last cs_batch_prepare uploaded (prepared
    blocks, reflection and node tables, set table). */
 int cs_batch_upload_bytes(cs_batch *b, size_t *bytes);
+
+/* Schedule of the mixed-precision persistent kernel (no counterpart in the
+   reference). Work comes from a device counter either as block tiles of 256
+   pixels (chunk 0; the block's threads synchronise per tile) or as warp
+   chunks of 32, 64, 128 or 256 pixels (no barrier), with blocks_per_sm
+   resident blocks (0 = the occupancy limit). By default (chunk -1) an
+   autotuner chooses both per dispatch key at the first mixed persistent run
+   (cs_batch_launch/capture/profile/run_host) on a device: every candidate
+   computes the same 1/32 of the group's pixels, timed with CUDA events, and
+   the fastest per pixel is kept for the process. cs_batch_set_schedule
+   forces a schedule (chunk -1 returns to the autotuner);
+   cs_batch_schedule reports the one in use for a key group (tuned = 1 when
+   the autotuner chose it, ns_per_pixel its timed sample). */
+int cs_batch_set_schedule(cs_batch *b, int chunk, int blocks_per_sm);
+int cs_batch_schedule(cs_batch *b, int group, int *key, int *chunk, int *blocks_per_sm, double *ns_per_pixel,
+                      int *tuned);
 int cs_batch_layout(cs_batch *b, int k, size_t *offset, int *xmin, int *xmax, int *ymin, int *ymax);
 /* Enqueue all images of the prepared batch into d_out (device memory,
    n_doubles capacity) on stream (NULL = the batch's stream); asynchronous. */
