@@ -988,15 +988,16 @@ int cs_batch_run_host(cs_batch *b, int mode, double *out, size_t n_doubles) {
     double *d_out = nullptr;
     cudaError_t e = cudaMallocAsync(&d_out, sizeof(double) * b->total_doubles, b->stream);
     if (e != cudaSuccess) return cuda_fail(b, e, "cudaMallocAsync(batch images)");
-    int rc = CS_OK;
-    if (mode == CS_MODE_MIXED) rc = ensure_schedule(b, d_out, b->stream);
-    for (int attempt = 0; attempt < 3 && rc == CS_OK; attempt++) {
+    int rc = mode == CS_MODE_MIXED ? ensure_schedule(b, d_out, b->stream) : CS_OK;
+    // a redo list that overflows is grown and the batch run again (at most twice)
+    for (int attempt = 0; rc == CS_OK && attempt < 3; attempt++) {
         rc = enqueue(b, d_out, b->stream, mode, CS_SCHED_PERSISTENT);
         if (rc || mode != CS_MODE_MIXED) break;
         long n = 0;
         rc = cs_batch_redo_pixels(b, b->stream, &n, nullptr);
-        if (rc != CS_ERR_SIZE) break;
+        if (rc != CS_ERR_SIZE || attempt == 2) break;
         b->redo_cap_req = std::max<long>(n, 2 * b->redo.cap);
+        rc = CS_OK;
     }
     if (rc == CS_OK && (e = cudaMemcpyAsync(out, d_out, sizeof(double) * b->total_doubles, cudaMemcpyDeviceToHost,
                                             b->stream)) != cudaSuccess)

@@ -924,11 +924,19 @@ __device__ inline void peak_sums(const cs_prepared &P, double qx, double qy, dou
     const double widthiso = 1.0 / P.uca;
     radintensity = 0.0;
     intensity = 0.0;
+    // Far from a reflection its term is exactly +0 (x2 beyond kPeakZero).
+    // That is settled first without the division: (q - qhkl)^2 above
+    // kPeakZero width^2 (1 + 1e-12) puts x2 beyond kPeakZero whatever the
+    // division's rounding; only the reflections nearer than that form x2 as
+    // the reference does.
+    const double far_iso = kPeakZero * sqr(widthiso) * (1 + 1e-12);
+    const double far_aniso = kPeakZero * (width * width) * (1 + 1e-12);
     for (int ii = 1; ii <= P.peakmax1; ii++) {
         const int mhkl = P.latpar1[ii][4];
         const int fhkl = P.latpar1[ii][5];
         if (mhkl == 0 || fhkl == 0) continue;
         const double qhkl = P.latpar3[ii][5];
+        if (sqr(q - qhkl) > far_iso) continue;  // the term is exactly +0
         const double x2 = sqr(q - qhkl) / sqr(widthiso);
         if (x2 > kPeakZero) continue;  // the term is exactly +0
         const double sq = exp(-4 * x2 / M_PI) / (M_PI * widthiso / 2.0);
@@ -939,6 +947,12 @@ __device__ inline void peak_sums(const cs_prepared &P, double qx, double qy, dou
         const double qhkl = P.latpar3[ii][5];
         const int mhkl_fhkl = P.latpar2[ii][4] * P.latpar2[ii][5];
         if (qhkl > 0 && mhkl_fhkl != 0) {
+            if ((q - qhkl) * (q - qhkl) > far_aniso && !P.twin) {
+                // radial Gaussian exactly +0: skipped when the angular factor
+                // is finite (as below), without forming x2
+                const double g3 = P.latpar3[ii][10], pn = P.latpar3[ii][11];
+                if (isfinite(g3) && isfinite(pn) && pn != 0) continue;
+            }
             const double qxhkl = P.latpar3[ii][2];
             const double qyhkl = P.latpar3[ii][3];
             const double qzhkl = P.latpar3[ii][4];
@@ -1386,7 +1400,8 @@ static __device__ __noinline__ double calc_generic(const Ctx &C, double qx, doub
                 break;
             }
         }
-    } else if (P.particle == 2) {  // disks, :173-225 (z-direction, axis cases; no lattice)
+    } else if (P.particle == 2) {  // disks, :173-225 (isotropic, or z-direction along an axis; no lattice)
+        if (P.ordis == 7) pq = formpq_disk(P, q, qx, qy, q, 7);
         if (P.ordis == 6) {
             switch (P.orcase) {
             case CS_ORC_XAXIS: pq = formpq_disk(P, fabs(qy), qx / q, 0, q, 6); break;

@@ -891,15 +891,16 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
             // FP32 closed form (its small-argument series where it cancels),
             // refined with FP64 arguments when its own estimate exceeds the
-            // switch; lattice pixels carry the estimate into the structure
-            // factor's error bound (lattice_combine), and a second pass takes
-            // the FP64 form where the structure factor amplifies it
+            // switch; lattice pixels skip that refinement and carry the
+            // estimate into the structure factor's error bound
+            // (lattice_combine): a second pass takes the FP64 form where the
+            // structure factor amplifies it
             if (F64) {
                 pql = cs64::len_factor(arglq, zl);
             } else {
                 float rel;
                 pql = cyl_len_factor_e<false>(arglq, zl, rel);
-                if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
+                if (!LAT && !(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
                 el = rel;
             }
         }
@@ -979,7 +980,7 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             } else {
                 pqr = cyl_pqr_asym<false>(argpq, zr, rel);
                 // (a zero length factor makes the product zero: no need to refine)
-                if (!(rel <= acc_switch<LAT>()) && !zero_len) pqr = cyl_pqr_asym<true>(argpq, zr, rel);
+                if (!LAT && !(rel <= acc_switch<LAT>()) && !zero_len) pqr = cyl_pqr_asym<true>(argpq, zr, rel);
             }
             // a finite factor of a zero product carries no error into it
             er = (zero_len && isfinite(pqr)) ? 0.0f : rel;
@@ -1012,15 +1013,16 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
             // FP32 closed form (its small-argument series where it cancels),
             // refined with FP64 arguments when its own estimate exceeds the
-            // switch; lattice pixels carry the estimate into the structure
-            // factor's error bound (lattice_combine), and a second pass takes
-            // the FP64 form where the structure factor amplifies it
+            // switch; lattice pixels skip that refinement and carry the
+            // estimate into the structure factor's error bound
+            // (lattice_combine): a second pass takes the FP64 form where the
+            // structure factor amplifies it
             if (F64) {
                 pql = cs64::len_factor(arglq, zl);
             } else {
                 float rel;
                 pql = cyl_len_factor_e<false>(arglq, zl, rel);
-                if (!(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
+                if (!LAT && !(rel <= acc_switch<LAT>())) pql = cyl_len_factor_e<true>(arglq, zl, rel);
                 el = rel;
             }
         }
@@ -1071,7 +1073,7 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             amp = cyl_fqr_asym_d(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
         } else {
             amp = cyl_fqr_asym<false>(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
-            if (!(rel <= acc_switch<LAT>())) amp = cyl_fqr_asym<true>(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
+            if (!LAT && !(rel <= acc_switch<LAT>())) amp = cyl_fqr_asym<true>(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
         }
         pqr = amp * amp;
         er = rel;

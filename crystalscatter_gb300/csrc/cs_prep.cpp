@@ -2151,6 +2151,7 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
                         (P.particle == 1 && P.ordis == 7 && (P.cs == 0 || P.cs == 1)) ||
                         (P.particle == 4 && P.ordis == 7 && P.cs == 0) ||
                         (P.particle == 2 && P.ordis == 6 && P.cs == 0 && !P.lattice && P.orcase != CS_ORC_GENERAL) ||
+                        (P.particle == 2 && P.ordis == 7 && P.cs == 0 && !P.lattice) ||
                         (P.particle == 3 && (P.ordis == 7 || P.ordis == 6)) ||
                         (P.particle == 5 && P.ordis == 7 && P.cs == 0);
         if (!ok) {

@@ -543,11 +543,87 @@ static double cyl_double_series(const cs_prepared *P, double qxs, double qys, co
     return pql;
 }
 
-/* formpq_partCylinder, Source/sc_lib_formpq_partCylinder.h:8-282 (ordis 0/6, cs 0) */
+/* cross-section closed form (4/pi)(T1 - T2 - 9/8 T3), Source/sc_lib_formpq_partCylinder.h:272-275 */
+static double cyl_cross_closed(double x, double zr) {
+    const double pqr1 = (1 / (zr * (zr - 1) * (zr - 2))) * pow(x, -3);
+    const double pqr2 = (1 / (zr * (zr - 1) * (zr - 2))) * pow(x, -3) * sin((zr - 2) * atan(2.0 * x)) /
+                        pow(1.0 + 4 * x * x, (zr - 2) / 2.0);
+    const double pqr3 = (1 / (zr * (zr - 1) * (zr - 2) * (zr - 3))) * pow(x, -4) * cos((zr - 3) * atan(2.0 * x)) /
+                        pow(1.0 + 4 * x * x, (zr - 3) / 2.0);
+    return (4 / M_PI) * (pqr1 - pqr2 - (9 / 8.0) * pqr3);
+}
+
+/* core/shell cross-section F121 + F122 + F123, Source/sc_lib_formpq_partCylinder.h:284-393 */
+static double cyl_cross_coreshell(const cs_prepared *P, double q, double zr) {
+    const double radiusm = P->radius / P->p1;
+    const double ccc1 = sqr(1 - P->rho) * pow(P->p1, 4);
+    const double ccc2 = 2 * P->rho * (1 - P->rho) * pow(P->p1, 2);
+    const double ccc3 = P->rho * P->rho;
+    const double vv3 = sqr((1 - P->rho) * pow(P->p1, 2) + P->rho);
+    const double argq = q * radiusm / (zr + 1);
+    const double argpq = q * P->radius / (zr + 1);
+    double F121, F122, F123;
+    if (q < (0.7 * P->limq[4]))
+        F121 = ccc1 * series_q(P->carrp[3], q, 120) / vv3;
+    else
+        F121 = ccc1 * cyl_cross_closed(argpq, zr) / vv3;
+    if (q < (1.5 * P->limq[5])) {
+        F122 = ccc2 * series_q(P->carrp[4], q, 120) / vv3;
+    } else {
+        const double d = argpq - argq, u = argpq + argq;
+        const double pqr1 = (1 / (zr * (zr - 1) * (zr - 2))) * pow(argq, -3) *
+                            (cos((zr - 2) * atan(d)) / pow(1.0 + sqr(d), (zr - 2) / 2.0) -
+                             sin((zr - 2) * atan(u)) / pow(1.0 + sqr(u), (zr - 2) / 2.0));
+        const double pqr2 = (1 / (zr * (zr - 1) * (zr - 2) * (zr - 3))) * pow(argq, -4) *
+                            ((1 - 1 / P->p1) * sin((zr - 3) * atan(d)) / pow(1.0 + sqr(d), (zr - 3) / 2.0) -
+                             (1 + 1 / P->p1) * cos((zr - 3) * atan(u)) / pow(1.0 + sqr(u), (zr - 3) / 2.0));
+        const double pqr3 = (1 / (zr * (zr - 1) * (zr - 2) * (zr - 3) * (zr - 4))) * pow(argq, -5) * (1 / P->p1) *
+                            (cos((zr - 4) * atan(d)) / pow(1.0 + sqr(d), (zr - 4) / 2.0) -
+                             sin((zr - 4) * atan(u)) / pow(1.0 + sqr(u), (zr - 4) / 2.0));
+        const double pqr = (4 / M_PI) * pow(P->p1, -3 / 2.0) * (pqr1 + (9 / 16.0) * pqr2 + (9 / 16.0) * (9 / 16.0) * pqr3);
+        F122 = ccc2 * pqr / vv3;
+    }
+    if (q < (0.6 * P->limq[6]))
+        F123 = ccc3 * series_q(P->carrp[5], q, 120) / vv3;
+    else
+        F123 = ccc3 * cyl_cross_closed(argq, zr) / vv3;
+    return F121 + F122 + F123;
+}
+
+/* isotropic length factor, Source/sc_lib_formpq_partCylinder.h:29-90 */
+static double cyl_len_iso(const cs_prepared *P, double q, double zl) {
+    if ((P->length / P->radius) < 2) {
+        if (q < (5 * P->limq[2])) {
+            double qqn[101];
+            qqn[0] = 1.0;
+            for (int nser = 1; nser <= 100; nser++) qqn[nser] = qqn[nser - 1] * q * q;
+            double pql = 0.0, oldpqsum = -10.0;
+            for (int nser = 0; nser <= 100; nser++) {
+                double binsum = 0.0;
+                for (int mser = 0; mser <= 100; mser++) binsum += P->carr11pm[nser][mser] * qqn[mser];
+                pql += P->carrp[1][nser] * qqn[nser] * binsum;
+                const double delser = fabs((pql - oldpqsum) / pql);
+                if (delser < 0.0001) break;
+                oldpqsum = pql;
+            }
+            return pql;
+        }
+        return P->por / pow(q, 4);
+    }
+    if (q < (0.6 * P->limq[1])) return series_q(P->carrp[0], q, 120);
+    const double arglq = q * P->length / (zl + 1);
+    double pql = (M_PI / (2.0 * zl)) * (1 / arglq);
+    pql = pql - (1 / (2.0 * zl * (zl - 1) * arglq * arglq)) * cos((zl - 1) * atan(2.0 * arglq)) /
+                    pow(1.0 + 4 * arglq * arglq, (zl - 1) / 2.0);
+    return pql;
+}
+
+/* formpq_partCylinder, Source/sc_lib_formpq_partCylinder.h:8-393 (ordis 0/6/7, cs 0/1) */
 static double formpq_partCylinder(const cs_prepared *P, double qxs, double qys, double q) {
     double pqr = 0, pql = 0;
     const double zl = P->sigmal == 1.0 ? (double)EPS9 : (1 - sqr(P->sigmal)) / sqr(P->sigmal);
     const double zr = P->sigma == 1.0 ? (double)EPS9 : (1 - sqr(P->sigma)) / (sqr(P->sigma));
+    if (P->ordis == 7) pql = cyl_len_iso(P, q, zl);
     if (P->ordis == 6) {
         if (P->orcase == 4)
             pql = 1.0;
@@ -599,7 +675,38 @@ static double formpq_partCylinder(const cs_prepared *P, double qxs, double qys, 
         }
         return pql * pqr;
     }
+    if (P->cs == 1) return pql * cyl_cross_coreshell(P, q, zr);
     return 0.0;
+}
+
+/* formpq_partDisk, isotropic, homogeneous: Source/sc_lib_formpq_partDisk.h:17-36 (longitudinal)
+   and :313-339 (cross-section) */
+static double formpq_partDisk_iso(const cs_prepared *P, double q) {
+    const double zl = (1 - sqr(P->sigmal)) / sqr(P->sigmal);
+    const double zr = (1 - sqr(P->sigma)) / (sqr(P->sigma));
+    double pql, pqr;
+    if (q < (0.5 * P->limq[1])) {
+        pql = 1.0;
+        double oldpqsum = 0.0, qqnn = 1.0;
+        for (int nser = 1; nser <= 80; nser++) {
+            qqnn = qqnn * q * q;
+            pql += P->carrp[0][nser] * qqnn;
+            const double delser = fabs((pql - oldpqsum) / pql);
+            if (delser < 0.0001) break;
+            oldpqsum = pql;
+        }
+    } else {
+        const double arglq = q * P->length / (zl + 1);
+        pql = (2 / (zl * (zl - 1))) * pow(arglq, -2);
+    }
+    if (q < (0.5 * P->limq[4])) {
+        pqr = series_q(P->carrp[3], q, 100);
+    } else {
+        const double argpq = q * P->radius / (zr + 1);
+        pqr = (1 / (2.0 * zr * (zr - 1))) * pow(argpq, -2) *
+              (1 - cos((zr - 1) * atan(2.0 * argpq)) / pow(1.0 + 4 * argpq * argpq, (zr - 1) / 2.0));
+    }
+    return pql * pqr;
 }
 
 /* formfq_partCylinder, Source/sc_lib_formfq_partCylinder.h:8-216 (ordis 0/6, cs 0) */
@@ -797,6 +904,20 @@ double oracle_pixel_q(const cs_prepared *P, double qx, double qy, double qz) {
         }
         return P->base + P->izero * (pq + P->iso) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
     }
+    case CS_KEY_GENERIC:
+        /* calc_GENERIC, Source/sc_gpu_generic.h:27-881, for the combinations
+           restated here: isotropic cylinders (cs 0/1) and isotropic
+           homogeneous disks, without a lattice (szq = szqiso = 1) */
+        if (P->particle == 1 && P->ordis == 7) {
+            const double pq = formpq_partCylinder(P, qx, qy, q);
+            return P->base + P->izero * (pq + P->iso * 1.0) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
+        }
+        if (P->particle == 2 && P->ordis == 7) {
+            const double pq = formpq_partDisk_iso(P, q);
+            const double pqiso = (P->iso > 0) ? formpq_partDisk_iso(P, q) : (double)0.0;
+            return P->base + P->izero * (pq + P->iso * pqiso) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
+        }
+        return NAN;
     default:
         return NAN;
     }
@@ -811,6 +932,9 @@ int oracle_supported(const cs_prepared *P) {
     case CS_KEY_CYL_NONE_ZDIR:
     case CS_KEY_CYL_GAUSS_BCT_ZDIR:
     case CS_KEY_CUBE_NONE_ISO: return 1;
+    case CS_KEY_GENERIC:
+        return !P->lattice && P->ordis == 7 && ((P->particle == 1 && (P->cs == 0 || P->cs == 1)) ||
+                                                 (P->particle == 2 && P->cs == 0));
     default: return 0;
     }
 }

@@ -89,6 +89,7 @@ def image_cases():
     cases["disk_zdir_x_g32"] = dict(disk, phi=0.0, theta=90.0)
     cases["disk_zdir_y_g32"] = dict(disk, phi=90.0, theta=90.0)
     cases["disk_zdir_z_iso_g32"] = dict(disk, phi=0.0, theta=0.0, iso=0.3)
+    cases["disk_iso_g32"] = dict(disk, Ordis=7)
     ves = dict(C.scaled(C.SPHERE, 32), ComboBoxParticle=3, Length=14.0, SigmaL=0.15)
     cases["vesicle_iso_g32"] = dict(ves, iso=0.2)
     cases["vesicle_zdir_g32"] = dict(ves, Ordis=6)

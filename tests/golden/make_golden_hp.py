@@ -9,7 +9,7 @@ double) with "hp_cond": the value's largest relative change when q moves by
 (oracle.cpu_oracle.quad_condition). Where the reference's own FP64 value is
 ill-conditioned ("cond" > 1e-12), the GPU paths are compared with "hp",
 within their tolerance or 10 x "hp_cond" where the exact value itself moves
-more. Usage (after make_golden.py):
+more. Usage (after make_golden.py; --only a,b for selected cases):
 
     python tests/golden/make_golden_hp.py
 """
@@ -29,8 +29,11 @@ from oracle import cpu_oracle  # noqa: E402
 def main():
     with open(os.path.join(HERE, "cases.json")) as f:
         cases = json.load(f)
+    only = None
+    if "--only" in sys.argv:
+        only = set(sys.argv[sys.argv.index("--only") + 1].split(","))
     for name, c in sorted(cases["images"].items()):
-        if c.get("ign_new_switch"):
+        if c.get("ign_new_switch") or (only is not None and name not in only):
             continue
         P = cpu_oracle.prepare(c["params"], c["ign_cbs"])
         if not cpu_oracle.supported(P):
