@@ -194,6 +194,7 @@ def _sig(lib):
     lib.cs_mlp_set_layer.argtypes = [M, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.cs_upsample_bilinear.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_void_p, ctypes.c_void_p]
+    lib.cs_rphi_device.argtypes = [ctypes.c_void_p] + [ctypes.c_int] * 8 + [ctypes.c_void_p, ctypes.c_void_p]
     lib.cs_simplex_minimize.argtypes = [_OBJECTIVE, ctypes.c_void_p, P(CsFitParam), ctypes.c_int, ctypes.c_double,
                                         ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double, P(CsFitReport)]
     lib.cs_calc_batch.argtypes = [B, P(CsParams), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -728,4 +729,25 @@ def upsample_bilinear(x, factor, stream=None):
     rc = load_library().cs_upsample_bilinear(x.data_ptr(), n, s, int(factor), out.data_ptr(), ctypes.c_void_p(stream))
     if rc != CS_OK:
         raise CrystalScatterError(rc, "upsample failed")
+    return out
+
+
+CS_RPHI_SCALE, CS_RPHI_CLIP, CS_RPHI_CLIP40 = 1, 2, 4
+
+
+def rphi_device(img, x0, x1, y0, y1, xcenter, ycenter, s, scale=False, clip=False, clip40=False, stream=None):
+    """The r-phi image (s x s CUDA float64) of a CUDA image (rows y0..y1-1,
+    columns x0..x1-1) around the beam centre, cs_rphi_device; the GPU form of
+    ``postproc.rphi`` (SasCalc_PostProc::generateRphi)."""
+    import torch
+    img = img.contiguous().to(torch.float64)
+    if img.numel() != (y1 - y0) * (x1 - x0):
+        raise ValueError("image size does not match its coordinate ranges")
+    out = torch.empty((s, s), dtype=torch.float64, device=img.device)
+    flags = (CS_RPHI_SCALE if scale else 0) | (CS_RPHI_CLIP if clip else 0) | (CS_RPHI_CLIP40 if clip40 else 0)
+    rc = load_library().cs_rphi_device(img.data_ptr(), x0, x1, y0, y1, xcenter, ycenter, s, flags,
+                                       out.data_ptr(), _torch_stream(stream))
+    if rc != CS_OK:
+        raise CrystalScatterError(rc, "r-phi transform rejected its arguments" if rc == CS_ERR_PARAM
+                                  else "r-phi transform failed")
     return out

@@ -18,7 +18,7 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libcrystalscatter.so")
 
 HOST_SOURCES = ["cs_prep.cpp", "cs_params.cpp", "cs_capi.cpp", "cs_batch.cpp", "cs_simplex.cpp"]
-CUDA_SOURCES = ["cs_kernels.cu", "cs_mixed.cu", "cs_noalloc.cu", "cs_mlp.cu", "cs_peaks.cu"]
+CUDA_SOURCES = ["cs_kernels.cu", "cs_mixed.cu", "cs_noalloc.cu", "cs_mlp.cu", "cs_peaks.cu", "cs_postproc.cu"]
 # cs_fp64_unit.cu is compiled once per dispatch key (the FP64 drop-in kernels
 # of that key), so that the keys' kernels compile in parallel
 FP64_UNIT = "cs_fp64_unit.cu"
@@ -29,7 +29,7 @@ UNIT_KEYS = ["CS_KEY_SPHERE_NONE_ISO", "CS_KEY_SPHERE_GAUSS_FCC_GAUSS", "CS_KEY_
 # share its FP64 functions (pixel geometry, power series, math library calls),
 # which must round identically there; FP32 code asks for fmaf where it wants one
 FMAD = {"cs_kernels.cu": "false", "cs_mixed.cu": "false", "cs_noalloc.cu": "false", "cs_mlp.cu": "true",
-        "cs_peaks.cu": "true", FP64_UNIT: "false"}
+        "cs_peaks.cu": "true", "cs_postproc.cu": "false", FP64_UNIT: "false"}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

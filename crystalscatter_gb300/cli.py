@@ -40,6 +40,9 @@ def main(argv=None):
     ap.add_argument("--out", default="")
     ap.add_argument("--sweep", type=int, default=0,
                     help="instead of one image: the first N parameter sets of the cylinder/BCT sweep as one batch")
+    ap.add_argument("--schedule", default="",
+                    help="sweep: CHUNK,BLOCKS_PER_SM of the mixed persistent kernel (0,0 = block tiles at full "
+                         "occupancy) instead of the autotuner's choice")
     a = ap.parse_args(argv)
     if a.sweep:
         return sweep(a)
@@ -79,6 +82,9 @@ def sweep(a):
     t0 = time.perf_counter()
     b.prepare(C.bct_sweep(a.sweep), bIgnoreCbs=True)
     t_prep = time.perf_counter() - t0
+    if a.schedule:
+        chunk, bps = (int(v) for v in a.schedule.split(","))
+        b.set_schedule(chunk, bps)
     times = []
     for _ in range(max(1, a.repeat)):
         t0 = time.perf_counter()

@@ -365,6 +365,21 @@ int cs_mlp_set_layer(cs_mlp *m, int l, const float *w, const float *b);
    (pixel-centre aligned, clamped at the border), device pointers */
 int cs_upsample_bilinear(const float *d_in, int n, int s, int factor, float *d_out, void *stream);
 
+/* ---- r-phi transform of the training-data generator ------------------------
+   Replaces SasCalc_PostProc::generateRphi (Source/sc_postproc.cpp:53-334)
+   with the scaling options of scaleAndClipData (:764-823): the s x s polar
+   image (row = angle, column = radius) of a device image d_img (rows y0..y1-1,
+   columns x0..x1-1, FP64, row-major) around the beam centre (xcenter,
+   ycenter) in the same coordinates, into device d_out (s*s doubles; entries
+   no radius step writes are 0). Minimum coordinates must be at most 0
+   (CS_ERR_PARAM otherwise, and for s < 2 or an image without radius steps).
+   Returns after the stream has finished the transform. */
+#define CS_RPHI_SCALE 1  /* divide by the maximum (running maximum from 0) */
+#define CS_RPHI_CLIP 2   /* (log10(|v| / 1e-20) + 6) / 6, clamped at 0 */
+#define CS_RPHI_CLIP40 4 /* 1 - (1 - v) / 0.6, clamped at 0 */
+int cs_rphi_device(const double *d_img, int x0, int x1, int y0, int y1, int xcenter, int ycenter, int s, int flags,
+                   double *d_out, void *stream);
+
 /* Host-buffer forms: run the prepared batch (persistent schedule, a redo
    overflow handled internally) and copy all images into out; cs_calc_batch
    prepares first. */

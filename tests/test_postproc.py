@@ -82,3 +82,20 @@ def test_rphi_radial_image_is_angle_independent():
 def test_rphi_rejects_positive_minimum():
     with pytest.raises(ValueError):
         postproc.rphi(np.ones((4, 4)), 1, 5, 0, 4, 2, 2, 4)
+
+
+def test_rphi_matches_reference_golden():
+    """postproc.rphi against the reference's own outputs committed in
+    tests/golden/rphi.npz (made by tests/golden/make_rphi_golden.py)."""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_rphi_golden import CASES, image
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "rphi.npz"))
+    for k in range(len(CASES)):
+        ref = z[f"ref{k}"]
+        x0, x1, y0, y1, xc, yc, s, f = (int(v) for v in z[f"args{k}"])
+        got = postproc.rphi(image(x1 - x0, y1 - y0, 100 + k), x0, x1, y0, y1, xc, yc, s,
+                            scale=bool(f & 1), clip=bool(f & 2), clip40=bool(f & 4))
+        written = ~np.isnan(ref)
+        assert np.all(got[~written] == 0.0)
+        assert np.max(np.abs(got[written] - ref[written])) <= 1e-12 * np.max(np.abs(ref[written]))
