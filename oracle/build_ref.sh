@@ -1,6 +1,7 @@
 #!/bin/sh
 # Builds the reference's own FP64 CPU calculation path (test oracle only) into
-# oracle/_ref/libscref.so (and its r-phi transform into libscpost.so),
+# oracle/_ref/libscref.so (its r-phi transform into libscpost.so, its
+# downhill simplex into libscsimplex.so),
 # straight from the reference sources where they lie.
 # The reference tree is read-only and is not copied: g++ reads the two
 # translation units below in place. The .cu file is compiled as plain C++,
@@ -46,3 +47,12 @@ g++ $CXXFLAGS -c "$HERE/ref_postproc.cpp" -o "$OUT/ref_postproc.o" &
 wait
 g++ -shared -o "$OUT/libscpost.so" "$OUT/sc_postproc.o" "$OUT/ref_postproc.o"
 echo "built $OUT/libscpost.so"
+# the downhill simplex (Source/sc_simplexfit2d.cpp) with the stand-in
+# calculation class of ref_stubs/simplex_calc.h, forced in ahead of the unit
+SFLAGS="$CXXFLAGS -DCONSOLENPROG"
+g++ $SFLAGS -include "$HERE/ref_stubs/simplex_calc.h" -c -x c++ "$REF/Source/sc_simplexfit2d.cpp" \
+    -o "$OUT/sc_simplexfit2d.o" &
+g++ $SFLAGS -c "$HERE/ref_simplex.cpp" -o "$OUT/ref_simplex.o" &
+wait
+g++ -shared -o "$OUT/libscsimplex.so" "$OUT/sc_simplexfit2d.o" "$OUT/ref_simplex.o"
+echo "built $OUT/libscsimplex.so"
