@@ -343,6 +343,17 @@ def config_row(cs, torch, name, flush, steps, cpu_seconds):
         row[mname + "_ms_per_image"] = 1e3 * tk / k
     row["speedup_mixed_over_fp64"] = row["mixed_pixels_per_s"] / row["fp64_pixels_per_s"]
     c.cleanup()
+    # main kernel vs FP64 redo: the same set as a one-set batch (persistent
+    # kernels), CUDA events around each (cs_batch_profile)
+    b = cs.SasCalcBatch()
+    b.prepare([C.WORKLOADS[name]])
+    total = b.info()[0]
+    db = torch.empty(total, dtype=torch.float64, device="cuda")
+    prof = [b.profile(db.data_ptr(), total) for _ in range(3)]
+    m_ms, r_ms = min(p[0] for p in prof), min(p[1] for p in prof)
+    row["split_one_set_batch_ms"] = {"main": m_ms, "redo": r_ms, "redo_share": r_ms / (m_ms + r_ms),
+                                     "redo_pixels": b.redo_pixels()[0], "schedule": b.schedule(0)}
+    b.cleanup()
     # the CPU oracle on the reference's own prepared constants
     blk = R.load(name)
     nt = cpu_threads()

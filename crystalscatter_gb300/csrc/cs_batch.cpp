@@ -17,10 +17,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <map>
@@ -65,7 +67,7 @@ struct cs_batch {
     bool any_twin = false;
 
     // arenas
-    float *d_pk = nullptr;  // aq, amf, iq, imf of all sets
+    float *d_pk = nullptr;  // aq, awl, iq, imf of all sets
     size_t pk_cap = 0;
     float4 *d_av = nullptr;
     size_t av_cap = 0;
@@ -73,6 +75,9 @@ struct cs_batch {
     size_t ai_cap = 0;
     cs_delta_node *d_delta = nullptr;  // one table per set that needs one
     size_t delta_cap = 0;
+    std::vector<cs::QTable> qtabs;  // pixel geometry tables, filled at every persistent run
+    double *d_qtab = nullptr;
+    size_t qtab_cap = 0;
     const cs_chi_node *d_chi = nullptr;
     cs_chi_node *d_chi_own = nullptr;
     double chi_b = -1;
@@ -219,6 +224,37 @@ int ensure_redo(cs_batch *b) {
 // prefix of the group's pixels (1/32 of them, at least 8 tiles per resident
 // block) with the main kernel alone, timed with CUDA events; the fastest per
 // pixel wins and is cached per (device, key) for the process.
+// Half-width of the square pixel region a set needs from a shared geometry
+// table, or -1 when its q vectors cannot come from one: only the z-direction
+// cylinder keys (whose mixed kernels take the drop-in's geometry too, so a
+// batch still equals single-set calls bit for bit), in beam geometry with
+// pixno = 2 zmax, where convert_idx2q's detector position of pixel (ihex, i)
+// is exactly (ihex, i) whatever the detector size.
+int qtable_half(const cs_prepared &P) {
+    if (P.key != CS_KEY_CYL_NONE_ZDIR && P.key != CS_KEY_CYL_GAUSS_BCT_ZDIR) return -1;
+    if (P.use1d || !P.usebeamstop) return -1;
+    if (P.pixnox != 2.0 * P.zmax || P.pixnoy != 2.0 * P.zmax) return -1;
+    const int h = std::max(std::max(std::abs(P.zzmin), std::abs(P.zzmax - 1)),
+                           std::max(std::abs(P.iimin), std::abs(P.iimax - 1)));
+    return h <= (1 << 14) ? h : -1;
+}
+
+// the detector geometry that decides a table's values, bit for bit
+std::array<uint64_t, 6> qtable_geometry(const cs_prepared &P) {
+    std::array<uint64_t, 6> g;
+    const double v[6] = {P.pixx_m, P.pixy_m, P.beamx0, P.beamy0, P.det, P.wave};
+    std::memcpy(g.data(), v, sizeof(v));
+    return g;
+}
+
+int enqueue_qtables(cs_batch *b, cudaStream_t s) {
+    for (const cs::QTable &t : b->qtabs) {
+        const int rc = cs::launch_qtable(t, s);
+        if (rc) return cuda_fail(b, cs::last_launch_error(), "geometry table launch");
+    }
+    return CS_OK;
+}
+
 std::mutex g_tune_mutex;
 std::map<std::pair<int, int>, cs_batch::Sched> g_tune_cache;
 
@@ -240,7 +276,7 @@ int tune_group(cs_batch *b, size_t gi, double *d_out, cudaStream_t s, cs_batch::
         if (e0) cudaEventDestroy(e0);
         return cuda_fail(b, e, "cudaEventCreate");
     }
-    int rc = CS_OK;
+    int rc = enqueue_qtables(b, s);
     double best = 1e300;
     for (size_t c = 0; c <= cand.size() && rc == CS_OK; c++) {
         // entry 0 runs twice: the first pass warms up (clocks, caches) untimed
@@ -322,6 +358,7 @@ int enqueue(cs_batch *b, double *d_out, cudaStream_t s, int mode, int schedule, 
         if (mode == CS_MODE_MIXED && b->any_twin) return fail(b, CS_ERR_UNSUPPORTED, "no mixed-precision kernel for twinned lattices");
         if ((e = cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned long long) * b->groups.size(), s)) != cudaSuccess)
             return cuda_fail(b, e, "cudaMemsetAsync(tile counters)");
+        if (int rc = enqueue_qtables(b, s)) return rc;
         if (mode == CS_MODE_MIXED) {
             int rc = ensure_redo(b);
             if (rc) return rc;
@@ -416,6 +453,7 @@ void cs_batch_destroy(cs_batch *b) {
     cudaFree(b->d_av);
     cudaFree(b->d_ai);
     cudaFree(b->d_delta);
+    cudaFree(b->d_qtab);
     cudaFree(b->d_chi_own);
     cudaFree(b->d_counters);
     cudaFree(b->redo.d_count);
@@ -558,7 +596,7 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
     size_t nf = 0, nv = 0, nd = 0;
     for (int k = 0; k < nsets; k++) {
         const auto &H = b->hpeaks[k];
-        nf += H.aq.size() + H.amf.size() + H.iq.size() + H.imf.size();
+        nf += H.aq.size() + H.awl.size() + H.iq.size() + H.imf.size();
         nv += H.av.size();
         if (cs::needs_delta_table(b->hprep[k])) nd++;
     }
@@ -600,7 +638,7 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
             };
             S.peaks.n_aniso = (int)H.aq.size();
             S.peaks.aq = put(H.aq);
-            S.peaks.amf = put(H.amf);
+            S.peaks.awl = put(H.awl);
             S.peaks.av = b->d_av + av.size();
             S.peaks.aidx = b->d_ai + ai.size();
             av.insert(av.end(), H.av.begin(), H.av.end());
@@ -608,6 +646,7 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
             S.peaks.n_iso = (int)H.iq.size();
             S.peaks.iq = put(H.iq);
             S.peaks.imf = put(H.imf);
+            cs::peak_constants(P, S.peaks);
         }
         S.out_offset = (long)b->offset[k];
         S.npix = region_pixels(P);
@@ -623,6 +662,46 @@ int cs_batch_prepare(cs_batch *b, const cs_params *sets, int nsets, int ign_new_
         S.tile_begin = g.tiles;
         g.tiles += (S.npix + CS_BATCH_TILE - 1) / CS_BATCH_TILE;
         g.set_end = j + 1;
+    }
+    // shared pixel geometry tables: one per detector geometry among the sets
+    // that can use one, as wide as its widest set
+    {
+        std::map<std::array<uint64_t, 6>, size_t> by_geom;
+        b->qtabs.clear();
+        for (int j = 0; j < nsets; j++) {
+            const cs_prepared &P = b->hprep[b->order[j]];
+            const int h = qtable_half(P);
+            if (h < 0) continue;
+            auto it = by_geom.find(qtable_geometry(P));
+            if (it == by_geom.end()) {
+                it = by_geom.emplace(qtable_geometry(P), b->qtabs.size()).first;
+                b->qtabs.push_back(cs::QTable{});
+            }
+            cs::QTable &t = b->qtabs[it->second];
+            if (h > t.half || t.prep == nullptr) {
+                t.half = std::max(h, t.half);
+                t.prep = b->dprep + b->order[j];
+            }
+        }
+        size_t need = 0;
+        for (const cs::QTable &t : b->qtabs) need += 3 * (size_t)(2 * t.half + 1) * (size_t)(2 * t.half + 1);
+        if (need && (rc = grow(b, b->d_qtab, b->qtab_cap, need, "cudaMalloc(geometry tables)"))) return rc;
+        size_t off = 0;
+        for (cs::QTable &t : b->qtabs) {
+            t.d = b->d_qtab + off;
+            off += 3 * (size_t)(2 * t.half + 1) * (size_t)(2 * t.half + 1);
+        }
+        for (int j = 0; j < nsets; j++) {
+            cs::BatchSetDev &S = b->hsets[j];
+            S.qtab = nullptr;
+            S.qhalf = S.qw = 0;
+            const cs_prepared &P = b->hprep[b->order[j]];
+            if (qtable_half(P) < 0) continue;
+            const cs::QTable &t = b->qtabs[by_geom.at(qtable_geometry(P))];
+            S.qtab = t.d;
+            S.qhalf = t.half;
+            S.qw = 2 * t.half + 1;
+        }
     }
     if ((rc = grow(b, b->dsets, b->dsets_cap, (size_t)nsets, "cudaMalloc(set table)"))) return rc;
     if ((rc = grow(b, b->d_counters, b->counters_cap, std::max<size_t>(b->groups.size(), 1), "cudaMalloc(tile counters)")))

@@ -91,6 +91,19 @@ __device__ __forceinline__ bool batch_next_chunk(const BatchSetDev *__restrict__
     return true;
 }
 
+// q of pixel (ihex, i) from the set's shared geometry table; false when the
+// set has none (the caller computes q itself).
+__device__ __forceinline__ bool batch_q_from_table(const BatchSetDev &S, int ihex, int i, double &qx, double &qy,
+                                                   double &qz) {
+    if (!S.qtab) return false;
+    const long n = (long)S.qw * S.qw;
+    const long j = (long)(i + S.qhalf) * S.qw + (ihex + S.qhalf);
+    qx = __ldg(S.qtab + j);
+    qy = __ldg(S.qtab + j + n);
+    qz = __ldg(S.qtab + j + 2 * n);
+    return true;
+}
+
 }  // namespace cs
 
 #endif

@@ -46,7 +46,26 @@ struct BatchSetDev {
     long npix;                   // calculated pixels (zzmax-zzmin)*(iimax-iimin)
     int nx;                      // zzmax - zzmin
     int key;                     // dispatch key
+    // Pixel geometry table shared by the sets of one detector geometry, or
+    // null: q of pixel (ihex, i) at qtab[j], qtab[j + qn], qtab[j + 2 qn]
+    // (x, y, z), j = (i + qhalf) qw + (ihex + qhalf), qn = qw * qw.
+    const double *qtab;
+    int qhalf, qw;
 };
+
+// One pixel geometry table: the q vectors of every pixel of a square
+// [-half, half]^2 detector region, computed with the drop-in's convert_idx2q
+// from the prepared block of its largest set (prep). Sets whose pixel
+// coordinates map to the same detector positions (mdet = ihex and ndet = i
+// exactly: pixno = 2 zmax) and share pixel size, beam centre, distance and
+// wavelength get bit for bit the q vectors they would compute themselves.
+struct QTable {
+    const cs_prepared *prep = nullptr;
+    int half = 0;
+    double *d = nullptr;
+};
+// Fills a table on stream s.
+int launch_qtable(const QTable &t, cudaStream_t s);
 
 // Sets [set_begin, set_end) of the device array share one key and own tiles
 // [0, tiles) of the group.

@@ -50,7 +50,7 @@ struct cs_handle {
     // mixed-precision path: compact peak tables and the FP64 redo list
     bool peaks_valid = false;
     cs::HostPeaks hpeaks;
-    float *d_aq = nullptr, *d_amf = nullptr, *d_iq = nullptr, *d_imf = nullptr;
+    float *d_aq = nullptr, *d_awl = nullptr, *d_iq = nullptr, *d_imf = nullptr;
     float4 *d_av = nullptr;
     int *d_aidx = nullptr;
     size_t peak_cap = 0;
@@ -212,14 +212,14 @@ int ensure_mixed(cs_handle *h) {
         const size_t n = std::max(h->hpeaks.aq.size(), h->hpeaks.iq.size()) + 1;
         if (n > h->peak_cap) {
             cudaFree(h->d_aq);
-            cudaFree(h->d_amf);
+            cudaFree(h->d_awl);
             cudaFree(h->d_iq);
             cudaFree(h->d_imf);
             cudaFree(h->d_av);
             cudaFree(h->d_aidx);
             if ((e = cudaMalloc(&h->d_aidx, sizeof(int) * n)) != cudaSuccess ||
                 (e = cudaMalloc(&h->d_aq, sizeof(float) * n)) != cudaSuccess ||
-                (e = cudaMalloc(&h->d_amf, sizeof(float) * n)) != cudaSuccess ||
+                (e = cudaMalloc(&h->d_awl, sizeof(float) * n)) != cudaSuccess ||
                 (e = cudaMalloc(&h->d_iq, sizeof(float) * n)) != cudaSuccess ||
                 (e = cudaMalloc(&h->d_imf, sizeof(float) * n)) != cudaSuccess ||
                 (e = cudaMalloc(&h->d_av, sizeof(float4) * 2 * n)) != cudaSuccess)
@@ -230,7 +230,7 @@ int ensure_mixed(cs_handle *h) {
         // synchronous copies: the host vectors are rebuilt on the next preparation
         if (!H.aq.empty()) {
             cudaMemcpy(h->d_aq, H.aq.data(), sizeof(float) * H.aq.size(), cudaMemcpyHostToDevice);
-            cudaMemcpy(h->d_amf, H.amf.data(), sizeof(float) * H.amf.size(), cudaMemcpyHostToDevice);
+            cudaMemcpy(h->d_awl, H.awl.data(), sizeof(float) * H.awl.size(), cudaMemcpyHostToDevice);
             cudaMemcpy(h->d_av, H.av.data(), sizeof(float4) * H.av.size(), cudaMemcpyHostToDevice);
             cudaMemcpy(h->d_aidx, H.aidx.data(), sizeof(int) * H.aidx.size(), cudaMemcpyHostToDevice);
         }
@@ -271,7 +271,7 @@ int run_image(cs_handle *h, double *d_out, cudaStream_t s, int mode) {
             T.n_aniso = (int)h->hpeaks.aq.size();
             T.aq = h->d_aq;
             T.av = h->d_av;
-            T.amf = h->d_amf;
+            T.awl = h->d_awl;
             T.aidx = h->d_aidx;
             T.n_iso = (int)h->hpeaks.iq.size();
             T.iq = h->d_iq;
@@ -326,7 +326,7 @@ void cs_destroy(cs_handle *h) {
     if (h->hprep) cudaFreeHost(h->hprep);
     if (h->hdelta) cudaFreeHost(h->hdelta);
     cudaFree(h->d_aq);
-    cudaFree(h->d_amf);
+    cudaFree(h->d_awl);
     cudaFree(h->d_iq);
     cudaFree(h->d_imf);
     cudaFree(h->d_av);
@@ -478,7 +478,7 @@ int cs_launch_prepared_mixed_noalloc(cs_handle *h, double *d_out, size_t n_doubl
             T.n_aniso = (int)h->hpeaks.aq.size();
             T.aq = h->d_aq;
             T.av = h->d_av;
-            T.amf = h->d_amf;
+            T.awl = h->d_awl;
             T.aidx = h->d_aidx;
             T.n_iso = (int)h->hpeaks.iq.size();
             T.iq = h->d_iq;

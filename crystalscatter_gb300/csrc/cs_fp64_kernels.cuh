@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(CS_BATCH_TILE) k_batch_fp64(const cs::BatchSet
         const int ihex = P.zzmin + (int)(t % S.nx);
         const int i = P.iimin + (int)(t / S.nx);
         double qx, qy, qz;
-        convert_idx2q(P, ihex, i, qx, qy, qz);
+        if (!cs::batch_q_from_table(S, ihex, i, qx, qy, qz)) convert_idx2q(P, ihex, i, qx, qy, qz);
         const double v = calc_pixel<KEY>(C, qx, qy, qz);
         out[S.out_offset + (long)(ihex - P.xmin) + (long)(P.xmax - P.xmin) * (long)(i - P.ymin)] = v;
     }
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(128) k_batch_redo(const cs::BatchSetDev *__res
         const int ihex = P.zzmin + (int)(t % S.nx);
         const int i = P.iimin + (int)(t / S.nx);
         double qx, qy, qz;
-        convert_idx2q(P, ihex, i, qx, qy, qz);
+        if (!cs::batch_q_from_table(S, ihex, i, qx, qy, qz)) convert_idx2q(P, ihex, i, qx, qy, qz);
         out[S.out_offset + (long)(ihex - P.xmin) + (long)(P.xmax - P.xmin) * (long)(i - P.ymin)] =
             calc_pixel<KEY>(C, qx, qy, qz);
     }

@@ -39,7 +39,7 @@ using cs64::Ctx;
 // closed forms / quadratures (a few FP32 roundings).
 #define EPS_SERIES 1.0e-14
 #define EPS_PQ 3.0e-7
-#define EPS_PEAK 1.0e-7  // peak sums beyond their own estimate (Kahan, table rounding)
+#define EPS_PEAK 1.0e-9  // peak sums beyond their own estimate (pair sums, table rounding)
 
 // decision guard: true when v is within `band` relative of threshold t
 __device__ __forceinline__ bool near(double v, double t, double band) { return fabs(v - t) <= band * fabs(t); }
@@ -315,18 +315,6 @@ __device__ float cyl_len_factor_e(double a_d, double z_d, float &rel) {
     rel = ((g + fabsf(C) * ep) / P) / fabsf(br) + 3e-7f;
     return (a1 / (a * a)) * br;
 }
-
-// ------------------------------------------------------ compensated addition
-struct Kahan {
-    float s = 0.0f, c = 0.0f;
-    __device__ __forceinline__ void add(float v) {
-        const float y = v - c;
-        const float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
 
 // ------------------------------------------------------- FP32 Romberg (chi)
 struct ChiArgsF {
@@ -672,8 +660,80 @@ __device__ __forceinline__ void scaled_square(float kh, float kl, float dh, floa
     xl = fmaf(kh, p, -xh) + fmaf(kh, pe, kl * p);
 }
 
-// exp2(-(xh + xl)): exp2f of the high part, first-order factor for the low one
-__device__ __forceinline__ float exp2_pair(float xh, float xl) { return exp2f(-xh) * fmaf(-xl, 0.6931472f, 1.0f); }
+// 2^(-j/64), j = 0..63, each the float pair (hi, lo) of its double value:
+// the table of Tang's table-driven exponential (ACM TOMS 15, 1989)
+__device__ const float2 kExp2m64[64] = {
+    {0x1.0000000000000p+0f, 0x0.0p+0f}, {0x1.fa7c180000000p-1f, 0x1.9e90d80000000p-29f},
+    {0x1.f507660000000p-1f, -0x1.246eb00000000p-27f}, {0x1.efa1be0000000p-1f, 0x1.cc2b440000000p-26f},
+    {0x1.ea4afa0000000p-1f, 0x1.52486c0000000p-28f}, {0x1.e502ee0000000p-1f, 0x1.e2cffe0000000p-27f},
+    {0x1.dfc9740000000p-1f, -0x1.908c940000000p-26f}, {0x1.da9e600000000p-1f, 0x1.ed99420000000p-28f},
+    {0x1.d5818e0000000p-1f, -0x1.822dbc0000000p-28f}, {0x1.d072d40000000p-1f, 0x1.40f1300000000p-26f},
+    {0x1.cb720e0000000p-1f, -0x1.8837cc0000000p-28f}, {0x1.c67f120000000p-1f, 0x1.cafa2a0000000p-26f},
+    {0x1.c199be0000000p-1f, -0x1.3d56b20000000p-28f}, {0x1.bcc1ea0000000p-1f, -0x1.f687c60000000p-26f},
+    {0x1.b7f7700000000p-1f, -0x1.a094380000000p-26f}, {0x1.b33a2c0000000p-1f, -0x1.ec3a820000000p-27f},
+    {0x1.ae89fa0000000p-1f, -0x1.a94b140000000p-27f}, {0x1.a9e6b60000000p-1f, -0x1.50c0480000000p-26f},
+    {0x1.a5503c0000000p-1f, -0x1.b83b540000000p-26f}, {0x1.a0c6680000000p-1f, -0x1.2886a60000000p-27f},
+    {0x1.9c49180000000p-1f, 0x1.51f8480000000p-28f}, {0x1.97d82a0000000p-1f, -0x1.0d8d800000000p-32f},
+    {0x1.93737c0000000p-1f, -0x1.e647440000000p-26f}, {0x1.8f1aea0000000p-1f, -0x1.baa2320000000p-27f},
+    {0x1.8ace540000000p-1f, 0x1.15506e0000000p-28f}, {0x1.868d9a0000000p-1f, -0x1.2edb440000000p-27f},
+    {0x1.82589a0000000p-1f, -0x1.accc7c0000000p-27f}, {0x1.7e2f340000000p-1f, -0x1.2616340000000p-26f},
+    {0x1.7a11480000000p-1f, -0x1.829fd00000000p-26f}, {0x1.75feb60000000p-1f, -0x1.37b3060000000p-26f},
+    {0x1.71f75e0000000p-1f, 0x1.1d8bee0000000p-26f}, {0x1.6dfb240000000p-1f, -0x1.cd72e80000000p-28f},
+    {0x1.6a09e60000000p-1f, 0x1.9fcef40000000p-27f}, {0x1.6623880000000p-1f, 0x1.2a91120000000p-28f},
+    {0x1.6247ec0000000p-1f, -0x1.f8b5500000000p-26f}, {0x1.5e76f20000000p-1f, -0x1.4a5bd80000000p-26f},
+    {0x1.5ab07e0000000p-1f, -0x1.5bd5ec0000000p-28f}, {0x1.56f4740000000p-1f, -0x1.295b040000000p-26f},
+    {0x1.5342b60000000p-1f, -0x1.2c56100000000p-26f}, {0x1.4f9b280000000p-1f, -0x1.2c5a6c0000000p-26f},
+    {0x1.4bfdae0000000p-1f, -0x1.593abc0000000p-26f}, {0x1.486a2c0000000p-1f, -0x1.47d8660000000p-26f},
+    {0x1.44e0860000000p-1f, 0x1.8624b40000000p-31f}, {0x1.4160a20000000p-1f, 0x1.f72e2a0000000p-29f},
+    {0x1.3dea640000000p-1f, 0x1.8246840000000p-26f}, {0x1.3a7db40000000p-1f, -0x1.634c020000000p-26f},
+    {0x1.371a740000000p-1f, -0x1.18aac60000000p-26f}, {0x1.33c08c0000000p-1f, -0x1.b37d200000000p-26f},
+    {0x1.306fe00000000p-1f, 0x1.4636e20000000p-26f}, {0x1.2d285a0000000p-1f, 0x1.b900c20000000p-27f},
+    {0x1.29e9e00000000p-1f, -0x1.5c04240000000p-26f}, {0x1.26b4560000000p-1f, 0x1.789f380000000p-27f},
+    {0x1.2387a60000000p-1f, 0x1.ceac480000000p-26f}, {0x1.2063b80000000p-1f, 0x1.0c519a0000000p-26f},
+    {0x1.1d48740000000p-1f, -0x1.d2e8ca0000000p-26f}, {0x1.1a35be0000000p-1f, 0x1.6df96e0000000p-26f},
+    {0x1.172b840000000p-1f, -0x1.c157420000000p-28f}, {0x1.1429aa0000000p-1f, 0x1.d525bc0000000p-26f},
+    {0x1.11301e0000000p-1f, -0x1.fdb4960000000p-26f}, {0x1.0e3ec40000000p-1f, -0x1.a585cc0000000p-26f},
+    {0x1.0b55860000000p-1f, 0x1.9f31220000000p-26f}, {0x1.0874520000000p-1f, -0x1.e2990e0000000p-27f},
+    {0x1.059b0e0000000p-1f, -0x1.9d4f520000000p-26f}, {0x1.02c9a40000000p-1f, -0x1.887fa00000000p-29f}};
+
+// s + e = a + b exactly, for |a| >= |b| (or a = 0)
+__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    e = b - (s - a);
+}
+
+// 2^-(xh + xl) as a float pair (eh + el), 0 <= xh < 2^14 (xl a low part):
+// xh = k/64 + r with r exact (both sides are multiples of xh's ulp, |r| <= 1/128),
+// 2^-(k/64) from the table scaled by 2^-(k>>6), and 2^-(r + xl) = 1 + p with
+// p = expm1(-(r + xl) ln 2), |p| < 0.0055, from its Taylor series through the
+// fifth power (remainder < 4e-17). p is formed in FP32, so its own error is
+// ~1e-7 of p, i.e. ~7e-10 of the result; with the other roundings the pair is
+// within 2e-9 (relative) of 2^-(xh + xl).
+__device__ __forceinline__ void exp2m_pair(float xh, float xl, float &eh, float &el) {
+    const float k = rintf(xh * 64.0f);
+    const float r = fmaf(k, -0.015625f, xh) + xl;
+    const int ki = (int)k;
+    const float2 t = __ldg(&kExp2m64[ki & 63]);
+    const float a = -r * 0.693147182f;
+    const float p = a * fmaf(a, fmaf(a, fmaf(a, fmaf(a, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f), 0.5f), 1.0f);
+    float sh, se;
+    fast_two_sum(t.x, fmaf(t.x, p, t.y), sh, se);
+    eh = ldexpf(sh, -(ki >> 6));
+    el = ldexpf(se, -(ki >> 6));
+}
+
+// float-pair accumulator (sum of float pairs, error ~1e-13 of the sum of
+// magnitudes)
+struct SumFF {
+    float h = 0.0f, l = 0.0f;
+    __device__ __forceinline__ void add(float bh, float bl) {
+        float s, e;
+        two_sum(h, bh, s, e);
+        e += l + bl;
+        fast_two_sum(s, e, h, l);
+    }
+    __device__ __forceinline__ double value() const { return (double)h + (double)l; }
+};
 
 // yphi = acos(1 - s) = 2 asin(sqrt(s/2)) and yphi^2 = 2 s (1 + r(s)) with
 // r(s) = sum_{n>=2} 2^n s^(n-1) / (n^2 C(2n, n)) (the series of asin^2); through
@@ -689,28 +749,37 @@ __device__ __forceinline__ float asin2_rest(float s) {
     return r * s;
 }
 
-// Error estimates of the sums: a term carries exp2f's error and the rounding
-// of its factors (c0), and the error of its angular argument (ephi); the
-// radial argument k (q - q_hkl)^2 is a float pair, exact to ~1e-12 of its
-// size. The sums' relative errors are the term-weighted means (eps_rad,
+// Error estimates of the sums: the terms are float pairs (exp2m_pair times the
+// reflection's factor as a float pair) summed as float pairs; a term carries
+// the pair exponential's error (c0) and the error of its angular argument
+// (ephi); the radial argument k (q - q_hkl)^2 is a float pair, exact to ~1e-12
+// of its size. The sums' relative errors are the term-weighted means (eps_rad,
 // eps_int).
 __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, double qy, double qz, double q,
                             double &radint, double &intens, double &eps_rad, double &eps_int, bool &guard) {
-    const float c0 = 3e-7f;
-    double width = 1;
-    if (P.debyescherrer) width = 4.0 / P.domainsize;
-    if (P.para) width = (4.0 / P.domainsize) + cs64::sqr(P.reldis) * P.dist * cs64::sqr(q);
-    width *= P.width_zuf;
-    const double widthiso = 1.0 / P.uca;
+    const float c0 = 3e-9f;
+    // per-set factors from the table (the anisotropic width depends on q when
+    // para is set: then it and its factors are formed here)
+    double kd_an = T.kd_an, inv_an = T.inv_an;
+    float dmax_an = T.dmax_an;
+    if (P.para) {
+        double width = 1;
+        if (P.debyescherrer) width = 4.0 / P.domainsize;
+        if (P.para) width = (4.0 / P.domainsize) + cs64::sqr(P.reldis) * P.dist * cs64::sqr(q);
+        width *= P.width_zuf;
+        kd_an = 4.0 / M_PI / (width * width) * 1.4426950408889634;
+        inv_an = 1.0 / (M_PI * width / 2.0);
+        dmax_an = (float)(9.4 * width);
+    }
     const float qf = (float)q;
     const float ql = (float)(q - (double)qf);
     // isotropic peaks: exp(-4 x2/pi) / (pi widthiso/2), x2 = (q-qhkl)^2/widthiso^2
     {
-        const double kd = 4.0 / M_PI / (widthiso * widthiso) * 1.4426950408889634;
+        const double kd = T.kd_iso;
         const float kh = (float)kd, kl = (float)(kd - (double)kh);
-        const float dmax = (float)(9.4 * widthiso);
+        const float dmax = T.dmax_iso;
         int i = lower_bound_f(T.iq, T.n_iso, qf - dmax);
-        Kahan s;
+        SumFF s;
         float w = 0.0f;
         for (; i < T.n_iso; i++) {
             const float qh = __ldg(T.iq + i);
@@ -718,22 +787,25 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
             two_sum(qf, -qh, dh, de);
             const float dl = de + ql;
             if (dh + dl < -dmax) break;
-            float xh, xl;
+            float xh, xl, eh, el;
             scaled_square(kh, kl, dh, dl, xh, xl);
-            const float t = exp2_pair(xh, xl) * __ldg(T.imf + i);
-            s.add(t);
-            w = fmaf(fabsf(t), c0, w);
+            exp2m_pair(xh, xl, eh, el);
+            const float m = __ldg(T.imf + i);  // an integer, exact
+            const float th = eh * m;
+            s.add(th, fmaf(eh, m, -th) + el * m);
+            w = fmaf(fabsf(th), c0, w);
         }
-        const double sum = s.value();
-        radint = sum / (M_PI * widthiso / 2.0);
-        eps_rad = sum != 0.0 ? (double)w / fabs(sum) : 0.0;
+        // the normalisation is a product (the pair sum is far more accurate
+        // than the bound needs) and the estimate's quotient FP32
+        radint = s.value() * T.inv_iso;
+        eps_rad = s.h != 0.0f ? (double)(w / fabsf(s.h)) : 0.0;
     }
     // anisotropic peaks
     {
-        const double kd = 4.0 / M_PI / (width * width) * 1.4426950408889634;
+        const double kd = kd_an;
         const float kh = (float)kd, kl = (float)(kd - (double)kh);
-        const float dmax = (float)(9.4 * width);
-        const double kphid = 4 * q * q / (M_PI * cs64::sqr(P.phiwidth)) * 1.4426950408889634;
+        const float dmax = dmax_an;
+        const double kphid = q * q * T.kphi;
         const float kph = (float)kphid, kpl = (float)(kphid - (double)kph);
         // unit q as a float pair; eps = 1 - |q|/q of the reference's cosine
         // (its q carries CS_EPS9)
@@ -741,9 +813,9 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
         const double uxd = qx * rn, uyd = qy * rn, uzd = qz * rn;
         const float fx = (float)uxd, fy = (float)uyd, fz = (float)uzd;
         const float lx = (float)(uxd - fx), ly = (float)(uyd - fy), lz = (float)(uzd - fz);
-        const float epsq = (float)(CS_EPS9 / q);
+        const float epsq = (float)CS_EPS9 / qf;
         int i = lower_bound_f(T.aq, T.n_aniso, qf - dmax);
-        Kahan s;
+        SumFF s;
         float w = 0.0f;
         for (; i < T.n_aniso; i++) {
             const float qh = __ldg(T.aq + i);
@@ -808,16 +880,18 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
                 xph = kph * yphi * yphi;
                 ephi = 2.1e-7f * kph * yphi / sqrtf(fmaxf(1.0f - c * c, 1e-10f));
             }
-            float xh, xl, sx, ex;
+            float xh, xl, sx, ex, eh, el;
             scaled_square(kh, kl, dh, dl, xh, xl);
             two_sum(xh, xph, sx, ex);
-            const float t = exp2_pair(sx, ex + xl + xpl) * v.w;
-            s.add(t);
-            w = fmaf(fabsf(t), c0 + ephi, w);
+            exp2m_pair(sx, ex + xl + xpl, eh, el);
+            // times mult g3/peaknorm1 as a float pair (v.w + awl)
+            const float wl = __ldg(T.awl + i);
+            const float th = eh * v.w;
+            s.add(th, fmaf(eh, v.w, -th) + fmaf(eh, wl, el * v.w));
+            w = fmaf(fabsf(th), c0 + ephi, w);
         }
-        const double sum = s.value();
-        intens = sum / (M_PI * width / 2.0);
-        eps_int = sum != 0.0 ? (double)w / fabs(sum) : 0.0;
+        intens = s.value() * inv_an;
+        eps_int = s.h != 0.0f ? (double)(w / fabsf(s.h)) : 0.0;
         if (!isfinite(intens)) guard = true;  // the reference stops at an infinite sum
     }
 }
@@ -1161,7 +1235,10 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
         return P.base + P.izero * (pq + P.iso) + tailv;
     }
     if (KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR) {
-        // form factors of the orientation case (first pass: FP32 closed forms)
+        // form factors of the orientation case, closed forms in FP64: the
+        // structure factor's cancellation (lattice_combine) amplifies their
+        // error, and an FP32 first pass with an FP64 second pass where the
+        // bound fails costs more (the warp runs both when one lane fails)
         auto forms = [&](auto f64tag, double &pq, double &fq) {
             constexpr bool F = decltype(f64tag)::value;
             switch (P.orcase) {
@@ -1185,22 +1262,11 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
             }
         };
         double pq = 0, fq = 0;
-        forms(std::false_type{}, pq, fq);
+        forms(std::true_type{}, pq, fq);
         double radint, intens, erad, eint;
         peak_sums_f(P, T, qx, qy, qz, q, radint, intens, erad, eint, guard);
         // the reference's BCT function multiplies szqiso by 1 instead of pq
-        bool g2 = false;
-        double v = lattice_combine(P, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, g2);
-        if (g2 && (ep > 1e-12 || ef > 1e-12)) {
-            // the structure factor amplifies the FP32 closed forms' error
-            // beyond the bound: second pass with their FP64 forms (the series
-            // branches are FP64 already and give the same values again)
-            forms(std::true_type{}, pq, fq);
-            g2 = false;
-            v = lattice_combine(P, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, g2);
-        }
-        guard = guard || g2;
-        return v;
+        return lattice_combine(P, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, guard);
     }
     guard = true;
     return 0.0;
@@ -1260,7 +1326,7 @@ __device__ __forceinline__ void batch_mixed_pixel(const cs::BatchSetDev *__restr
     const int ihex = P.zzmin + (int)(t % S.nx);
     const int i = P.iimin + (int)(t / S.nx);
     double qx, qy, qz;
-    q_of_pixel<KEY>(P, q_geom(P), ihex, i, qx, qy, qz);
+    if (!cs::batch_q_from_table(S, ihex, i, qx, qy, qz)) q_of_pixel<KEY>(P, q_geom(P), ihex, i, qx, qy, qz);
     bool guard = false;
     const double v = calc_mixed<KEY>(C, S.peaks, qx, qy, qz, guard);
     out[S.out_offset + (long)(ihex - P.xmin) + (long)(P.xmax - P.xmin) * (long)(i - P.ymin)] = v;
@@ -1354,10 +1420,24 @@ __global__ void __launch_bounds__(128) k_batch_redo_cyl_warp(const cs::BatchSetD
 
 namespace cs {
 
+void peak_constants(const cs_prepared &P, csm::PeakTab &T) {
+    const double widthiso = 1.0 / P.uca;
+    T.kd_iso = 4.0 / M_PI / (widthiso * widthiso) * 1.4426950408889634;
+    T.inv_iso = 1.0 / (M_PI * widthiso / 2.0);
+    T.dmax_iso = (float)(9.4 * widthiso);
+    double width = 1;
+    if (P.debyescherrer) width = 4.0 / P.domainsize;
+    width *= P.width_zuf;
+    T.kd_an = 4.0 / M_PI / (width * width) * 1.4426950408889634;
+    T.inv_an = 1.0 / (M_PI * width / 2.0);
+    T.dmax_an = (float)(9.4 * width);
+    T.kphi = 4.0 / (M_PI * P.phiwidth * P.phiwidth) * 1.4426950408889634;
+}
+
 // Compact, sorted reflection tables from the prepared block (see PeakTab).
 void build_peak_tables(const cs_prepared &P, HostPeaks &H) {
-    H.aq.clear(); H.amf.clear(); H.av.clear(); H.iq.clear(); H.imf.clear(); H.aidx.clear();
-    struct A { float q; float4 v, vl; float mf; int idx; };
+    H.aq.clear(); H.awl.clear(); H.av.clear(); H.iq.clear(); H.imf.clear(); H.aidx.clear();
+    struct A { float q; float4 v, vl; float wl; int idx; };
     std::vector<A> an;
     for (int ii = 1; ii <= P.peakmax2 && ii < CS_LATPARLEN; ii++) {
         const float qh = P.latpar3[ii][5];
@@ -1371,11 +1451,11 @@ void build_peak_tables(const cs_prepared &P, HostPeaks &H) {
         const double hx = P.latpar3[ii][2], hy = P.latpar3[ii][3], hz = P.latpar3[ii][4];
         const double hn = std::sqrt(hx * hx + hy * hy + hz * hz);
         const double ux = hx / hn, uy = hy / hn, uz = hz / hn;
-        a.v = make_float4((float)ux, (float)uy, (float)uz,
-                          (float)((double)P.latpar3[ii][10] / (double)P.latpar3[ii][11] * (double)mf));
+        const double wd = (double)P.latpar3[ii][10] / (double)P.latpar3[ii][11] * (double)mf;
+        a.v = make_float4((float)ux, (float)uy, (float)uz, (float)wd);
+        a.wl = (float)(wd - (double)(float)wd);
         a.vl = make_float4((float)(ux - (double)(float)ux), (float)(uy - (double)(float)uy), (float)(uz - (double)(float)uz),
                            (float)(1.0 - hn / q));
-        a.mf = (float)mf;
         a.idx = ii;
         an.push_back(a);
     }
@@ -1384,7 +1464,7 @@ void build_peak_tables(const cs_prepared &P, HostPeaks &H) {
         H.aq.push_back(a.q);
         H.av.push_back(a.v);
         H.av.push_back(a.vl);
-        H.amf.push_back(a.mf);
+        H.awl.push_back(a.wl);
         H.aidx.push_back(a.idx);
     }
     struct I { float q; float mf; };
@@ -1436,8 +1516,10 @@ static void launch_mixed_key(const DevSet &D, const csm::PeakTab &T, const cs_pr
         launch_redo(D, P, d_out, S, s);
 }
 
-int launch_image_mixed(const DevSet &D, const csm::PeakTab &T, const cs_prepared &P, double *d_out, MixedScratch &S,
+int launch_image_mixed(const DevSet &D, const csm::PeakTab &T0, const cs_prepared &P, double *d_out, MixedScratch &S,
                        cudaStream_t s) {
+    csm::PeakTab T = T0;
+    if (P.lattice) peak_constants(P, T);
     const int nx = P.zzmax - P.zzmin, ny = P.iimax - P.iimin;
     if (nx <= 0 || ny <= 0) return CS_OK;
     if (P.twin) return CS_ERR_UNSUPPORTED;
@@ -1456,6 +1538,30 @@ int launch_image_mixed(const DevSet &D, const csm::PeakTab &T, const cs_prepared
 
 
 // ---- batch launchers -------------------------------------------------------
+
+// Pixel geometry table (cs_batch.h): the drop-in's convert_idx2q of every
+// pixel of [-half, half]^2; this unit rounds as the FP64 units do (no
+// contraction), so the values are the ones each set would compute.
+__global__ void k_qtable(const cs_prepared *__restrict__ P, int half, double *__restrict__ q) {
+    const int w = 2 * half + 1;
+    const long n = (long)w * w;
+    for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
+        const int ihex = (int)(j % w) - half;
+        const int i = (int)(j / w) - half;
+        double qx, qy, qz;
+        cs64::convert_idx2q(*P, ihex, i, qx, qy, qz);
+        q[j] = qx;
+        q[j + n] = qy;
+        q[j + 2 * n] = qz;
+    }
+}
+
+int launch_qtable(const QTable &t, cudaStream_t s) {
+    const long n = (long)(2 * t.half + 1) * (2 * t.half + 1);
+    const int grid = (int)std::min<long>((n + 255) / 256, (long)sm_count_m() * 8);
+    k_qtable<<<grid, 256, 0, s>>>(t.prep, t.half, t.d);
+    return launch_status();
+}
 
 int launch_batch_mixed(const BatchSetDev *d_sets, const BatchGroup &g, int group_index, unsigned long long *d_counter,
                        const cs_chi_node *d_chi, double *d_out, const BatchRedo &R, int grid, cudaStream_t s,

@@ -18,11 +18,17 @@ struct PeakTab {
     const float *aq = nullptr;   // q_hkl
     const float4 *av = nullptr;  // per reflection two entries: unit q_hkl (x, y, z), mult * g3/peaknorm1;
                                  // low parts of the unit vector, 1 - |h|/q_hkl
-    const float *amf = nullptr;  // multiplicity * structure factor (also folded into av[2i].w)
+    const float *awl = nullptr;  // low part of av[2i].w (mult g3/peaknorm1 = av[2i].w + awl[i])
     const int *aidx = nullptr;   // row of the reflection in latpar2/latpar3
     int n_iso = 0;
     const float *iq = nullptr;
     const float *imf = nullptr;
+    // per-set factors of the sums (cs::peak_constants): exp2 scales
+    // 4 log2(e)/(pi w^2) and normalisations 1/(pi w/2) of the isotropic and
+    // anisotropic peaks, their windows 9.4 w, and 4 log2(e)/(pi phiwidth^2);
+    // the anisotropic ones only when the width does not depend on q (para 0)
+    double kd_iso = 0, inv_iso = 0, kd_an = 0, inv_an = 0, kphi = 0;
+    float dmax_iso = 0, dmax_an = 0;
 };
 
 }  // namespace csm
@@ -38,11 +44,13 @@ struct MixedScratch {
 
 // Host form of the compact peak tables (built from the prepared block).
 struct HostPeaks {
-    std::vector<float> aq, amf, iq, imf;
+    std::vector<float> aq, awl, iq, imf;
     std::vector<float4> av;
     std::vector<int> aidx;
 };
 void build_peak_tables(const cs_prepared &P, HostPeaks &H);
+// fills the per-set factors of T from the prepared block
+void peak_constants(const cs_prepared &P, csm::PeakTab &T);
 
 int launch_image_mixed(const DevSet &D, const csm::PeakTab &T, const cs_prepared &P, double *d_out, MixedScratch &S,
                        cudaStream_t s);
