@@ -281,21 +281,27 @@ struct ChiArgs {
     int i1;
 };
 
-__device__ __forceinline__ double chi_integrand(const ChiArgs &A, double cx, double sx, double cd, double sd) {
+// the integrand's argument; false for the cases without one (integrand 0)
+__device__ __forceinline__ bool chi_argument(const ChiArgs &A, double cx, double sx, double cd, double sd,
+                                             double &argx) {
     const double eps = 0.0000000001;
-    double argx;
     switch (A.i1) {
     case 1: {
         const double mlx1 = A.p11 * cx * sd + A.p12 * sx * sd + A.p13 * cd;
         const double mlx2 = A.p21 * sx * sd + A.p22 * cx * sd + A.p23 * cd;
         argx = (A.qx * mlx1 + A.qy * mlx2 + eps) * A.l / A.zp1;
-        break;
+        return true;
     }
-    case 2: argx = (A.qx * cd - A.qy * sx * sd + eps) * A.l / A.zp1; break;
-    case 3: argx = (A.qx * sx * sd + A.qy * cd + eps) * A.l / A.zp1; break;
-    case 4: argx = (A.qx * sx * sd - A.qy * cx * sd + eps) * A.l / A.zp1; break;
-    default: return 0.0;
+    case 2: argx = (A.qx * cd - A.qy * sx * sd + eps) * A.l / A.zp1; return true;
+    case 3: argx = (A.qx * sx * sd + A.qy * cd + eps) * A.l / A.zp1; return true;
+    case 4: argx = (A.qx * sx * sd - A.qy * cx * sd + eps) * A.l / A.zp1; return true;
+    default: return false;
     }
+}
+
+__device__ __forceinline__ double chi_integrand(const ChiArgs &A, double cx, double sx, double cd, double sd) {
+    double argx;
+    if (!chi_argument(A, cx, sx, cd, sd, argx)) return 0.0;
     if (len_factor_small(argx, A.zm1)) return len_factor_series(argx, A.zm1);
     return (A.a1 / (argx * argx)) * (1 - cos(A.zm1 * atan(2.0 * argx)) / pow(1.0 + 4 * argx * argx, A.zm1h));
 }

@@ -22,6 +22,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "cs_ff.cuh"
 #include "cs_fp64.cuh"
 #include "cs_launch.h"
 #include "cs_batch.cuh"
@@ -39,7 +40,7 @@ using cs64::Ctx;
 // closed forms / quadratures (a few FP32 roundings).
 #define EPS_SERIES 1.0e-14
 #define EPS_PQ 3.0e-7
-#define EPS_PEAK 1.0e-9  // peak sums beyond their own estimate (pair sums, table rounding)
+#define EPS_PEAK 1.0e-12  // peak sums beyond their own estimate (pair sums, table rounding)
 
 // decision guard: true when v is within `band` relative of threshold t
 __device__ __forceinline__ bool near(double v, double t, double band) { return fabs(v - t) <= band * fabs(t); }
@@ -207,24 +208,9 @@ __device__ float cyl_pqr_asym(double argpq_d, double zr_d, float &rel) {
     return v;
 }
 
-// The same in FP64, for the second pass of lattice pixels whose structure
-// factor amplifies the FP32 form's error (calc_mixed): one atan, one log1p,
-// two exps, a sine and a cosine; its own error is that of a few FP64
-// roundings per term, relative to the sum.
-__device__ double cyl_pqr_asym_d(double argpq, double zr, float &rel) {
-    const double t = atan(2.0 * argpq), L = log1p(4.0 * argpq * argpq);
-    const double a3 = argpq * argpq * argpq;
-    const double pqr1 = (1.0 / (zr * (zr - 1) * (zr - 2))) / a3;
-    const double pqr2 = pqr1 * sin((zr - 2) * t) / exp((zr - 2) / 2.0 * L);
-    const double b3 = (1.0 / (zr * (zr - 1) * (zr - 2) * (zr - 3))) / (a3 * argpq);
-    const double pqr3 = b3 * cos((zr - 3) * t) / exp((zr - 3) / 2.0 * L);
-    const double v = (4.0 / M_PI) * (pqr1 - pqr2 - (9.0 / 8.0) * pqr3);
-    rel = (float)((fabs(pqr1) + fabs(pqr2) + fabs(pqr3)) * 1e-13 / fabs(v) + 1e-15);
-    return v;
-}
-
 // FP64 amplitude of the cylinder cross-section F(q) asymptote (the drop-in's
-// expression with the prepared Gamma ratios), for the same second pass
+// expression with the prepared Gamma ratios), for lattice pixels (whose F(q)
+// radial factor is almost always its FP64 series: q below limqf4)
 __device__ double cyl_fqr_asym_d(double a, double zr, double g0, double g1, float &rel) {
     const double t = atan(a);
     const double p1 = g0 * pow(a, -3 / 2.0) * (sin((zr - 1 / 2.0) * t) - cos((zr - 1 / 2.0) * t)) /
@@ -543,11 +529,73 @@ __device__ double qromb_delta_f(const Ctx &C, const ChiArgsF &A, bool &guard) {
     return pq;
 }
 
+// qrombchid by the whole warp (chi nodes over the lanes, FP64 sums and
+// extrapolation, the FP64 path's arguments) with the integrand's closed form
+// in float pairs (csff::cyl_len_closed, ~1e-13) instead of FP64: the value
+// agrees with cs64::qromb_chi_warp to ~1e-12, and its stop decisions are the
+// FP64 path's except within 1e-8 of the threshold, which sets `band` (the
+// caller then takes the FP64 form).
+__device__ double qromb_chi_warp_pair(const Ctx &C, const cs64::ChiArgs &A, double cd, double sd, bool &band) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const double b = C.P->romb_chi_b;
+    auto f = [&](double cx, double sx) -> double {
+        double argx;
+        if (!cs64::chi_argument(A, cx, sx, cd, sd, argx)) return 0.0;
+        if (cs64::len_factor_small(argx, A.zm1)) return cs64::len_factor_series(argx, A.zm1);
+        float rel;
+        return csff::cyl_len_closed(argx, A.z, rel);
+    };
+    double win[5];
+    double cur, pq = 0.0, dss = 0.0;
+    int cnt;
+    {
+        double v = 0.0;
+        if (lane < 2) {
+            const cs_chi_node n = C.chi[lane];
+            v = f(n.c, n.s);
+        }
+        cur = 0.5 * b * (__shfl_sync(full, v, 0) + __shfl_sync(full, v, 1));
+        cnt = 1;
+    }
+    win[4] = cur;
+    for (int j = 2; j <= CS_NODE_LEVELS; j++) {
+        const cs_chi_node *nd = C.chi + CS_NODE_OFFSET(j);
+        double sump = 0.0;
+        for (int base = 0; base < cnt; base += 32) {
+            double v = 0.0;
+            if (base + lane < cnt) {
+                const cs_chi_node n = nd[base + lane];
+                v = f(n.c, n.s);
+            }
+            const int m = (cnt - base) < 32 ? (cnt - base) : 32;
+            for (int u = 0; u < m; u++) sump += __shfl_sync(full, v, u);
+        }
+        cur = 0.5 * (cur + b * sump / (double)cnt);
+        cnt = 2 * cnt;
+        win[0] = win[1];
+        win[1] = win[2];
+        win[2] = win[3];
+        win[3] = win[4];
+        win[4] = cur;
+        if (j >= 5) {
+            cs64::polint5(win, pq, dss);
+            const double lhs = fabs(dss), rhs = 1.0e-4 * fabs(pq);
+            if (fabs(lhs - rhs) <= 1e-8 * rhs || !isfinite(pq)) band = true;
+            if (lhs < rhs) return pq;
+            if (fabs(pq) < 1.0e-300) return pq;
+        }
+    }
+    band = true;  // beyond the node table: the FP64 form's own loop
+    return pq;
+}
+
 // The outer (delta) quadrature for the warp-level redo of one guarded pixel:
 // the delta nodes of a level spread over the lanes, each lane's inner
 // integral in FP32; an inner integral whose FP32 form is in its guard band is
-// recomputed by the whole warp in FP64 (cs64::qromb_chi_warp on the FP64
-// arguments: the FP64 path's value). Every lane returns the same value and
+// recomputed by the whole warp with the float-pair integrand
+// (qromb_chi_warp_pair), and in FP64 (cs64::qromb_chi_warp on the FP64
+// arguments: the FP64 path's value) where that one's decision is in its band. Every lane returns the same value and
 // guard; what stays guarded (the outer decision, a non-finite value) is left
 // to the exact FP64 pixel.
 __device__ double qromb_delta_warp_f(const Ctx &C, const ChiArgsF &A, bool &guard) {
@@ -569,7 +617,9 @@ __device__ double qromb_delta_warp_f(const Ctx &C, const ChiArgsF &A, bool &guar
             const int l = __ffs(m) - 1;
             m &= m - 1;
             const double cl = __shfl_sync(full, c, l), sl = __shfl_sync(full, s, l);
-            const double w = cs64::qromb_chi_warp(C, A64, cl, sl);
+            bool band = false;
+            double w = qromb_chi_warp_pair(C, A64, cl, sl, band);
+            if (band) w = cs64::qromb_chi_warp(C, A64, cl, sl);
             if (lane == l) v = w;
         }
         if (active && !isfinite(v)) bad = true;
@@ -660,41 +710,6 @@ __device__ __forceinline__ void scaled_square(float kh, float kl, float dh, floa
     xl = fmaf(kh, p, -xh) + fmaf(kh, pe, kl * p);
 }
 
-// 2^(-j/64), j = 0..63, each the float pair (hi, lo) of its double value:
-// the table of Tang's table-driven exponential (ACM TOMS 15, 1989)
-__device__ const float2 kExp2m64[64] = {
-    {0x1.0000000000000p+0f, 0x0.0p+0f}, {0x1.fa7c180000000p-1f, 0x1.9e90d80000000p-29f},
-    {0x1.f507660000000p-1f, -0x1.246eb00000000p-27f}, {0x1.efa1be0000000p-1f, 0x1.cc2b440000000p-26f},
-    {0x1.ea4afa0000000p-1f, 0x1.52486c0000000p-28f}, {0x1.e502ee0000000p-1f, 0x1.e2cffe0000000p-27f},
-    {0x1.dfc9740000000p-1f, -0x1.908c940000000p-26f}, {0x1.da9e600000000p-1f, 0x1.ed99420000000p-28f},
-    {0x1.d5818e0000000p-1f, -0x1.822dbc0000000p-28f}, {0x1.d072d40000000p-1f, 0x1.40f1300000000p-26f},
-    {0x1.cb720e0000000p-1f, -0x1.8837cc0000000p-28f}, {0x1.c67f120000000p-1f, 0x1.cafa2a0000000p-26f},
-    {0x1.c199be0000000p-1f, -0x1.3d56b20000000p-28f}, {0x1.bcc1ea0000000p-1f, -0x1.f687c60000000p-26f},
-    {0x1.b7f7700000000p-1f, -0x1.a094380000000p-26f}, {0x1.b33a2c0000000p-1f, -0x1.ec3a820000000p-27f},
-    {0x1.ae89fa0000000p-1f, -0x1.a94b140000000p-27f}, {0x1.a9e6b60000000p-1f, -0x1.50c0480000000p-26f},
-    {0x1.a5503c0000000p-1f, -0x1.b83b540000000p-26f}, {0x1.a0c6680000000p-1f, -0x1.2886a60000000p-27f},
-    {0x1.9c49180000000p-1f, 0x1.51f8480000000p-28f}, {0x1.97d82a0000000p-1f, -0x1.0d8d800000000p-32f},
-    {0x1.93737c0000000p-1f, -0x1.e647440000000p-26f}, {0x1.8f1aea0000000p-1f, -0x1.baa2320000000p-27f},
-    {0x1.8ace540000000p-1f, 0x1.15506e0000000p-28f}, {0x1.868d9a0000000p-1f, -0x1.2edb440000000p-27f},
-    {0x1.82589a0000000p-1f, -0x1.accc7c0000000p-27f}, {0x1.7e2f340000000p-1f, -0x1.2616340000000p-26f},
-    {0x1.7a11480000000p-1f, -0x1.829fd00000000p-26f}, {0x1.75feb60000000p-1f, -0x1.37b3060000000p-26f},
-    {0x1.71f75e0000000p-1f, 0x1.1d8bee0000000p-26f}, {0x1.6dfb240000000p-1f, -0x1.cd72e80000000p-28f},
-    {0x1.6a09e60000000p-1f, 0x1.9fcef40000000p-27f}, {0x1.6623880000000p-1f, 0x1.2a91120000000p-28f},
-    {0x1.6247ec0000000p-1f, -0x1.f8b5500000000p-26f}, {0x1.5e76f20000000p-1f, -0x1.4a5bd80000000p-26f},
-    {0x1.5ab07e0000000p-1f, -0x1.5bd5ec0000000p-28f}, {0x1.56f4740000000p-1f, -0x1.295b040000000p-26f},
-    {0x1.5342b60000000p-1f, -0x1.2c56100000000p-26f}, {0x1.4f9b280000000p-1f, -0x1.2c5a6c0000000p-26f},
-    {0x1.4bfdae0000000p-1f, -0x1.593abc0000000p-26f}, {0x1.486a2c0000000p-1f, -0x1.47d8660000000p-26f},
-    {0x1.44e0860000000p-1f, 0x1.8624b40000000p-31f}, {0x1.4160a20000000p-1f, 0x1.f72e2a0000000p-29f},
-    {0x1.3dea640000000p-1f, 0x1.8246840000000p-26f}, {0x1.3a7db40000000p-1f, -0x1.634c020000000p-26f},
-    {0x1.371a740000000p-1f, -0x1.18aac60000000p-26f}, {0x1.33c08c0000000p-1f, -0x1.b37d200000000p-26f},
-    {0x1.306fe00000000p-1f, 0x1.4636e20000000p-26f}, {0x1.2d285a0000000p-1f, 0x1.b900c20000000p-27f},
-    {0x1.29e9e00000000p-1f, -0x1.5c04240000000p-26f}, {0x1.26b4560000000p-1f, 0x1.789f380000000p-27f},
-    {0x1.2387a60000000p-1f, 0x1.ceac480000000p-26f}, {0x1.2063b80000000p-1f, 0x1.0c519a0000000p-26f},
-    {0x1.1d48740000000p-1f, -0x1.d2e8ca0000000p-26f}, {0x1.1a35be0000000p-1f, 0x1.6df96e0000000p-26f},
-    {0x1.172b840000000p-1f, -0x1.c157420000000p-28f}, {0x1.1429aa0000000p-1f, 0x1.d525bc0000000p-26f},
-    {0x1.11301e0000000p-1f, -0x1.fdb4960000000p-26f}, {0x1.0e3ec40000000p-1f, -0x1.a585cc0000000p-26f},
-    {0x1.0b55860000000p-1f, 0x1.9f31220000000p-26f}, {0x1.0874520000000p-1f, -0x1.e2990e0000000p-27f},
-    {0x1.059b0e0000000p-1f, -0x1.9d4f520000000p-26f}, {0x1.02c9a40000000p-1f, -0x1.887fa00000000p-29f}};
 
 // s + e = a + b exactly, for |a| >= |b| (or a = 0)
 __device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e) {
@@ -702,24 +717,27 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &
     e = b - (s - a);
 }
 
-// 2^-(xh + xl) as a float pair (eh + el), 0 <= xh < 2^14 (xl a low part):
-// xh = k/64 + r with r exact (both sides are multiples of xh's ulp, |r| <= 1/128),
-// 2^-(k/64) from the table scaled by 2^-(k>>6), and 2^-(r + xl) = 1 + p with
-// p = expm1(-(r + xl) ln 2), |p| < 0.0055, from its Taylor series through the
-// fifth power (remainder < 4e-17). p is formed in FP32, so its own error is
-// ~1e-7 of p, i.e. ~7e-10 of the result; with the other roundings the pair is
-// within 2e-9 (relative) of 2^-(xh + xl).
+// 2^-(xh + xl) as a float pair (eh + el), 0 <= xh < 2^14 (xl a low part),
+// with the table of 2^(-j/64) of cs_ff.cuh (Tang's table-driven
+// exponential): xh = k/64 + r with r exact (both sides are multiples of xh's
+// ulp, |r| <= 1/128), a = -(r + xl) ln 2 as a pair, and 2^-(r + xl) = 1 + p,
+// p = a + a^2/2 + a^3 (1/6 + a/24 + a^2/120) (remainder < 3e-17; the cubic
+// tail, below 3e-8, in FP32). The pair is within ~3e-14 (relative) of
+// 2^-(xh + xl).
 __device__ __forceinline__ void exp2m_pair(float xh, float xl, float &eh, float &el) {
     const float k = rintf(xh * 64.0f);
-    const float r = fmaf(k, -0.015625f, xh) + xl;
+    const float r = fmaf(k, -0.015625f, xh);  // exact
     const int ki = (int)k;
-    const float2 t = __ldg(&kExp2m64[ki & 63]);
-    const float a = -r * 0.693147182f;
-    const float p = a * fmaf(a, fmaf(a, fmaf(a, fmaf(a, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f), 0.5f), 1.0f);
-    float sh, se;
-    fast_two_sum(t.x, fmaf(t.x, p, t.y), sh, se);
-    eh = ldexpf(sh, -(ki >> 6));
-    el = ldexpf(se, -(ki >> 6));
+    const csff::ff t = csff::from_pair(&csff::kExp2m64[ki & 63]);
+    csff::ff rr;
+    csff::two_sum(r, xl, rr.hi, rr.lo);
+    const csff::ff a = csff::neg(csff::mul(rr, csff::ff{0x1.62e43p-1f, -0x1.05c61p-29f}));  // -(r + xl) ln 2
+    const float ah = a.hi;
+    const float tail = ah * ah * ah * fmaf(ah, fmaf(ah, 1.0f / 120.0f, 1.0f / 24.0f), 1.0f / 6.0f);
+    const csff::ff p = csff::add_f(csff::add(a, csff::mul_f(csff::sqr(a), 0.5f)), tail);
+    const csff::ff e = csff::add(t, csff::mul(t, p));
+    eh = ldexpf(e.hi, -(ki >> 6));
+    el = ldexpf(e.lo, -(ki >> 6));
 }
 
 // float-pair accumulator (sum of float pairs, error ~1e-13 of the sum of
@@ -757,7 +775,9 @@ __device__ __forceinline__ float asin2_rest(float s) {
 // eps_int).
 __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, double qy, double qz, double q,
                             double &radint, double &intens, double &eps_rad, double &eps_int, bool &guard) {
-    const float c0 = 3e-9f;
+    // per term: the pair exponential (3e-14) and the argument pair's own
+    // rounding (~4e-15 of the exponent, added per term below)
+    const float c0 = 5e-14f;
     // per-set factors from the table (the anisotropic width depends on q when
     // para is set: then it and its factors are formed here)
     double kd_an = T.kd_an, inv_an = T.inv_an;
@@ -793,7 +813,7 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
             const float m = __ldg(T.imf + i);  // an integer, exact
             const float th = eh * m;
             s.add(th, fmaf(eh, m, -th) + el * m);
-            w = fmaf(fabsf(th), c0, w);
+            w = fmaf(fabsf(th), fmaf(4e-15f, xh, c0), w);
         }
         // the normalisation is a product (the pair sum is far more accurate
         // than the bound needs) and the estimate's quotient FP32
@@ -868,8 +888,12 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
                     // kphi yphi^2 = 2 kphi s (1 + r): 2 kphi s as a pair, r small
                     const float ah = (2.0f * kph) * shh;
                     const float al = fmaf(2.0f * kph, shh, -ah) + 2.0f * fmaf(kph, shl, kpl * shh);
-                    two_sum(ah, fmaf(ah, asin2_rest(sh), al), xph, xpl);
-                    ephi = 1e-8f * xph;
+                    // r from FP32 coefficients: ~2e-7 of r; s as a pair: ~4e-15
+                    // of kphi absolute
+                    const float rs = asin2_rest(sh);
+                    // (ah + al)(1 + r): the low part takes its share of r too
+                    two_sum(ah, fmaf(ah, rs, fmaf(al, rs, al)), xph, xpl);
+                    ephi = fmaf(xph, fmaf(2e-7f, rs, 1e-13f), 4e-15f * kph);
                 } else {
                     const float yphi = 2.0f * asinf(sqrtf(0.5f * sh));
                     xph = kph * yphi * yphi;
@@ -888,7 +912,7 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
             const float wl = __ldg(T.awl + i);
             const float th = eh * v.w;
             s.add(th, fmaf(eh, v.w, -th) + fmaf(eh, wl, el * v.w));
-            w = fmaf(fabsf(th), c0 + ephi, w);
+            w = fmaf(fabsf(th), fmaf(4e-15f, sx, c0) + ephi, w);
         }
         intens = s.value() * inv_an;
         eps_int = s.h != 0.0f ? (double)(w / fabsf(s.h)) : 0.0;
@@ -942,8 +966,10 @@ __device__ double sphere_fq_mixed(const cs_prepared &P, double q, bool &guard, d
 }
 
 // formpq_partCylinder, ordis 0 and 6, cs 0 (mixed)
-// F64: the closed forms in FP64 (the second pass of lattice pixels).
-template <bool LAT, bool WARP = false, bool F64 = false>
+// PAIR: the closed forms in float pairs (csff::cyl_len_closed,
+// csff::cyl_cross_asym: ~1e-13), for lattice pixels, whose structure factor
+// can amplify the form factors' errors by orders of magnitude.
+template <bool LAT, bool WARP = false, bool PAIR = false>
 __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, bool &guard, double &err) {
     const cs_prepared &P = *C.P;
     if (P.cs != 0) {
@@ -965,12 +991,15 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
             // FP32 closed form (its small-argument series where it cancels),
             // refined with FP64 arguments when its own estimate exceeds the
-            // switch; lattice pixels skip that refinement and carry the
-            // estimate into the structure factor's error bound
-            // (lattice_combine): a second pass takes the FP64 form where the
-            // structure factor amplifies it
-            if (F64) {
-                pql = cs64::len_factor(arglq, zl);
+            // switch; lattice pixels take the float-pair form (PAIR)
+            if (PAIR) {
+                if (cs64::len_factor_small(arglq, zl - 1)) {
+                    pql = cs64::len_factor_series(arglq, zl - 1);
+                } else {
+                    float rel;
+                    pql = csff::cyl_len_closed(arglq, zl, rel);
+                    el = rel;
+                }
             } else {
                 float rel;
                 pql = cyl_len_factor_e<false>(arglq, zl, rel);
@@ -1049,8 +1078,8 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
             float rel;
             const double zr = z_of(P.sigma);
             const double argpq = q * P.radius / (zr + 1);
-            if (F64) {
-                pqr = cyl_pqr_asym_d(argpq, zr, rel);
+            if (PAIR) {
+                pqr = csff::cyl_cross_asym(argpq, zr, rel);
             } else {
                 pqr = cyl_pqr_asym<false>(argpq, zr, rel);
                 // (a zero length factor makes the product zero: no need to refine)
@@ -1066,7 +1095,7 @@ __device__ double cyl_pq_mixed(const Ctx &C, double qxs, double qys, double q, b
 
 
 // formfq_partCylinder, ordis 0 and 6, cs 0 (mixed)
-template <bool LAT, bool F64 = false>
+template <bool LAT, bool PAIR = false>
 __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qys, double q, bool &guard,
                              double &err) {
     const cs_prepared &P = *C.P;
@@ -1087,12 +1116,15 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
             const double arglq = (qxs + qys + CS_EPS9) * P.length / (zl + 1);
             // FP32 closed form (its small-argument series where it cancels),
             // refined with FP64 arguments when its own estimate exceeds the
-            // switch; lattice pixels skip that refinement and carry the
-            // estimate into the structure factor's error bound
-            // (lattice_combine): a second pass takes the FP64 form where the
-            // structure factor amplifies it
-            if (F64) {
-                pql = cs64::len_factor(arglq, zl);
+            // switch; lattice pixels take the float-pair form (PAIR)
+            if (PAIR) {
+                if (cs64::len_factor_small(arglq, zl - 1)) {
+                    pql = cs64::len_factor_series(arglq, zl - 1);
+                } else {
+                    float rel;
+                    pql = csff::cyl_len_closed(arglq, zl, rel);
+                    el = rel;
+                }
             } else {
                 float rel;
                 pql = cyl_len_factor_e<false>(arglq, zl, rel);
@@ -1143,7 +1175,7 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
         const double a = q * P.radius / (zr + 1);
         float rel;
         double amp;
-        if (F64) {
+        if (PAIR) {
             amp = cyl_fqr_asym_d(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
         } else {
             amp = cyl_fqr_asym<false>(a, zr, P.gamma_ratio[0], P.gamma_ratio[1], rel);
@@ -1165,25 +1197,27 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
 // (szq -> 0 between peaks, I0 szq pq against base) the input errors are
 // amplified; a first-order estimate of the result's error is propagated
 // alongside, and a pixel whose estimate exceeds 5e-6 of |I| (half the 1e-5 bar)
-// is recomputed in FP64.
-__device__ __forceinline__ double lattice_combine(const cs_prepared &P, double q, double pq, double errp, double fq,
-                                                  double errf, double pqi, double errpi, double radint, double intens,
-                                                  double eps_rad, double eps_int, double tailv, bool &guard) {
-    const double v = P.latpar[1] * P.latpar[2];
-    const double r2 = 8 * M_PI * M_PI * M_PI * radint / (4 * M_PI * v);
-    // Debye-Waller factors in FP64 (two exps per pixel): in FP32 the rounding
-    // of the argument alone moves them by |arg| 6e-8, which dominated the
-    // error estimate of pixels where szq cancels
-    const double e2 = exp(-P.ucb * q * q), e1 = exp(-P.dwfactor * q * q);
+// is recomputed in FP64. The Debye-Waller factors are FP64 exponentials (in
+// FP32 the rounding of the argument alone moved them by |arg| 6e-8, which
+// dominated the estimate where szq cancels; the iso factor szqiso cancels
+// too), the ratio F/P a float-pair quotient, and the lattice volume's factors
+// 2 pi/V and 2 pi^2/V per set.
+__device__ __forceinline__ double lattice_combine(const cs_prepared &P, const PeakTab &T, double q, double pq,
+                                                  double errp, double fq, double errf, double pqi, double errpi,
+                                                  double radint, double intens, double eps_rad, double eps_int,
+                                                  double tailv, bool &guard) {
+    const double r2 = radint * T.c_r2;
+    const double q2 = q * q;
+    const double e2 = exp(-P.ucb * q2), e1 = exp(-P.dwfactor * q2);
     const double ee2 = 4e-16, ee1 = 4e-16;
     const double szqiso = 1 + (r2 - 1) * e2;
-    const double r1 = 2 * M_PI * intens / v;
-    const double ratio = fq / pq;
+    const double r1 = intens * T.c_r1;
+    const double ratio = csff::to_double(csff::div(csff::from_double(fq), csff::from_double(pq)));
     const double t = ratio * (r1 - 1) * e1;
     const double szq = 1 + t;
     const double res = P.base + P.izero * (szq * pq + P.iso * szqiso * pqi) + tailv;
-    // first-order error bound
-    const double dt = fabs(t) * (errf + errp + ee1) + fabs(ratio * e1 * r1) * (eps_int + EPS_PEAK);
+    // first-order error bound (the quotient's own 1e-14 included)
+    const double dt = fabs(t) * (errf + errp + ee1 + 1e-14) + fabs(ratio * e1 * r1) * (eps_int + EPS_PEAK);
     const double d1 = fabs(pq) * dt + fabs(szq * pq) * errp;
     const double d2 = fabs(P.iso) * (fabs(pqi) * (fabs(r2 * e2) * (eps_rad + EPS_PEAK) + fabs((r2 - 1) * e2) * ee2) +
                                      fabs(szqiso * pqi) * errpi);
@@ -1212,7 +1246,7 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
         const double fq = sphere_fq_mixed<true>(P, q, guard, ef);
         double radint, intens, erad, eint;
         peak_sums_f(P, T, qx, qy, qz, q, radint, intens, erad, eint, guard);
-        return lattice_combine(P, q, pq, ep, fq, ef, pq, ep, radint, intens, erad, eint, tailv, guard);
+        return lattice_combine(P, T, q, pq, ep, fq, ef, pq, ep, radint, intens, erad, eint, tailv, guard);
     }
     if (KEY == CS_KEY_CYL_NONE_GAUSS) {
         double pq;
@@ -1235,12 +1269,13 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
         return P.base + P.izero * (pq + P.iso) + tailv;
     }
     if (KEY == CS_KEY_CYL_GAUSS_BCT_ZDIR) {
-        // form factors of the orientation case, closed forms in FP64: the
-        // structure factor's cancellation (lattice_combine) amplifies their
-        // error, and an FP32 first pass with an FP64 second pass where the
-        // bound fails costs more (the warp runs both when one lane fails)
-        auto forms = [&](auto f64tag, double &pq, double &fq) {
-            constexpr bool F = decltype(f64tag)::value;
+        // form factors of the orientation case, closed forms in float pairs:
+        // the structure factor's cancellation (lattice_combine) amplifies
+        // their error by orders of magnitude. (An FP32 first pass with a
+        // second pass where the bound fails was slower: 30 % of the pixels
+        // failed, and a warp runs both passes when one lane fails.)
+        auto forms = [&](double &pq, double &fq) {
+            constexpr bool F = true;
             switch (P.orcase) {
             case CS_ORC_GENERAL:
                 pq = cyl_pq_mixed<true, false, F>(C, qx * P.cosphi * P.sintheta, qy * P.sinphi * P.sintheta, q, guard, ep);
@@ -1262,11 +1297,11 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
             }
         };
         double pq = 0, fq = 0;
-        forms(std::true_type{}, pq, fq);
+        forms(pq, fq);
         double radint, intens, erad, eint;
         peak_sums_f(P, T, qx, qy, qz, q, radint, intens, erad, eint, guard);
         // the reference's BCT function multiplies szqiso by 1 instead of pq
-        return lattice_combine(P, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, guard);
+        return lattice_combine(P, T, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, guard);
     }
     guard = true;
     return 0.0;
@@ -1432,6 +1467,9 @@ void peak_constants(const cs_prepared &P, csm::PeakTab &T) {
     T.inv_an = 1.0 / (M_PI * width / 2.0);
     T.dmax_an = (float)(9.4 * width);
     T.kphi = 4.0 / (M_PI * P.phiwidth * P.phiwidth) * 1.4426950408889634;
+    const double v = P.latpar[1] * P.latpar[2];
+    T.c_r1 = 2 * M_PI / v;
+    T.c_r2 = 8 * M_PI * M_PI * M_PI / (4 * M_PI * v);
 }
 
 // Compact, sorted reflection tables from the prepared block (see PeakTab).

@@ -28,6 +28,8 @@ struct PeakTab {
     // anisotropic peaks, their windows 9.4 w, and 4 log2(e)/(pi phiwidth^2);
     // the anisotropic ones only when the width does not depend on q (para 0)
     double kd_iso = 0, inv_iso = 0, kd_an = 0, inv_an = 0, kphi = 0;
+    // the structure factors' 2 pi/V and 8 pi^3/(4 pi V), V the cell volume
+    double c_r1 = 0, c_r2 = 0;
     float dmax_iso = 0, dmax_an = 0;
 };
 
