@@ -69,10 +69,16 @@ def parse():
     ap.add_argument("--no-extra", action="store_true", help="skip the per-config table")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison legs of the sweep")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--surrogate", default="", help="surrogate-seeded fits of this family ('2', '2x'); off by default")
-    ap.add_argument("--surrogate-train", type=int, default=32768)
-    ap.add_argument("--surrogate-epochs", type=int, default=200)
-    ap.add_argument("--surrogate-targets", type=int, default=8)
+    ap.add_argument("--surrogate", default="2,2x",
+                    help="config 5: surrogate-seeded fits of these families ('2' as specified, '2x' its phi = 0 "
+                         "variant), comma-separated; '' skips them")
+    ap.add_argument("--surrogate-train", default="30000,8192",
+                    help="training patterns per family (the specification's 200000 for family 2 take ~5 minutes of "
+                         "host preparation on a 16-core host: pass them explicitly)")
+    ap.add_argument("--surrogate-grid", default="256,64",
+                    help="GridPoints of the training patterns per family (256: the 512x512 detector)")
+    ap.add_argument("--surrogate-epochs", default="60,150", help="training epochs per family")
+    ap.add_argument("--surrogate-targets", default="16,4", help="fit targets per family (of the 1000 specified)")
     return ap.parse_args()
 
 
@@ -258,6 +264,11 @@ def roofline(work, key, pixels, seconds, peaks, traffic_per_pixel=None):
             "traffic": (t * pixels) if t is not None else None,
             "algorithmic_bytes": 8.0 * pixels,
             "pipes": {k: {"achieved": v[0], "peak": v[1], "unit": v[2], "frac": v[0] / v[1]} for k, v in rates.items()},
+            # issue-slot view of the same kernel (ncu, the capture that gave
+            # the counts): a DADD or DMUL fills an FP64 issue slot but counts
+            # one flop, so the flop fraction reads below the pipe's busy share
+            "pipe_active_pct_ncu": {"fp64": w.get("fp64_pipe_pct"), "fma": w.get("fma_pipe_pct"),
+                                    "xu": w.get("xu_pipe_pct")},
             "kernel": w.get("kernel"), "kernel_ms": seconds * 1e3, "pixels": pixels,
             "peaks": "measured here (cs_measure_pipe_peaks: FFMA, FFMA2, DFMA, MUFU.EX2 chains)",
             "work_source": w.get("source")}
@@ -287,9 +298,11 @@ def cpu_baseline_blocks(names, seconds, whole=True):
                       f"rows over {nt} host threads"}
 
 
-def sweep_sample_names():
+def sweep_sample_names(nsets=None):
+    """the reference-prepared sample sets of the sweep (k = 0, 64, ..., 4032),
+    those below nsets when given"""
     from oracle import ref_prepared as R
-    return [f"bct_set{k:04d}" for k in R.sweep_sample()]
+    return [f"bct_set{k:04d}" for k in R.sweep_sample() if nsets is None or k < nsets]
 
 
 # --------------------------------------------------------------- native arm
@@ -407,7 +420,7 @@ def sweep_accuracy_vs_cpu(b, out_host_view, names, rows_per_set=8):
     st = rel_stats(np.concatenate(gi), np.concatenate(ri), np.concatenate(ci))
     if worst is not None:
         st["worst_where_cond_le_1e-6"] = dict(zip(("rel", "set", "ihex", "i", "gpu", "cpu", "cond"), worst))
-    st["sample"] = f"{len(names)} reference-prepared sets (k = 0, 64, ..., 4032), {rows_per_set} ihex rows each"
+    st["sample"] = f"{len(names)} reference-prepared sets (k = 0, 64, ...), {rows_per_set} ihex rows each"
     return st
 
 
@@ -497,7 +510,7 @@ def sweep(cs, torch, C, args, world, peaks, work, clocks_start):
     # accuracy vs the CPU oracle on the reference-prepared sample sets
     host = out.cpu()
     hv = host.numpy()
-    row["accuracy_vs_cpu"] = sweep_accuracy_vs_cpu(b, lambda o, n: hv[o:o + n], sweep_sample_names())
+    row["accuracy_vs_cpu"] = sweep_accuracy_vs_cpu(b, lambda o, n: hv[o:o + n], sweep_sample_names(args.sweep_sets))
     del host, hv
     # e2e: the C-ABI host-buffer call, host parameters in, images out
     pinned = torch.empty(total, dtype=torch.float64, pin_memory=True)
@@ -520,19 +533,39 @@ def sweep(cs, torch, C, args, world, peaks, work, clocks_start):
 
 
 def surrogate_fits(args):
-    """Config 5: the surrogate trained on simulator patterns, then plain fits
-    (FP64, one vertex at a time, random start) against surrogate-seeded fits
-    (batched, mixed precision) run until they reach the plain fit's chi^2."""
+    """Config 5, per family: the surrogate (8 -> 512 -> 512 -> 512 -> 64x64)
+    trained on simulator patterns generated on the GPU and averaged to 64 x 64
+    there; then per target (Poisson noise, 1e4 counts at the peak, 256 x 256)
+    the plain fit (FP64, one vertex at a time, random start), the
+    surrogate-seeded fit (batched, mixed precision, until it reaches the plain
+    fit's chi^2) and the same batched mixed fit from the random start."""
     from crystalscatter_gb300 import surrogate as S
-    fam = S.Family(args.surrogate)
-    t0 = time.perf_counter()
-    U, Y = S.training_set(fam, args.surrogate_train, seed=11)
-    t_data = time.perf_counter() - t0
-    sur = S.Surrogate(fam, seed=11)
-    info = sur.train(U, Y, epochs=args.surrogate_epochs)
-    res = S.compare_fits(fam, sur, n_targets=args.surrogate_targets, seed=101)
-    res.update({"train_patterns": args.surrogate_train, "pattern_seconds": t_data, "training": info})
-    return res
+    fams = [f for f in args.surrogate.split(",") if f]
+    def per(v, i, conv):
+        parts = str(v).split(",")
+        return conv(parts[min(i, len(parts) - 1)])
+    out = {}
+    for i, name in enumerate(fams):
+        n_train = per(args.surrogate_train, i, int)
+        grid = per(args.surrogate_grid, i, int)
+        epochs = per(args.surrogate_epochs, i, int)
+        n_targets = per(args.surrogate_targets, i, int)
+        fam = S.Family(name, train_grid=grid)
+        t0 = time.perf_counter()
+        U, Y, t_prep = S.training_set_device(fam, n_train, seed=11)
+        t_data = time.perf_counter() - t0
+        sur = S.Surrogate(fam, seed=11)
+        info = sur.train(U, Y, epochs=epochs)
+        del U, Y
+        res = S.compare_fits(fam, sur, n_targets=n_targets, seed=101)
+        res.update({"train_patterns": n_train, "pattern_detector": f"{2 * grid}x{2 * grid}",
+                    "pattern_seconds": t_data, "pattern_host_prep_seconds": t_prep,
+                    "training": {k: v for k, v in info.items() if k != "loss_per_epoch"},
+                    "final_loss": info["loss_per_epoch"][-1] if info["loss_per_epoch"] else None,
+                    "targets_note": f"{n_targets} of the 1000 specified targets (seeded), the rest not run",
+                    "patterns_note": f"{n_train} training patterns (specified: 200000 of family 2)"})
+        out[name] = res
+    return out
 
 
 def native(args):
