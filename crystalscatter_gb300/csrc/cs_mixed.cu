@@ -1205,13 +1205,21 @@ __device__ double cyl_fq_mixed(const Ctx &C, double limql, double qxs, double qy
 __device__ __forceinline__ double lattice_combine(const cs_prepared &P, const PeakTab &T, double q, double pq,
                                                   double errp, double fq, double errf, double pqi, double errpi,
                                                   double radint, double intens, double eps_rad, double eps_int,
-                                                  double tailv, bool &guard) {
+                                                  double tailv, bool &guard, bool fq_exact = false) {
     const double r2 = radint * T.c_r2;
-    const double q2 = q * q;
-    const double e2 = exp(-P.ucb * q2), e1 = exp(-P.dwfactor * q2);
+    const double e2 = exp(-P.ucb * q * q), e1 = exp(-P.dwfactor * q * q);  // the drop-in's operations
     const double ee2 = 4e-16, ee1 = 4e-16;
     const double szqiso = 1 + (r2 - 1) * e2;
     const double r1 = intens * T.c_r1;
+    if (fq_exact && !isfinite(fq) && isfinite(pq)) {
+        // F(q) from the FP64 series, bit for bit the drop-in's, is not finite:
+        // so is the drop-in's result, its class (NaN, +-inf) set by the signs
+        // of the finite factors, which are the drop-in's unless r1 - 1 is
+        // within its error of 0
+        const double res = P.base + P.izero * ((1 + (fq / pq) * (r1 - 1) * e1) * pq + P.iso * szqiso * pqi) + tailv;
+        if (!(fabs(r1 - 1) > 1e-9 * fabs(r1)) && !isnan(fq)) guard = true;
+        return res;
+    }
     const double ratio = csff::to_double(csff::div(csff::from_double(fq), csff::from_double(pq)));
     const double t = ratio * (r1 - 1) * e1;
     const double szq = 1 + t;
@@ -1300,8 +1308,19 @@ __device__ double calc_mixed(const Ctx &C, const PeakTab &T, double qx, double q
         forms(pq, fq);
         double radint, intens, erad, eint;
         peak_sums_f(P, T, qx, qy, qz, q, radint, intens, erad, eint, guard);
+        // F(q) of the z-direction cylinder from its two FP64 series (length
+        // factor below 0.6 limqf1 of its argument, radial below limqf4): the
+        // drop-in's value bit for bit
+        double limql = q;
+        switch (P.orcase) {
+        case CS_ORC_GENERAL: limql = sqrt(P.cosphi * qx * qx + P.sinphi * qy * qy + CS_EPS9); break;
+        case CS_ORC_XAXIS: limql = fabs(qx); break;
+        case CS_ORC_YAXIS: limql = fabs(qy); break;
+        default: break;
+        }
+        const bool fq_exact = P.ordis == 6 && P.cs == 0 && limql < 0.6 * P.limqf[1] && q < P.limqf[4];
         // the reference's BCT function multiplies szqiso by 1 instead of pq
-        return lattice_combine(P, T, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, guard);
+        return lattice_combine(P, T, q, pq, ep, fq, ef, 1.0, 0.0, radint, intens, erad, eint, tailv, guard, fq_exact);
     }
     guard = true;
     return 0.0;

@@ -40,3 +40,13 @@ def test_surrogate_start_beats_random_start():
         c_r = np.median([exact_chi2(fam, target, rng.uniform(-1, 1, len(fam.keys))) for _ in range(5)])
         wins += c_s < 0.5 * c_r
     assert wins >= 3
+
+
+def test_device_training_set_matches_host_path():
+    """The device-resident pattern generation (batched launch, averaging on
+    the GPU) gives the host path's coarse log10 targets."""
+    fam = S.Family("2x", train_grid=64)
+    U, Y = S.training_set(fam, 40, seed=3)
+    Ud, Yd, _ = S.training_set_device(fam, 40, seed=3, chunk=16)
+    assert np.array_equal(U, Ud.cpu().numpy())
+    assert np.max(np.abs(Yd.cpu().numpy() - Y)) <= 2e-6 * max(1.0, float(np.max(np.abs(Y))))
