@@ -755,17 +755,31 @@ struct SumFF {
 
 // yphi = acos(1 - s) = 2 asin(sqrt(s/2)) and yphi^2 = 2 s (1 + r(s)) with
 // r(s) = sum_{n>=2} 2^n s^(n-1) / (n^2 C(2n, n)) (the series of asin^2); through
-// n = 17 the remainder is below 1e-12 for s < 1/2 (yphi < 60 degrees)
-__device__ __forceinline__ float asin2_rest(float s) {
-    const float c[16] = {1.666666667e-01f, 4.444444444e-02f, 1.428571429e-02f, 5.079365079e-03f,
-                         1.924001924e-03f, 7.611436183e-04f, 3.108003108e-04f, 1.300079731e-04f,
-                         5.542445171e-05f, 2.399326914e-05f, 1.051878828e-05f, 4.660632346e-06f,
-                         2.083721869e-06f, 9.388723824e-07f, 4.258997702e-07f, 1.943499843e-07f};
-    float r = c[15];
+// n = 17 the remainder is below 1e-12 for s < 1/2 (yphi < 60 degrees).
+// r(s) for s = sh + sl as a pair (rh + rl): r = s (1/6 + s (2/45 + s Q(s)))
+// with 1/6 and 2/45 as float pairs and the product s (2/45 + s Q) exact, so
+// that the FP32 rounding of Q's Horner sum enters r only through terms of
+// ~s^2/70 of it: r within ~1e-8 (relative) instead of ~1e-7
+__device__ __forceinline__ void asin2_rest_pair(float sh, float sl, float &rh, float &rl) {
+    const float c[14] = {1.428571429e-02f, 5.079365079e-03f, 1.924001924e-03f, 7.611436183e-04f,
+                         3.108003108e-04f, 1.300079731e-04f, 5.542445171e-05f, 2.399326914e-05f,
+                         1.051878828e-05f, 4.660632346e-06f, 2.083721869e-06f, 9.388723824e-07f,
+                         4.258997702e-07f, 1.943499843e-07f};
+    const float c0h = (float)(1.0 / 6.0), c0l = (float)(1.0 / 6.0 - (double)(float)(1.0 / 6.0));
+    const float c1h = (float)(2.0 / 45.0), c1l = (float)(2.0 / 45.0 - (double)(float)(2.0 / 45.0));
+    float q = c[13];
 #pragma unroll
-    for (int n = 14; n >= 0; n--) r = fmaf(r, s, c[n]);
-    return r * s;
+    for (int n = 12; n >= 0; n--) q = fmaf(q, sh, c[n]);
+    const float inner = fmaf(q, sh, c1h) + c1l;  // 2/45 + s Q
+    const float ph = sh * inner;
+    const float pe = fmaf(sh, inner, -ph);
+    float bh, be;
+    two_sum(c0h, ph, bh, be);
+    be += c0l + fmaf(sl, inner, pe);  // 1/6 + s inner = bh + be
+    rh = sh * bh;
+    rl = fmaf(sh, bh, -rh) + fmaf(sh, be, sl * bh);
 }
+
 
 // Error estimates of the sums: the terms are float pairs (exp2m_pair times the
 // reflection's factor as a float pair) summed as float pairs; a term carries
@@ -888,12 +902,13 @@ __device__ void peak_sums_f(const cs_prepared &P, const PeakTab &T, double qx, d
                     // kphi yphi^2 = 2 kphi s (1 + r): 2 kphi s as a pair, r small
                     const float ah = (2.0f * kph) * shh;
                     const float al = fmaf(2.0f * kph, shh, -ah) + 2.0f * fmaf(kph, shl, kpl * shh);
-                    // r from FP32 coefficients: ~2e-7 of r; s as a pair: ~4e-15
+                    // r as a pair from the pair s: ~2e-8 of r; s itself: ~4e-15
                     // of kphi absolute
-                    const float rs = asin2_rest(sh);
-                    // (ah + al)(1 + r): the low part takes its share of r too
-                    two_sum(ah, fmaf(ah, rs, fmaf(al, rs, al)), xph, xpl);
-                    ephi = fmaf(xph, fmaf(2e-7f, rs, 1e-13f), 4e-15f * kph);
+                    float rh, rl;
+                    asin2_rest_pair(shh, shl, rh, rl);
+                    // (ah + al)(1 + rh + rl): the low parts take their shares too
+                    two_sum(ah, fmaf(ah, rh, fmaf(al, rh, fmaf(ah, rl, al))), xph, xpl);
+                    ephi = fmaf(xph, fmaf(3e-8f, rh, 1e-13f), 4e-15f * kph);
                 } else {
                     const float yphi = 2.0f * asinf(sqrtf(0.5f * sh));
                     xph = kph * yphi * yphi;
