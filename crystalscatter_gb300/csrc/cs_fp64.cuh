@@ -306,8 +306,109 @@ __device__ __forceinline__ double chi_integrand(const ChiArgs &A, double cx, dou
     return (A.a1 / (argx * argx)) * (1 - cos(A.zm1 * atan(2.0 * argx)) / pow(1.0 + 4 * argx * argx, A.zm1h));
 }
 
+// The integrand at the interval's ends (level 1 of trapzdchid): for the
+// cylinder cases both ends take their own angle.
+__device__ __forceinline__ void chi_ends(const ChiArgs &A, const cs_chi_node &n0, const cs_chi_node &n1, double cd,
+                                         double sd, double &pa, double &pb) {
+    pa = chi_integrand(A, n0.c, n0.s, cd, sd);
+    pb = chi_integrand(A, n1.c, n1.s, cd, sd);
+}
+
+// chi integrand of trapzdchid for the disk P(q) cases i1 = 8..11 (i3 = 0),
+// Source/sc_calc_generic_gpu.cu:1849-2260 (interval ends) and 2604-2840
+// (interior nodes), with sigma = sigmal and l = the disk radius (length). The
+// unit vector of the pixel's q (qxl, qyl) meets the disk normal at qnn; the
+// Schulz-averaged disk factor at x = sqrt(1 - qnn^2) l qn/(z+1) is, for
+// sigmal < 0.15, its series in x^2/4 (carr2p) below x = 0.015 and its
+// asymptote above, otherwise the Ornstein-Zernike-like form.
+struct DiskChiArgs {
+    double qxl, qyl, qn, l, z, sigma;
+    double p11, p12, p13, p21, p22, p23;
+    const double *carr;
+    int i1;
+};
+
+__device__ __forceinline__ DiskChiArgs disk_chi_args(const cs_prepared &P, double qx, double qy, int i1,
+                                                     const double *carr) {
+    const double eps = 0.0000000001;
+    DiskChiArgs A;
+    A.sigma = P.sigmal;
+    A.z = (1 - A.sigma * A.sigma) / (A.sigma * A.sigma);
+    A.qn = sqrt(qx * qx + qy * qy + eps);
+    A.qxl = qx / A.qn;
+    A.qyl = qy / A.qn;
+    A.l = P.length;
+    A.p11 = P.romb_p[0];
+    A.p12 = P.romb_p[1];
+    A.p13 = P.romb_p[2];
+    A.p21 = P.romb_p[3];
+    A.p22 = P.romb_p[4];
+    A.p23 = P.romb_p[5];
+    A.carr = carr;
+    A.i1 = i1;
+    return A;
+}
+
+// qnn from the angle chi: (c1, s1) enter the first direction component and
+// (s2, c2) the second; every interior node passes (cos, sin, sin, cos) of its
+// own chi. The reference's general-case end a takes cos(a) with sin(b) and
+// sin(a) with cos(b) (:1856-1857); disk_chi_ends passes them so.
+__device__ __forceinline__ double disk_chi_value(const DiskChiArgs &A, double c1, double s1, double s2, double c2,
+                                                 double cd, double sd) {
+    const double eps = 0.0000000001;
+    double qnn;
+    switch (A.i1) {
+    case 8: {
+        const double ml1 = A.p11 * c1 * sd + A.p12 * s1 * sd + A.p13 * cd;
+        const double ml2 = A.p21 * s2 * sd + A.p22 * c2 * sd + A.p23 * cd;
+        qnn = A.qxl * ml1 + A.qyl * ml2;
+        break;
+    }
+    case 9: qnn = A.qxl * cd - A.qyl * s1 * sd; break;
+    case 10: qnn = A.qxl * s1 * sd + A.qyl * cd; break;
+    case 11: qnn = A.qxl * s1 * sd - A.qyl * c1 * sd; break;
+    default: return 0.0;
+    }
+    const double z = A.z;
+    const double x = sqrt(1.0 - qnn * qnn + eps) * A.l * A.qn / (z + 1);
+    if (A.sigma < 0.15) {
+        if (x < 0.015) {
+            double px = 1, oldpx = 0, argser = 1;
+            for (int i = 1; i <= 50; i++) {
+                argser = argser * x * x / 4.0;
+                px = px + A.carr[i] * argser;
+                if (series_converged(px, oldpx)) break;
+                oldpx = px;
+            }
+            return px;
+        }
+        const double px1 = (1 / (z * (z - 1) * (z - 2))) * pow(x, -3);
+        const double px2 = (1 / (z * (z - 1) * (z - 2))) * pow(x, -3) * sin((z - 2) * atan(2.0 * x)) /
+                           pow(1.0 + 4 * x * x, (z - 2) / 2.0);
+        const double px3 = (1 / (z * (z - 1) * (z - 2) * (z - 3))) * pow(x, -4) * cos((z - 3) * atan(2.0 * x)) /
+                           pow(1.0 + 4 * x * x, (z - 3) / 2.0);
+        return (4 / M_PI) * (px1 - px2 - (9 / 8.0) * px3);
+    }
+    const double px1 = (1 / (z * (z - 1) * (z - 2))) * pow(x, -3);
+    return 1 / (1.0 + M_PI / (4.0 * px1));
+}
+
+__device__ __forceinline__ double chi_integrand(const DiskChiArgs &A, double cx, double sx, double cd, double sd) {
+    return disk_chi_value(A, cx, sx, sx, cx, cd, sd);
+}
+
+__device__ __forceinline__ void chi_ends(const DiskChiArgs &A, const cs_chi_node &n0, const cs_chi_node &n1, double cd,
+                                         double sd, double &pa, double &pb) {
+    if (A.i1 == 8)
+        pa = disk_chi_value(A, n0.c, n1.s, n0.s, n1.c, cd, sd);
+    else
+        pa = disk_chi_value(A, n0.c, n0.s, n0.s, n0.c, cd, sd);
+    pb = disk_chi_value(A, n1.c, n1.s, n1.s, n1.c, cd, sd);
+}
+
 // qrombchid over chi in [0, chi_b] for one delta node (cd = cos(delta), sd = sin(delta)).
-__device__ inline double qromb_chi(const Ctx &C, const ChiArgs &A, double cd, double sd) {
+template <class Args>
+__device__ inline double qromb_chi(const Ctx &C, const Args &A, double cd, double sd) {
     const double a = 0.0, b = C.P->romb_chi_b;
     double win[5];
     double cur;
@@ -315,8 +416,8 @@ __device__ inline double qromb_chi(const Ctx &C, const ChiArgs &A, double cd, do
     double pq = 0.0, dss = 0.0;
     {
         const cs_chi_node n0 = C.chi[0], n1 = C.chi[1];
-        double pa = chi_integrand(A, n0.c, n0.s, cd, sd);
-        double pb = chi_integrand(A, n1.c, n1.s, cd, sd);
+        double pa, pb;
+        chi_ends(A, n0, n1, cd, sd, pa, pb);
         cur = 0.5 * (b - a) * (pa + pb);
         cnt = 1;
     }
@@ -420,14 +521,10 @@ __device__ inline double qromb_chi_warp(const Ctx &C, const ChiArgs &A, double c
     return pq;
 }
 
-// qrombdeltac(i0 = 4): Gaussian-weighted delta integral of qrombchid.
-__device__ inline double qromb_delta_cyl(const Ctx &C, const ChiArgs &A) {
-    // Orientation cases outside 1..4 (the 0-based general case) reach no
-    // branch of the chi integrand, which is then 0 at every node: every
-    // trapezoid estimate is +0, the Neville extrapolation gives +0, and the
-    // reference's loop stops at j = 5 on |I| < 1e-100 with +0. That value is
-    // returned directly.
-    if (A.i1 < 1 || A.i1 > 4) return 0.0;
+// qrombdeltac(i0 = 4 cylinder, 6 disk form factor): Gaussian-weighted delta
+// integral of qrombchid (both cases weigh alike, :1051-1070, 1104-1120).
+template <class Args>
+__device__ inline double qromb_delta(const Ctx &C, const Args &A) {
     const cs_prepared &P = *C.P;
     const double a = 0.0, b = P.romb_delta_b;
     const double dbeta = P.romb_dbeta;
@@ -482,6 +579,15 @@ __device__ inline double qromb_delta_cyl(const Ctx &C, const ChiArgs &A) {
         }
     }
     return pq;
+}
+
+// i0 = 4. Orientation cases outside 1..4 (the 0-based general case) reach no
+// branch of the chi integrand, which is then 0 at every node: every trapezoid
+// estimate is +0, the Neville extrapolation gives +0, and the reference's loop
+// stops at j = 5 on |I| < 1e-100 with +0. That value is returned directly.
+__device__ inline double qromb_delta_cyl(const Ctx &C, const ChiArgs &A) {
+    if (A.i1 < 1 || A.i1 > 4) return 0.0;
+    return qromb_delta(C, A);
 }
 
 // The same integral with the delta nodes of a level spread over the lanes of a
@@ -1265,6 +1371,29 @@ __device__ inline double calc_cube_none_iso(const Ctx &C, double qx, double qy, 
     return P.base + P.izero * (pq + P.iso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
 }
 
+// Transverse factor of the homogeneous disk (thickness 2 radius),
+// Source/sc_lib_formpq_partDisk.h:310-340: its series below 0.5 limq4, else
+// the closed form.
+__device__ inline double disk_cross(const cs_prepared &P, double q) {
+    const double zr = (1 - sqr(P.sigma)) / (sqr(P.sigma));
+    double pqr;
+    if (q < (0.5 * P.limq[4])) {
+        pqr = 1.0;
+        double oldpqsum = 0.0, qqnn = 1.0;
+        for (int nser = 1; nser <= 100; nser++) {
+            qqnn = qqnn * q * q;
+            pqr += P.carrp[3][nser] * qqnn;
+            if (series_converged(pqr, oldpqsum)) break;
+            oldpqsum = pqr;
+        }
+    } else {
+        const double argpq = q * P.radius / (zr + 1);
+        pqr = (1 / (2.0 * zr * (zr - 1))) * pow(argpq, -2) *
+              (1 - cos((zr - 1) * atan(2.0 * argpq)) / pow(1.0 + 4 * argpq * argpq, (zr - 1) / 2.0));
+    }
+    return pqr;
+}
+
 // formpq_partDisk, homogeneous disk, ordis 7 and 6 with its transverse part,
 // Source/sc_lib_formpq_partDisk.h:8-136 and :310-340. orcase is compared with
 // 1..4 as the reference compares it, although its enum is 0-based (1 = x
@@ -1274,9 +1403,8 @@ __device__ inline double calc_cube_none_iso(const Ctx &C, double qx, double qy, 
 // in the closed form; the preparation does not offer it.
 __device__ inline double formpq_disk(const cs_prepared &P, double limql, double qxs, double qys, double q, int ordis) {
     const double zl = (1 - sqr(P.sigmal)) / sqr(P.sigmal);
-    const double zr = (1 - sqr(P.sigma)) / (sqr(P.sigma));
     const double *c1 = P.carrp[0];
-    double pql = 0, pqr;
+    double pql = 0;
     if (ordis == 7) {
         if (q < (0.5 * P.limq[1])) {
             pql = 1.0;
@@ -1326,21 +1454,135 @@ __device__ inline double formpq_disk(const cs_prepared &P, double limql, double 
             pql = (4 / M_PI) * (pqr1 - pqr2 - (9 / 8.0) * pqr3);
         }
     }
-    if (q < (0.5 * P.limq[4])) {
+    return pql * disk_cross(P, q);
+}
+
+// Length factor of the homogeneous disk with the Gaussian orientation
+// distribution along an axis (formpq_partDisk ordis 0,
+// Source/sc_lib_formpq_partDisk.h:137-236; formfq_partDisk ordis 0,
+// Source/sc_lib_formfq_partDisk.h:136-324, with the F coefficients). Below
+// the switch value lim it is the triple series
+//   1 + sum_n c1[n] q^2n sum_m carr11pm[n][m] sum_l qxs^2l qys^2(m-l)
+// (carr22pm, the reference's inner weight, is 1 throughout); the inner sum
+// over l depends on m alone and is formed once per m, in the reference's
+// order, which leaves every rounding as it is. Above it, the delta/chi
+// quadrature of trapzdchid's disk case i1 = orcase + 7 (orcase compared with
+// 1..3 as the reference compares it) with the series coefficients c2,
+// divided by the distribution's norm.
+__device__ inline double disk_len_gauss(const Ctx &C, double qx, double qy, double qxs, double qys, double q,
+                                        const double *c1, const double *c2, double lim) {
+    const cs_prepared &P = *C.P;
+    if (q < lim) {
+        double qxn[121], qyn[121], bm[121];
+        double pql = 1.0, oldpqsum = 0.0, qqnn = 1.0;
+        qxn[0] = 1.0;
+        qyn[0] = 1.0;
+        bm[0] = 1.0;  // 0.0 + 1*1*1
+        for (int nser = 1; nser <= 120; nser++) {
+            qqnn = qqnn * q * q;
+            qxn[nser] = qxn[nser - 1] * qxs * qxs;
+            qyn[nser] = qyn[nser - 1] * qys * qys;
+            double b1 = 0.0;
+            for (int lser = 0; lser <= nser; lser++) b1 += qxn[lser] * qyn[nser - lser];
+            bm[nser] = b1;
+            double binsum = 0.0;
+            for (int mser = 0; mser <= nser; mser++) binsum += P.carr11pm[nser][mser] * bm[mser];
+            pql += c1[nser] * qqnn * binsum;
+            if (series_converged(pql, oldpqsum)) break;
+            oldpqsum = pql;
+        }
+        return pql;
+    }
+    const DiskChiArgs A = disk_chi_args(P, qx, qy, P.orcase + 7, c2);
+    return qromb_delta(C, A) / P.norm;
+}
+
+// P(q) of the Gaussian disk: x axis (1) switching at 6 limq1, y (2) and z (3)
+// at 6000 limq1
+__device__ inline double formpq_disk_gauss(const Ctx &C, double qx, double qy, double qxs, double qys, double q) {
+    const cs_prepared &P = *C.P;
+    const double lim = (P.orcase == 1 ? 6.0 : 6000.0) * P.limq[1];
+    return disk_len_gauss(C, qx, qy, qxs, qys, q, P.carrp[0], P.carrp[1], lim) * disk_cross(P, q);
+}
+
+// formfq_partDisk, homogeneous disk (cs 0), Source/sc_lib_formfq_partDisk.h:8-352:
+// the longitudinal factor from the F coefficients (carr1f, and carr2f in the
+// quadrature's series) and the switch point limq1f, times the square of the
+// transverse amplitude (series carr4f below 0.5 limq4f, else its closed
+// form). The z-direction closed form is the P(q) one, as in the reference.
+__device__ inline double formfq_disk(const Ctx &C, double qx, double qy, double qxs, double qys, double q) {
+    const cs_prepared &P = *C.P;
+    const double zl = (1 - sqr(P.sigmal)) / sqr(P.sigmal);
+    const double zr = (1 - sqr(P.sigma)) / (sqr(P.sigma));
+    const double *c1 = P.carrf[0];
+    double pql = 0, pqr;
+    if (P.ordis == 7) {
+        if (q < (0.5 * P.limqf[1])) {
+            pql = 1.0;
+            double oldpqsum = 0.0, qqnn = 1.0;
+            for (int nser = 1; nser <= 80; nser++) {
+                qqnn = qqnn * q * q;
+                pql += c1[nser] * qqnn;
+                if (series_converged(pql, oldpqsum)) break;
+                oldpqsum = pql;
+            }
+        } else {
+            const double arglq = q * P.length / (zl + 1);
+            pql = (2 / (zl * (zl - 1))) * pow(arglq, -2);
+        }
+    }
+    if (P.ordis == 6) {
+        if (q < (0.5 * P.limqf[1])) {
+            pql = 1.0;
+            double oldpqsum = 0.0, qqnn = 1.0;
+            const double w = P.orcase == 1 ? qxs + qys : (P.orcase == 2 ? qxs : qys);
+            for (int nser = 1; nser <= 120; nser++) {
+                qqnn = qqnn * q * q;
+                if (P.orcase == 4)
+                    pql += c1[nser] * qqnn;
+                else if (P.orcase >= 1 && P.orcase <= 3)
+                    pql += c1[nser] * qqnn * pow(1.0 - w * w, nser);
+                else
+                    break;
+                if (series_converged(pql, oldpqsum)) break;
+                oldpqsum = pql;
+            }
+        } else {
+            double arglq = 0;
+            if (P.orcase == 1) {
+                const double qnarg = qxs + qys;
+                arglq = sqrt(1.0 - qnarg * qnarg) * q * P.length / (zl + 1) + CS_EPS9;
+            }
+            if (P.orcase == 2) arglq = sqrt(1.0 - qxs * qxs) * q * P.length / (zl + 1) + CS_EPS9;
+            if (P.orcase == 3) arglq = sqrt(1.0 - qys * qys) * q * P.length / (zl + 1) + CS_EPS9;
+            if (P.orcase == 4) arglq = q * P.length / (zl + 1) + CS_EPS9;
+            const double pqr1 = (1 / (zl * (zl - 1) * (zl - 2))) * pow(arglq, -3);
+            const double pqr2 = (1 / (zl * (zl - 1) * (zl - 2))) * pow(arglq, -3) * sin((zl - 2) * atan(2.0 * arglq)) /
+                                pow(1.0 + 4 * arglq * arglq, (zl - 2) / 2.0);
+            const double pqr3 = (1 / (zl * (zl - 1) * (zl - 2) * (zl - 3))) * pow(arglq, -4) *
+                                cos((zl - 3) * atan(2.0 * arglq)) / pow(1.0 + 4 * arglq * arglq, (zl - 3) / 2.0);
+            pql = (4 / M_PI) * (pqr1 - pqr2 - (9 / 8.0) * pqr3);
+        }
+    }
+    if (P.ordis == 0) {
+        // x axis (1) switching at 1.2 limq1f, y (2) and z (3) at 0.9 limq1f
+        const double lim = (P.orcase == 1 ? 1.2 : 0.9) * P.limqf[1];
+        pql = disk_len_gauss(C, qx, qy, qxs, qys, q, c1, P.carrf[1], lim);
+    }
+    if (q < (0.5 * P.limqf[4])) {
         pqr = 1.0;
         double oldpqsum = 0.0, qqnn = 1.0;
-        for (int nser = 1; nser <= 100; nser++) {
+        for (int nser = 1; nser <= 120; nser++) {
             qqnn = qqnn * q * q;
-            pqr += P.carrp[3][nser] * qqnn;
+            pqr += P.carrf[3][nser] * qqnn;
             if (series_converged(pqr, oldpqsum)) break;
             oldpqsum = pqr;
         }
     } else {
         const double argpq = q * P.radius / (zr + 1);
-        pqr = (1 / (2.0 * zr * (zr - 1))) * pow(argpq, -2) *
-              (1 - cos((zr - 1) * atan(2.0 * argpq)) / pow(1.0 + 4 * argpq * argpq, (zr - 1) / 2.0));
+        pqr = (1 / zr) * pow(argpq, -1) * sin(zr * atan(argpq)) / pow(1.0 + argpq * argpq, zr / 2.0);
     }
-    return pql * pqr;
+    return pql * pqr * pqr;
 }
 
 // calc_GENERIC, Source/sc_gpu_generic.h:27-881, for the particles the
@@ -1406,16 +1648,41 @@ static __device__ __noinline__ double calc_generic(const Ctx &C, double qx, doub
                 break;
             }
         }
-    } else if (P.particle == 2) {  // disks, :173-225 (isotropic, or z-direction along an axis; no lattice)
-        if (P.ordis == 7) pq = formpq_disk(P, q, qx, qy, q, 7);
+    } else if (P.particle == 2) {  // disks, :173-265 (isotropic, z-direction or Gaussian along an axis)
+        if (P.ordis == 7) {
+            pq = formpq_disk(P, q, qx, qy, q, 7);
+            if (P.lattice) fq = formfq_disk(C, qx, qy, qx, qy, q);
+        }
         if (P.ordis == 6) {
             switch (P.orcase) {
-            case CS_ORC_XAXIS: pq = formpq_disk(P, fabs(qy), qx / q, 0, q, 6); break;
-            case CS_ORC_YAXIS: pq = formpq_disk(P, fabs(qx), 0, qy / q, q, 6); break;
-            case CS_ORC_ZAXIS: pq = formpq_disk(P, q, qx, qy, q, 6); break;
+            case CS_ORC_XAXIS:
+                pq = formpq_disk(P, fabs(qy), qx / q, 0, q, 6);
+                if (P.lattice) fq = formfq_disk(C, qx, qy, qx / q, 0, q);
+                break;
+            case CS_ORC_YAXIS:
+                pq = formpq_disk(P, fabs(qx), 0, qy / q, q, 6);
+                if (P.lattice) fq = formfq_disk(C, qx, qy, 0, qy / q, q);
+                break;
+            case CS_ORC_ZAXIS:
+                pq = formpq_disk(P, q, qx, qy, q, 6);
+                if (P.lattice) fq = formfq_disk(C, qx, qy, qx, qy, q);
+                break;
             }
         }
         pqiso = (P.iso > 0) ? formpq_disk(P, q, qx, qy, q, 7) : 0.0;
+        if (P.ordis == 0) {
+            switch (P.orcase) {
+            case CS_ORC_XAXIS:
+            case CS_ORC_YAXIS:
+                pq = formpq_disk_gauss(C, qx, qy, qx / q, qy / q, q);
+                if (P.lattice) fq = formfq_disk(C, qx, qy, qx / q, qy / q, q);
+                break;
+            case CS_ORC_ZAXIS:
+                pq = formpq_disk_gauss(C, qx, qy, qx, qy, q);
+                if (P.lattice) fq = formfq_disk(C, qx, qy, qx, qy, q);
+                break;
+            }
+        }
     } else if (P.particle == 3) {  // vesicles, :271-277
         pq = polyvesicle(P, q);
         fq = pq;

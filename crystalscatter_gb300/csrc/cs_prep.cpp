@@ -827,9 +827,106 @@ bool Prep::coefficients() {
         // sit in code the reference compiles out), so all of them equal the
         // i0 = 2 norm integral bit for bit. It is computed once.
         const double intl_const = qromb_delta_1d(1, 0, P.dbeta);
-        if (cdim != 1) supported = false;
+        if (cdim == 2) {
+            // homogeneous disks along an axis: x :6045-6130, y :6875-6960,
+            // z :7644-7730. The x and y blocks differ only in carr11pm (whose
+            // moment-based first assignment the reference overwrites at once);
+            // the z block leaves carr11pm at 1 and folds the delta moments into
+            // carr1p. The general orientation is not offered: the reference's
+            // disk P(q) has no branch for it and returns an uninitialised value.
+            if (P.cs != 0 || P.orcase == CS_ORC_GENERAL) {
+                supported = false;
+            } else {
+                double z12v[kNmax + 1];
+                z12v[0] = 1.0;
+                double xrn_n = 1.0;
+                long double xln_n = 1.0;
+                const int orc = P.orcase;
+                double carr2i[kNmax + 1];
+                if (orc == CS_ORC_ZAXIS) {
+                    carr2i[0] = 1;
+                    for (int n = 1; n <= nmax; n++) {
+                        fkv[n] = fkv[n - 1] * n;
+                        fk2v[n] = fk2v[n - 1] * (2 * n - 1) * (2 * n);
+                        carr2i[n] = std::pow(-1, n) * fk2v[n] * intl_const /
+                                    (std::pow(4.0, n) * fkv[n] * fkv[n] * fkv[n] * P.norm);
+                    }
+                }
+                for (int n = 1; n <= nmax; n++) {
+                    z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
+                    z12vl[n] = z12vl[n - 1] * ((zl + 1) - 2 + 2 * n) * ((zl + 1) - 1 + 2 * n);
+                    if (orc != CS_ORC_ZAXIS) {
+                        fkv[n] = fkv[n - 1] * n;
+                        fk2v[n] = fk2v[n - 1] * (2 * n - 1) * (2 * n);
+                    }
+                    gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
+                    xln_n = -xln_n * xl2z;
+                    xrn_n = -xrn_n * xr2z;
+                    double sump;
+                    if (orc == CS_ORC_ZAXIS) {
+                        sump = 0.0;
+                        for (int m = 0; m <= n; m++) sump += carr2i[m] / fkv[n - m];
+                        carr1p[n] = std::pow(4.0, n + 1) * gam3[n] * z12vl[n] * xln_n * sump /
+                                    (std::sqrt(M_PI) * (n + 2) * (n + 1) * (n + 1) * fkv[n] * fkv[n]);
+                        double sump1 = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            sump1 += z12vl[m] * z12vl[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                        carr1f[n] = xln_n * fkv[n] * sump1 * sump;
+                    } else {
+                        for (int m = 0; m <= n; m++) {
+                            if (orc == CS_ORC_XAXIS)
+                                P.carr11pm[n][m] = std::pow(-1, m) * fk2v[m] / (std::pow(4.0, m) * fkv[m] * fkv[n - m]);
+                            else
+                                P.carr11pm[n][m] = std::pow(-1, m) * fk2v[m] / (fkv[m] * fkv[n - m]);
+                        }
+                        carr1p[n] = std::pow(4.0, n + 1) * gam3[n] * z12vl[n] * xln_n /
+                                    (std::sqrt(M_PI) * (n + 2) * (n + 1) * (n + 1) * fkv[n] * fkv[n]);
+                        sump = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            sump += z12vl[m] * z12vl[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                        carr1f[n] = xln_n * fkv[n] * sump;
+                    }
+                    // cross-section
+                    carr4p[n] = std::pow(4.0, n) * std::sqrt(M_PI) * z12v[n] * xrn_n / (2.0 * (n + 1) * gam3[n] * fkv[n]);
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        sump += z12v[m] * z12v[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                    carr4f[n] = M_PI * xln_n * sump / 4.0;
+                    // the series of the orientation integral's Bessel approximation
+                    carr2p[n] = std::pow(4.0, n + 1) * gam3[n] * z12vl[n] * xln_n /
+                                (std::sqrt(M_PI) * (n + 2) * (n + 1) * (n + 1) * fkv[n] * fkv[n] * fkv[n]);
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        sump += z12vl[m] * z12vl[n - m] /
+                                ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                    carr2f[n] = std::sqrt(M_PI) * fkv[n] * xln_n * sump / (2.0 * gam3[n]);
+                    if (search1) {
+                        if (carr1p[n] < 1e-50) {
+                            n1 = n;
+                            search1 = false;
+                        }
+                    }
+                    if (search4) {
+                        if (carr4p[n] < 1e-50) {
+                            n4 = n;
+                            search4 = false;
+                        }
+                    }
+                    if (std::fabs(carr1f[n]) < kMin) {
+                        if (n < n1f) n1f = n;
+                    }
+                    if (std::fabs(carr4f[n]) < kMin) {
+                        if (n < n4f) n4f = n;
+                    }
+                }
+                intl = intl_const;
+                done = true;
+            }
+        } else if (cdim != 1) {
+            supported = false;
+        }
 
-        if (supported && P.orcase == CS_ORC_GENERAL) {
+        if (supported && cdim == 1 && P.orcase == CS_ORC_GENERAL) {
             // :4655-4760 (cylinder, homogeneous)
             P.polphi = 0;
             const double p11 = -std::cos(P.polphi * M_PI / 180.0) * std::cos(P.poltheta * M_PI / 180.0);
@@ -960,7 +1057,7 @@ bool Prep::coefficients() {
                 supported = false;
             }
         }
-        if (supported && P.orcase == CS_ORC_GENERAL) {
+        if (supported && cdim == 1 && P.orcase == CS_ORC_GENERAL) {
             // second general-orientation block, :5549-5617. Its qrombdeltac
             // loop (:5562-5569) discards every result and is not repeated.
             for (int n = 1; n <= 2 * nmax; n++) fkv[n] = fkv[n - 1] * n;
@@ -991,7 +1088,7 @@ bool Prep::coefficients() {
             }
             done = true;
         }
-        if (supported && (P.orcase == CS_ORC_XAXIS || P.orcase == CS_ORC_YAXIS || P.orcase == CS_ORC_ZAXIS)) {
+        if (supported && cdim == 1 && (P.orcase == CS_ORC_XAXIS || P.orcase == CS_ORC_YAXIS || P.orcase == CS_ORC_ZAXIS)) {
             // x-axis :5619-5692, y-axis :6453-6526, z-axis :7265-7331 (cylinder, homogeneous)
             if (P.cs != 0) {
                 supported = false;
@@ -1996,13 +2093,14 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
     }
 
     {
-        // limits and direction matrix of qrombdeltac for the cylinder
-        // orientation average (Source/sc_calc_generic_gpu.cu:1394-1434), with
+        // limits and direction matrix of qrombdeltac for the cylinder and disk
+        // orientation averages (Source/sc_calc_generic_gpu.cu:1394-1434), with
         // theta = polTheta and phi = 0 as formpq_partCylinder passes them
-        // (Source/sc_lib_formpq_partCylinder.h:207)
+        // (Source/sc_lib_formpq_partCylinder.h:207), phi = polPhi as
+        // formpq_partDisk does (Source/sc_lib_formpq_partDisk.h:183)
         const double dbeta = P.dbeta * M_PI / 180.0;
         const double theta = P.poltheta * M_PI / 180.0;
-        const double phi = 0 * M_PI / 180.0;
+        const double phi = (P.particle == 2 ? P.polphi : 0) * M_PI / 180.0;
         double delmax = dbeta * std::sqrt(std::log(1.0 / 0.00001));
         if (delmax > M_PI / 2.0) delmax = M_PI / 2.0;
         float blim = delmax;
@@ -2144,14 +2242,16 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
         // the generic pixel function covers the particles prepared above:
         // spheres, cylinders (z-direction, Gaussian orientation; isotropic,
         // homogeneous or core/shell), homogeneous
-        // isotropic cubes, z-direction disks along an axis without a lattice,
+        // isotropic cubes, homogeneous disks (isotropic, or z-direction or
+        // Gaussian along an axis),
         // isotropic or z-direction vesicles, and homogeneous isotropic
         // ellipsoids
         const bool ok = P.particle == 0 || (P.particle == 1 && (P.ordis == 6 || P.ordis == 0)) ||
                         (P.particle == 1 && P.ordis == 7 && (P.cs == 0 || P.cs == 1)) ||
                         (P.particle == 4 && P.ordis == 7 && P.cs == 0) ||
-                        (P.particle == 2 && P.ordis == 6 && P.cs == 0 && !P.lattice && P.orcase != CS_ORC_GENERAL) ||
-                        (P.particle == 2 && P.ordis == 7 && P.cs == 0 && !P.lattice) ||
+                        (P.particle == 2 && (P.ordis == 6 || P.ordis == 0) && P.cs == 0 &&
+                         P.orcase != CS_ORC_GENERAL) ||
+                        (P.particle == 2 && P.ordis == 7 && P.cs == 0) ||
                         (P.particle == 3 && (P.ordis == 7 || P.ordis == 6)) ||
                         (P.particle == 5 && P.ordis == 7 && P.cs == 0);
         if (!ok) {
@@ -2220,6 +2320,6 @@ void build_delta_table(double delta_b, double dbeta, cs_delta_node *tab) {
     }
 }
 
-bool needs_delta_table(const cs_prepared &P) { return P.ordis == 0 && P.part == 1; }
+bool needs_delta_table(const cs_prepared &P) { return P.ordis == 0 && (P.part == 1 || P.part == 2); }
 
 }  // namespace cs

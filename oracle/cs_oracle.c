@@ -354,8 +354,55 @@ static void polint(const double *xa, const double *ya, int n, double *y, double 
 typedef struct {
     double l, sigma, qx, qy;
     double p11, p12, p13, p21, p22, p23;
+    const CS_PDOUBLE_T *carr1; /* carr2p for the disk cases */
     int i1;
 } chid_args;
+
+/* disk P(q) integrand of trapzdchid (i1 = 8..11, i3 = 0) for the cosines and
+   sines of chi entering the two direction components: (c1, s1) the first,
+   (s2, c2) the second. Source/sc_calc_generic_gpu.cu:1849-2260 (interval
+   ends, where case 8 pairs cos(a) with sin(b) and sin(a) with cos(b)) and
+   2604-2840 (interior nodes). */
+static double disk_chid_value(const chid_args *A, double c1, double s1, double s2, double c2, double delta) {
+    const double eps = 0.0000000001;
+    const double sigma = A->sigma, qx = A->qx, qy = A->qy, l = A->l;
+    const double z = (1 - sigma * sigma) / (sigma * sigma);
+    const double qn = sqrt(qx * qx + qy * qy + eps);
+    const double qxl = qx / qn;
+    const double qyl = qy / qn;
+    double qnn;
+    if (A->i1 == 8) {
+        const double ml1 = A->p11 * c1 * NODE_SIN(delta) + A->p12 * s1 * NODE_SIN(delta) + A->p13 * NODE_COS(delta);
+        const double ml2 = A->p21 * s2 * NODE_SIN(delta) + A->p22 * c2 * NODE_SIN(delta) + A->p23 * NODE_COS(delta);
+        qnn = qxl * ml1 + qyl * ml2;
+    } else if (A->i1 == 9) {
+        qnn = qxl * NODE_COS(delta) - qyl * s1 * NODE_SIN(delta);
+    } else if (A->i1 == 10) {
+        qnn = qxl * s1 * NODE_SIN(delta) + qyl * NODE_COS(delta);
+    } else {
+        qnn = qxl * s1 * NODE_SIN(delta) - qyl * c1 * NODE_SIN(delta);
+    }
+    const double x = sqrt(1.0 - qnn * qnn + eps) * l * qn / (z + 1);
+    if (sigma < 0.15) {
+        if (x < 0.015) {
+            double px = 1, oldpx = 0, argser = 1;
+            for (int i = 1; i <= 50; i++) {
+                argser = argser * x * x / 4.0;
+                px = px + A->carr1[i] * argser;
+                const double delser = fabs((px - oldpx) / px);
+                if (delser < 0.0001) break;
+                oldpx = px;
+            }
+            return px;
+        }
+        const double px1 = (1 / (z * (z - 1) * (z - 2))) * pow(x, -3);
+        const double px2 = (1 / (z * (z - 1) * (z - 2))) * pow(x, -3) * sin((z - 2) * atan(2.0 * x)) / pow(1.0 + 4 * x * x, (z - 2) / 2.0);
+        const double px3 = (1 / (z * (z - 1) * (z - 2) * (z - 3))) * pow(x, -4) * cos((z - 3) * atan(2.0 * x)) / pow(1.0 + 4 * x * x, (z - 3) / 2.0);
+        return (4 / M_PI) * (px1 - px2 - (9 / 8.0) * px3);
+    }
+    const double px1 = (1 / (z * (z - 1) * (z - 2))) * pow(x, -3);
+    return 1 / (1.0 + M_PI / (4.0 * px1));
+}
 
 /* one trapzdchid integrand value, Source/sc_calc_generic_gpu.cu:1632-1734, 2455-2528 */
 static double chid_value(const chid_args *A, double x, double delta) {
@@ -373,6 +420,8 @@ static double chid_value(const chid_args *A, double x, double delta) {
         argx = (qx * NODE_SIN(x) * NODE_SIN(delta) + qy * NODE_COS(delta) + eps) * l / (z + 1);
     } else if (A->i1 == 4) {
         argx = (qx * NODE_SIN(x) * NODE_SIN(delta) - qy * NODE_COS(x) * NODE_SIN(delta) + eps) * l / (z + 1);
+    } else if (A->i1 >= 8 && A->i1 <= 11) {
+        return disk_chid_value(A, NODE_COS(x), NODE_SIN(x), NODE_SIN(x), NODE_COS(x), delta);
     } else {
         return 0.0; /* no branch of trapzdchid for this i1: the integrand stays 0 */
     }
@@ -383,7 +432,8 @@ static double chid_value(const chid_args *A, double x, double delta) {
 /* trapzdchid, Source/sc_calc_generic_gpu.cu:1590-2965 */
 static void trapzdchid(double a, double b, const chid_args *A, double delta, double *pq, int n, int *cnt) {
     if (n == 1) {
-        double pa = chid_value(A, a, delta);
+        double pa = A->i1 == 8 ? disk_chid_value(A, NODE_COS(a), NODE_SIN(b), NODE_SIN(a), NODE_COS(b), delta)
+                               : chid_value(A, a, delta);
         double pb = chid_value(A, b, delta);
         *pq = 0.5 * (b - a) * (pa + pb);
         *cnt = 1;
@@ -455,13 +505,23 @@ static void trapzddeltac4(double a, double b, double dbeta, const chid_args *A, 
 
 /* qrombdeltac(p1, sigma, alfa, theta, phi, qx, qy, qz, 9,9,9,9, i0=4, i1, 0,0,0, ...),
    Source/sc_calc_generic_gpu.cu:1370-1488 */
+static double qrombdeltac_carr(const cs_prepared *P, double sigma, double theta_deg, double phi_deg, double qx,
+                               double qy, int i1, const CS_PDOUBLE_T *carr1);
+
 static double qrombdeltac4(const cs_prepared *P, double sigma, double theta_deg, double phi_deg, double qx, double qy,
                            int i1) {
+    return qrombdeltac_carr(P, sigma, theta_deg, phi_deg, qx, qy, i1, P->carrp[1]);
+}
+
+/* the same with i0 = 6 (disk form factor), whose delta weighting is that of
+   i0 = 4 (:1104-1120) and whose chi integrand reads the series carr1 */
+static double qrombdeltac_carr(const cs_prepared *P, double sigma, double theta_deg, double phi_deg, double qx,
+                               double qy, int i1, const CS_PDOUBLE_T *carr1) {
 #ifdef CS_ORACLE_SKIP_ZERO_INTEGRAL
     /* operation-counting build only: an orientation case outside 1..4 has an
        identically zero integrand whose Romberg result is exactly +0; its
        (result-free) work is left out of the algorithmic operation count */
-    if (i1 < 1 || i1 > 4) return 0.0;
+    if ((i1 < 1 || i1 > 4) && (i1 < 8 || i1 > 11)) return 0.0;
 #endif
     const double eps = 1.0e-4;
     const int jmax = 20, k = 5;
@@ -494,6 +554,7 @@ static double qrombdeltac4(const cs_prepared *P, double sigma, double theta_deg,
     A.p21 = p21;
     A.p22 = p22;
     A.p23 = p23;
+    A.carr1 = carr1;
     A.i1 = i1;
     hp[1] = 1.0;
     for (int j = 1; j <= jmax; j++) {
@@ -709,6 +770,49 @@ static double formpq_partDisk_iso(const cs_prepared *P, double q) {
     return pql * pqr;
 }
 
+/* formpq_partDisk, homogeneous disk with the Gaussian orientation
+   distribution along an axis (ordis 0), Source/sc_lib_formpq_partDisk.h:137-236,
+   times its transverse part (:310-340). orcase is compared with 1..3 as the
+   reference compares it: the x axis switches to the quadrature at 6 limq1, the
+   y and z axes at 6000 limq1. */
+static double formpq_partDisk_gauss(const cs_prepared *P, double qx, double qy, double qxs, double qys, double q) {
+    const double zr = (1 - sqr(P->sigma)) / (sqr(P->sigma));
+    double pql, pqr;
+    if (q < ((P->orcase == 1 ? 6.0 : 6000.0) * P->limq[1])) {
+        double qxn[121], qyn[121];
+        double oldpqsum = 0.0, qqnn = 1.0;
+        pql = 1.0;
+        qxn[0] = 1.0;
+        qyn[0] = 1.0;
+        for (int nser = 1; nser <= 120; nser++) {
+            qqnn = qqnn * q * q;
+            qxn[nser] = qxn[nser - 1] * qxs * qxs;
+            qyn[nser] = qyn[nser - 1] * qys * qys;
+            double binsum = 0.0;
+            for (int mser = 0; mser <= nser; mser++) {
+                double binsum1 = 0.0;
+                for (int lser = 0; lser <= mser; lser++) binsum1 += 1.0 * qxn[lser] * qyn[mser - lser]; /* carr22pm = 1 */
+                binsum += P->carr11pm[nser][mser] * binsum1;
+            }
+            pql += P->carrp[0][nser] * qqnn * binsum;
+            const double delser = fabs((pql - oldpqsum) / pql);
+            if (delser < 0.0001) break;
+            oldpqsum = pql;
+        }
+    } else {
+        pql = qrombdeltac_carr(P, P->sigmal, P->poltheta, P->polphi, qx, qy, P->orcase + 7, P->carrp[1]);
+        pql = pql / P->norm;
+    }
+    if (q < (0.5 * P->limq[4])) {
+        pqr = series_q(P->carrp[3], q, 100);
+    } else {
+        const double argpq = q * P->radius / (zr + 1);
+        pqr = (1 / (2.0 * zr * (zr - 1))) * pow(argpq, -2) *
+              (1 - cos((zr - 1) * atan(2.0 * argpq)) / pow(1.0 + 4 * argpq * argpq, (zr - 1) / 2.0));
+    }
+    return pql * pqr;
+}
+
 /* formfq_partCylinder, Source/sc_lib_formfq_partCylinder.h:8-216 (ordis 0/6, cs 0) */
 static double formfq_partCylinder(const cs_prepared *P, double limql, double qxs, double qys, double q) {
     const double zl = (1 - sqr(P->sigmal)) / sqr(P->sigmal);
@@ -906,14 +1010,22 @@ double oracle_pixel_q(const cs_prepared *P, double qx, double qy, double qz) {
     }
     case CS_KEY_GENERIC:
         /* calc_GENERIC, Source/sc_gpu_generic.h:27-881, for the combinations
-           restated here: isotropic cylinders (cs 0/1) and isotropic
-           homogeneous disks, without a lattice (szq = szqiso = 1) */
+           restated here: isotropic cylinders (cs 0/1), isotropic homogeneous
+           disks and homogeneous disks with the Gaussian orientation along an
+           axis, without a lattice (szq = szqiso = 1) */
         if (P->particle == 1 && P->ordis == 7) {
             const double pq = formpq_partCylinder(P, qx, qy, q);
             return P->base + P->izero * (pq + P->iso * 1.0) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
         }
         if (P->particle == 2 && P->ordis == 7) {
             const double pq = formpq_partDisk_iso(P, q);
+            const double pqiso = (P->iso > 0) ? formpq_partDisk_iso(P, q) : (double)0.0;
+            return P->base + P->izero * (pq + P->iso * pqiso) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
+        }
+        if (P->particle == 2 && P->ordis == 0) {
+            /* :255-288, orcXaxis and orcYaxis pass qx/q, qy/q, orcZaxis qx, qy */
+            const double pq = P->orcase == 3 ? formpq_partDisk_gauss(P, qx, qy, qx, qy, q)
+                                             : formpq_partDisk_gauss(P, qx, qy, qx / q, qy / q, q);
             const double pqiso = (P->iso > 0) ? formpq_partDisk_iso(P, q) : (double)0.0;
             return P->base + P->izero * (pq + P->iso * pqiso) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
         }
@@ -933,8 +1045,10 @@ int oracle_supported(const cs_prepared *P) {
     case CS_KEY_CYL_GAUSS_BCT_ZDIR:
     case CS_KEY_CUBE_NONE_ISO: return 1;
     case CS_KEY_GENERIC:
-        return !P->lattice && P->ordis == 7 && ((P->particle == 1 && (P->cs == 0 || P->cs == 1)) ||
-                                                 (P->particle == 2 && P->cs == 0));
+        return !P->lattice && ((P->ordis == 7 && ((P->particle == 1 && (P->cs == 0 || P->cs == 1)) ||
+                                                  (P->particle == 2 && P->cs == 0))) ||
+                               (P->ordis == 0 && P->particle == 2 && P->cs == 0 && P->orcase >= 1 &&
+                                P->orcase <= 3));
     default: return 0;
     }
 }

@@ -34,8 +34,8 @@ sys.path.insert(0, ROOT)
 from crystalscatter_gb300 import configs as C  # noqa: E402
 from oracle import cpu_oracle, refbind  # noqa: E402
 
-ARRAYS = ["carr1p", "carr2p", "carr3p", "carr4p", "carr5p", "carr6p", "carr1f", "carr4f", "carr5f", "carr6f",
-          "carr11pm"]
+ARRAYS = ["carr1p", "carr2p", "carr3p", "carr4p", "carr5p", "carr6p", "carr1f", "carr2f", "carr4f", "carr5f",
+          "carr6f", "carr11pm"]
 SCALARS = ["limq1", "limq2", "limq3", "limq4", "limq5", "limq6", "limq1f", "limq4f", "norm", "order", "orcase",
            "peakmax1", "peakmax2", "latpar1", "latpar2", "latpar3", "newswitch"]
 
@@ -90,6 +90,23 @@ def image_cases():
     cases["disk_zdir_y_g32"] = dict(disk, phi=90.0, theta=90.0)
     cases["disk_zdir_z_iso_g32"] = dict(disk, phi=0.0, theta=0.0, iso=0.3)
     cases["disk_iso_g32"] = dict(disk, Ordis=7)
+    # Gaussian orientation along an axis: the x axis switches from the triple
+    # series to the delta/chi quadrature at 6 limq1, the y and z axes at
+    # 6000 limq1; SigmaL 0.2 takes the quadrature's Ornstein-Zernike-like form
+    dg24 = dict(C.scaled(C.CYL_GAUSS, 24), ComboBoxParticle=2, Ordis=0, EditRadius=2.0, Length=30.0)
+    dg16 = dict(C.scaled(C.CYL_GAUSS, 16), ComboBoxParticle=2, Ordis=0, EditRadius=2.0, Length=30.0)
+    cases["disk_gauss_x_g24"] = dict(dg24, phi=0.0, theta=90.0)
+    cases["disk_gauss_x_oz_g16"] = dict(dg16, phi=0.0, theta=90.0, SigmaL=0.2)
+    cases["disk_gauss_y_g24"] = dict(dg24, phi=90.0, theta=90.0)
+    cases["disk_gauss_z_g24"] = dict(dg24, phi=0.0, theta=0.0, iso=0.2)
+    cases["disk_gauss_z90_g16"] = dict(dg16, phi=90.0, theta=0.0)
+    # disks on lattices: F(q) from the F coefficients
+    dl = dict(sph, ComboBoxParticle=2, EditRadius=2.0, Length=12.0, SigmaL=0.1)
+    cases["disk_iso_fcc_g24"] = dict(dl, Ordis=7)
+    cases["disk_zdir_z_fcc_g24"] = dict(dl, Ordis=6, theta=0.0, phi=0.0)
+    cases["disk_gauss_x_fcc_g24"] = dict(dl, Ordis=0, theta=90.0, phi=0.0, EditDbeta=15.0)
+    cases["disk_zdir_y_bcc_g16"] = dict(C.scaled(C.SPHERE_FCC, 16), LType=4, ComboBoxParticle=2, EditRadius=2.0,
+                                        Length=12.0, SigmaL=0.1, Ordis=6, theta=90.0, phi=90.0)
     ves = dict(C.scaled(C.SPHERE, 32), ComboBoxParticle=3, Length=14.0, SigmaL=0.15)
     cases["vesicle_iso_g32"] = dict(ves, iso=0.2)
     cases["vesicle_zdir_g32"] = dict(ves, Ordis=6)

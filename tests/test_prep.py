@@ -34,8 +34,8 @@ def _skipped(case, name):
     return no_lattice and p.get("ComboBoxParticle") == 1 and p.get("Ordis", 0) == 0 and name in F_ONLY_LATTICE
 
 ARR = {"carr1p": ("carrp", 0), "carr2p": ("carrp", 1), "carr3p": ("carrp", 2), "carr4p": ("carrp", 3),
-       "carr5p": ("carrp", 4), "carr6p": ("carrp", 5), "carr1f": ("carrf", 0), "carr4f": ("carrf", 3),
-       "carr5f": ("carrf", 4), "carr6f": ("carrf", 5)}
+       "carr5p": ("carrp", 4), "carr6p": ("carrp", 5), "carr1f": ("carrf", 0), "carr2f": ("carrf", 1),
+       "carr4f": ("carrf", 3), "carr5f": ("carrf", 4), "carr6f": ("carrf", 5)}
 
 
 def _close(a, b, rtol):
@@ -55,8 +55,8 @@ def test_prepared_constants_match_reference(name):
     rc, P, msg = prepared.prepare(p, 0, case["ign_cbs"])
     assert rc == 0, msg
     for a, (field, k) in ARR.items():
-        if _skipped(case, a):
-            continue
+        if _skipped(case, a) or a not in g:
+            continue  # (carr2f is stored for the cases whose pixel function reads it)
         ours = np.array(getattr(P, field)[k][:])
         assert _close(g[a], ours, 1e-15), a
     ours11 = np.array(P.carr11pm).reshape(131, 131)
