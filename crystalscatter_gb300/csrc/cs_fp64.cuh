@@ -1371,10 +1371,51 @@ __device__ inline double calc_cube_none_iso(const Ctx &C, double qx, double qy, 
     return P.base + P.izero * (pq + P.iso) + P.ifluc / (1 + q * q * P.rfluc * P.rfluc);
 }
 
-// Transverse factor of the homogeneous disk (thickness 2 radius),
-// Source/sc_lib_formpq_partDisk.h:310-340: its series below 0.5 limq4, else
-// the closed form.
+// Transverse factor of the core/shell disk, F121 + F122 + F123
+// (Source/sc_lib_formpq_partDisk.h:344-420): core, cross and shell terms,
+// each its series (carr4p/5p/6p) below its switch point or its closed form.
+__device__ inline double disk_cross_coreshell(const cs_prepared &P, double q) {
+    const double zr = (1 - sqr(P.sigma)) / (sqr(P.sigma));
+    const double radiusm = P.radius / P.p1;
+    const double ccc1 = sqr(1 - P.rho) * pow(P.p1, 2);
+    const double ccc2 = 2 * P.rho * (1 - P.rho) * pow(P.p1, 1);
+    const double ccc3 = P.rho * P.rho;
+    const double vv3 = sqr((1 - P.rho) * pow(P.p1, 1) + P.rho);
+    const double argq = q * radiusm / (zr + 1);
+    const double argpq = q * P.radius / (zr + 1);
+    double F121, F122, F123;
+    if (q < (0.8 * P.limq[4])) {
+        F121 = ccc1 * series_q(P.carrp[3], q, 120) / vv3;
+    } else {
+        const double pqr = (1 / (2.0 * zr * (zr - 1))) * pow(argpq, -2) *
+                           (1 - cos((zr - 1) * atan(2.0 * argpq)) / pow(1.0 + 4 * argpq * argpq, (zr - 1) / 2.0));
+        F121 = ccc1 * pqr / vv3;
+    }
+    if (q < (2.0 * P.limq[5])) {
+        F122 = ccc2 * series_q(P.carrp[4], q, 120) / vv3;
+    } else {
+        const double argbm = (zr + 1) * atan(argpq - argq);
+        const double nenbm = pow(1.0 + 4 * sqr(argpq - argq), (zr + 1) / 2.0);
+        const double argbp = (zr + 1) * atan(argpq + argq);
+        const double nenbp = pow(1.0 + 4 * sqr(argpq + argq), (zr + 1) / 2.0);
+        const double pqr = (1 / (2.0 * zr * (zr - 1) * (zr - 2) * argpq * argq)) * (cos(argbm) / nenbm - cos(argbp) / nenbp);
+        F122 = ccc2 * pqr / vv3;
+    }
+    if (q < (0.3 * P.limq[6])) {
+        F123 = ccc3 * series_q(P.carrp[5], q, 120) / vv3;
+    } else {
+        const double pqr = (1 / (2.0 * zr * (zr - 1))) * pow(argq, -2) *
+                           (1 - cos((zr - 1) * atan(2.0 * argq)) / pow(1.0 + 4 * argq * argq, (zr - 1) / 2.0));
+        F123 = ccc3 * pqr / vv3;
+    }
+    return F121 + F122 + F123;
+}
+
+// Transverse factor of the disk (thickness 2 radius): homogeneous,
+// Source/sc_lib_formpq_partDisk.h:310-340, its series below 0.5 limq4, else
+// the closed form; core/shell above.
 __device__ inline double disk_cross(const cs_prepared &P, double q) {
+    if (P.cs == 1) return disk_cross_coreshell(P, q);
     const double zr = (1 - sqr(P.sigma)) / (sqr(P.sigma));
     double pqr;
     if (q < (0.5 * P.limq[4])) {
@@ -1505,11 +1546,13 @@ __device__ inline double formpq_disk_gauss(const Ctx &C, double qx, double qy, d
     return disk_len_gauss(C, qx, qy, qxs, qys, q, P.carrp[0], P.carrp[1], lim) * disk_cross(P, q);
 }
 
-// formfq_partDisk, homogeneous disk (cs 0), Source/sc_lib_formfq_partDisk.h:8-352:
-// the longitudinal factor from the F coefficients (carr1f, and carr2f in the
-// quadrature's series) and the switch point limq1f, times the square of the
-// transverse amplitude (series carr4f below 0.5 limq4f, else its closed
-// form). The z-direction closed form is the P(q) one, as in the reference.
+// formfq_partDisk, homogeneous and core/shell disks (cs 0/1),
+// Source/sc_lib_formfq_partDisk.h:8-441: the longitudinal factor from the F
+// coefficients (carr1f, and carr2f in the quadrature's series) and the switch
+// point limq1f, times the square of the transverse amplitude (homogeneous:
+// series carr4f below 0.5 limq4f, else its closed form) or the core/shell
+// sum of products of amplitudes. The z-direction closed form is the P(q)
+// one, as in the reference.
 __device__ inline double formfq_disk(const Ctx &C, double qx, double qy, double qxs, double qys, double q) {
     const cs_prepared &P = *C.P;
     const double zl = (1 - sqr(P.sigmal)) / sqr(P.sigmal);
@@ -1568,6 +1611,37 @@ __device__ inline double formfq_disk(const Ctx &C, double qx, double qy, double 
         // x axis (1) switching at 1.2 limq1f, y (2) and z (3) at 0.9 limq1f
         const double lim = (P.orcase == 1 ? 1.2 : 0.9) * P.limqf[1];
         pql = disk_len_gauss(C, qx, qy, qxs, qys, q, c1, P.carrf[1], lim);
+    }
+    if (P.cs == 1) {
+        // core/shell, :355-441: core, cross and shell amplitudes
+        const double radiusm = P.radius / P.p1;
+        const double ccc1 = sqr(1 - P.rho) * pow(P.p1, 2);
+        const double ccc2 = 2 * P.rho * (1 - P.rho) * pow(P.p1, 1);
+        const double ccc3 = sqr(P.rho);
+        const double vv3 = sqr((1 - P.rho) * pow(P.p1, 1) + P.rho);
+        const double argq = q * radiusm / (zr + 1);
+        const double argpq = q * P.radius / (zr + 1);
+        double F121, F122, F123;
+        if (q < (0.8 * P.limqf[4])) {
+            F121 = ccc1 * series_q(P.carrf[3], q, 120) / vv3;
+        } else {
+            const double a = (1 / zr) * pow(argpq, -1) * sin(zr * atan(argpq)) / pow(1.0 + argpq * argpq, zr / 2.0);
+            F121 = ccc1 * a * a / vv3;
+        }
+        if (q < (1.0 * P.limqf[5])) {
+            F122 = ccc2 * series_q(P.carrf[4], q, 120) / vv3;
+        } else {
+            const double a = (1 / zr) * pow(argpq, -1) * sin(zr * atan(argpq)) / pow(1.0 + argpq * argpq, zr / 2.0);
+            const double a1 = (1 / zr) * pow(argq, -1) * sin(zr * atan(argq)) / pow(1.0 + argq * argq, zr / 2.0);
+            F122 = ccc2 * a * a1 / vv3;
+        }
+        if (q < (0.3 * P.limqf[6])) {
+            F123 = ccc3 * series_q(P.carrf[5], q, 120) / vv3;
+        } else {
+            const double a = (1 / zr) * pow(argq, -1) * sin(zr * atan(argq)) / pow(1.0 + argq * argq, zr / 2.0);
+            F123 = ccc3 * a * a / vv3;
+        }
+        return pql * (F121 + F122 + F123);
     }
     if (q < (0.5 * P.limqf[4])) {
         pqr = 1.0;

@@ -813,6 +813,91 @@ bool Prep::coefficients() {
                 }
             }
             done = true;
+        } else if (P.cs == 1 && (cdim == 1 || cdim == 2)) {
+            // core/shell, :4213-4361: core (carr4), cross (carr5) and shell
+            // (carr6) terms of the cross-section
+            double xrmn_n = 1.0;
+            double xrn_n = 1.0;
+            for (int n = 1; n <= nmax; n++) {
+                z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
+                z12vl[n] = z12vl[n - 1] * ((zl + 1) - 2 + 2 * n) * ((zl + 1) - 1 + 2 * n);
+                fkv[n] = fkv[n - 1] * n;
+                fk2v[n] = fk2v[n - 1] * (2 * n - 1) * (2 * n);
+                gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
+                xln_n = -xln_n * xl2z;
+                xrn_n = -xrn_n * xr2z;
+                xrmn_n = -xrmn_n * xrm2z;
+                pn[n] = pn[n - 1] * p * p;
+                double sump;
+                if (cdim == 1) {
+                    carr1p[n] = std::sqrt(M_PI) * std::pow(4.0, n) * z12vl[n] * xln_n / (2.0 * (n + 1) * gam3[n] * fkv[n]);
+                    carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
+                                ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n] * fkv[n]);
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++) sump += pn[m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                    carr5p[n] = z12v[n] * xrmn_n * sump;
+                    carr6p[n] = carr4p[n] / pn[n];
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        sump += z12vl[m] * z12vl[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                    carr1f[n] = M_PI * xln_n * sump / 4.0;
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        sump += z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                    carr4f[n] = xrn_n * sump;
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        sump += pn[m] * z12v[m] * z12v[n - m] /
+                                ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                    carr5f[n] = xrmn_n * sump;
+                    carr6f[n] = carr4f[n] / pn[n];
+                } else {
+                    carr1p[n] = std::pow(4.0, n + 1) * gam3[n] * z12vl[n] * xln_n /
+                                (std::sqrt(M_PI) * (n + 2) * (n + 1) * (n + 1) * fkv[n] * fkv[n] * fkv[n]);
+                    carr4p[n] = std::pow(4.0, n) * std::sqrt(M_PI) * z12v[n] * xrn_n / (2.0 * (n + 1) * gam3[n] * fkv[n]);
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++) sump += pn[m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                    carr5p[n] = M_PI * z12v[n] * xrmn_n * sump / 4.0;
+                    carr6p[n] = carr4p[n] / pn[n];
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        sump += z12vl[m] * z12vl[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                    carr1f[n] = std::sqrt(M_PI) * fkv[n] * xln_n * sump / (2.0 * gam3[n]);
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++) sump += z12v[m] * z12v[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                    carr4f[n] = M_PI * xrn_n * sump / 4.0;
+                    sump = 0.0;
+                    for (int m = 0; m <= n; m++)
+                        sump += pn[m] * z12v[m] * z12v[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                    carr5f[n] = M_PI * xrmn_n * sump / 4.0;
+                    carr6f[n] = carr4f[n] / pn[n];
+                }
+                if (std::fabs(carr1p[n]) < kMin) {
+                    if (n < n1) n1 = n;
+                }
+                if (std::fabs(carr4p[n]) < kMin) {
+                    if (n < n4) n4 = n;
+                }
+                if (std::fabs(carr5p[n]) < kMin) {
+                    if (n < n5) n5 = n;
+                }
+                if (std::fabs(carr6p[n]) < kMin) {
+                    if (n < n6) n6 = n;
+                }
+                if (std::fabs(carr1f[n]) < kMin) {
+                    if (n < n1f) n1f = n;
+                }
+                if (std::fabs(carr4f[n]) < kMin) {
+                    if (n < n4f) n4f = n;
+                }
+                if (std::fabs(carr5f[n]) < kMin) {
+                    if (n < n5f) n5f = n;
+                }
+                if (std::fabs(carr6f[n]) < kMin) {
+                    if (n < n6f) n6f = n;
+                }
+            }
+            done = true;
         } else {
             supported = false;
         }
@@ -927,7 +1012,8 @@ bool Prep::coefficients() {
         }
 
         if (supported && cdim == 1 && P.orcase == CS_ORC_GENERAL) {
-            // :4655-4760 (cylinder, homogeneous)
+            // :4655-4760 (cylinder, homogeneous) and :4763-4889 (core/shell:
+            // the same carr11pm and length coefficients, its own cross-section)
             P.polphi = 0;
             const double p11 = -std::cos(P.polphi * M_PI / 180.0) * std::cos(P.poltheta * M_PI / 180.0);
             const double p13 = std::cos(P.polphi * M_PI / 180.0) * std::sin(P.poltheta * M_PI / 180.0);
@@ -941,7 +1027,9 @@ bool Prep::coefficients() {
                 pw4[e] = std::pow(4.0, e);
                 pw21[e] = std::pow(sqr(p21), e);
             }
-            if (P.cs == 0) {
+            if (P.cs == 0 || P.cs == 1) {
+                const bool cs1 = P.cs == 1;
+                bool search5 = true, search6 = true;
                 double z12v[kNmax + 1];
                 z12v[0] = 1.0;
                 double xrn_n = 1.0;
@@ -962,7 +1050,8 @@ bool Prep::coefficients() {
                 // recurrences (serial), then the rows of every n (parallel),
                 // then the searches over n (serial)
                 long double xln[kNmax + 1];
-                double xrn[kNmax + 1];
+                double xrn[kNmax + 1], xrmn[kNmax + 1];
+                double xrmn_n = 1.0;
                 for (int n = 1; n <= nmax; n++) {
                     z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
                     z12vl[n] = z12vl[n - 1] * ((zl + 1) - 2 + 2 * n) * ((zl + 1) - 1 + 2 * n);
@@ -975,6 +1064,11 @@ bool Prep::coefficients() {
                     xrn_n = -xrn_n * xr2z;
                     xln[n] = xln_n;
                     xrn[n] = xrn_n;
+                    if (cs1) {
+                        xrmn_n = -xrmn_n * xrm2z;
+                        xrmn[n] = xrmn_n;
+                        pn[n] = pn[n - 1] * p * p;
+                    }
                 }
                 // pw11/pw13 are powers of numbers <= 1: once a power underflows
                 // to 0 all higher ones are 0, and so is every numerator that
@@ -1022,14 +1116,36 @@ bool Prep::coefficients() {
                         carr1f[n] = fk2v[n] * xln_n * sump / (std::pow(4.0, n));
                     }
                     carr2f[n] = carr2p[n];
-                    carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
-                                ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n]);
-                    if (need_f) {
+                    if (!cs1) {
+                        carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
+                                    ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n]);
+                        if (need_f) {
+                            double sump = 0.0;
+                            for (int m = 0; m <= n; m++)
+                                sump = sump + z12v[m] * z12v[n - m] /
+                                                  ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                            carr4f[n] = xrn_n * sump;
+                        }
+                    } else {
+                        // core (carr4), cross (carr5) and shell (carr6) terms
+                        const double xrmn_n = xrmn[n];
+                        carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
+                                    ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n] * fkv[n]);
                         double sump = 0.0;
-                        for (int m = 0; m <= n; m++)
-                            sump = sump + z12v[m] * z12v[n - m] /
-                                              ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
-                        carr4f[n] = xrn_n * sump;
+                        for (int m = 0; m <= n; m++) sump += pn[m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                        carr5p[n] = z12v[n] * xrmn_n * sump;
+                        carr6p[n] = carr4p[n] / pn[n];
+                        if (need_f) {
+                            sump = 0.0;
+                            for (int m = 0; m <= n; m++)
+                                sump += z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                            carr4f[n] = xrn_n * sump;
+                            sump = 0.0;
+                            for (int m = 0; m <= n; m++)
+                                sump += pn[m] * z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                            carr5f[n] = xrmn_n * sump;
+                            carr6f[n] = carr4f[n] / pn[n];
+                        }
                     }
                 });
                 for (int n = 1; n <= nmax; n++) {
@@ -1045,11 +1161,29 @@ bool Prep::coefficients() {
                             search4 = false;
                         }
                     }
+                    if (cs1 && search5) {
+                        if (carr5p[n] < 1e-50) {
+                            n5 = n;
+                            search5 = false;
+                        }
+                    }
+                    if (cs1 && search6) {
+                        if (carr6p[n] < 1e-50) {
+                            n6 = n;
+                            search6 = false;
+                        }
+                    }
                     if (std::fabs(carr1f[n]) < kMin) {
                         if (n < n1f) n1f = n;
                     }
                     if (std::fabs(carr4f[n]) < kMin) {
                         if (n < n4f) n4f = n;
+                    }
+                    if (cs1 && std::fabs(carr5f[n]) < kMin) {
+                        if (n < n5f) n5f = n;
+                    }
+                    if (cs1 && std::fabs(carr6f[n]) < kMin) {
+                        if (n < n6f) n6f = n;
                     }
                 }
                 done = true;
@@ -1089,10 +1223,16 @@ bool Prep::coefficients() {
             done = true;
         }
         if (supported && cdim == 1 && (P.orcase == CS_ORC_XAXIS || P.orcase == CS_ORC_YAXIS || P.orcase == CS_ORC_ZAXIS)) {
-            // x-axis :5619-5692, y-axis :6453-6526, z-axis :7265-7331 (cylinder, homogeneous)
-            if (P.cs != 0) {
+            // x-axis :5619-5692, y-axis :6453-6526, z-axis :7265-7331 (cylinder,
+            // homogeneous); core/shell :5696-5817, :6530-6649, :7335-7447 (the
+            // same length coefficients but for the x axis's z12vl, which uses
+            // zl there, and the z axis's carr1f, divided by 4^(n+1); its own
+            // cross-section)
+            if (P.cs != 0 && P.cs != 1) {
                 supported = false;
             } else {
+                const bool cs1 = P.cs == 1;
+                bool search5 = true, search6 = true;
                 double z12v[kNmax + 1];
                 z12v[0] = 1.0;
                 double xrn_n = 1.0;
@@ -1100,10 +1240,11 @@ bool Prep::coefficients() {
                 const int orc = P.orcase;
                 // recurrences (serial), rows of every n (parallel), searches (serial)
                 long double xln[kNmax + 1];
-                double xrn[kNmax + 1];
+                double xrn[kNmax + 1], xrmn[kNmax + 1];
+                double xrmn_n = 1.0;
                 for (int n = 1; n <= nmax; n++) {
                     z12v[n] = z12v[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);
-                    if (orc == CS_ORC_XAXIS)
+                    if (orc == CS_ORC_XAXIS && !cs1)
                         z12vl[n] = z12vl[n - 1] * ((z + 1) - 2 + 2 * n) * ((z + 1) - 1 + 2 * n);  // uses z, :5636
                     else
                         z12vl[n] = z12vl[n - 1] * ((zl + 1) - 2 + 2 * n) * ((zl + 1) - 1 + 2 * n);
@@ -1114,6 +1255,11 @@ bool Prep::coefficients() {
                     xrn_n = -xrn_n * xr2z;
                     xln[n] = xln_n;
                     xrn[n] = xrn_n;
+                    if (cs1) {
+                        xrmn_n = -xrmn_n * xrm2z;
+                        xrmn[n] = xrmn_n;
+                        pn[n] = pn[n - 1] * p * p;
+                    }
                 }
                 const double intl_v = intl_const;  // every qrombdeltac moment of these blocks
                 parallel_n(1, nmax, [&](int n) {
@@ -1141,14 +1287,35 @@ bool Prep::coefficients() {
                         sump = 0.0;
                         for (int m = 0; m <= n; m++)
                             sump += z12vl[m] * z12vl[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
-                        carr1f[n] = fk2v[n] * xln_n * sump * intl_v / (std::pow(4.0, n) * fkv[n] * fkv[n] * P.norm);
+                        carr1f[n] = fk2v[n] * xln_n * sump * intl_v /
+                                    (std::pow(4.0, cs1 ? n + 1 : n) * fkv[n] * fkv[n] * P.norm);
                     }
-                    carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
-                                ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n]);
-                    sump = 0.0;
-                    for (int m = 0; m <= n; m++)
-                        sump = sump + z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
-                    carr4f[n] = xrn_n * sump;
+                    if (!cs1) {
+                        carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
+                                    ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n]);
+                        sump = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            sump = sump + z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m] * fkv[m] * fkv[n - m]);
+                        carr4f[n] = xrn_n * sump;
+                    } else {
+                        // core (carr4), cross (carr5) and shell (carr6) terms
+                        const double xrmn_n = xrmn[n];
+                        carr4p[n] = 4 * (n + 1 / 2.0) * fk2v[n] * z12v[n] * xrn_n /
+                                    ((n + 2) * (n + 1) * fkv[n] * fkv[n] * (n + 1) * fkv[n] * fkv[n]);
+                        sump = 0.0;
+                        for (int m = 0; m <= n; m++) sump = sump + pn[m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                        carr5p[n] = z12v[n] * xrmn_n * sump;
+                        carr6p[n] = carr4p[n] / pn[n];
+                        sump = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            sump = sump + z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                        carr4f[n] = xrn_n * sump;
+                        sump = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            sump = sump + pn[m] * z12v[m] * z12v[n - m] / ((m + 1) * fkv[m] * (n - m + 1) * fkv[n - m]);
+                        carr5f[n] = xrmn_n * sump;
+                        carr6f[n] = carr4f[n] / pn[n];
+                    }
                 });
                 intl = intl_v;
                 for (int n = 1; n <= nmax; n++) {
@@ -1164,11 +1331,29 @@ bool Prep::coefficients() {
                             search4 = false;
                         }
                     }
+                    if (cs1 && search5) {
+                        if (carr5p[n] < 1e-50) {
+                            n5 = n;
+                            search5 = false;
+                        }
+                    }
+                    if (cs1 && search6) {
+                        if (carr6p[n] < 1e-50) {
+                            n6 = n;
+                            search6 = false;
+                        }
+                    }
                     if (std::fabs(carr1f[n]) < kMin) {
                         if (n < n1f) n1f = n;
                     }
                     if (std::fabs(carr4f[n]) < kMin) {
                         if (n < n4f) n4f = n;
+                    }
+                    if (cs1 && std::fabs(carr5f[n]) < kMin) {
+                        if (n < n5f) n5f = n;
+                    }
+                    if (cs1 && std::fabs(carr6f[n]) < kMin) {
+                        if (n < n6f) n6f = n;
                     }
                 }
                 done = true;
@@ -2242,16 +2427,18 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
         // the generic pixel function covers the particles prepared above:
         // spheres, cylinders (z-direction, Gaussian orientation; isotropic,
         // homogeneous or core/shell), homogeneous
-        // isotropic cubes, homogeneous disks (isotropic, or z-direction or
-        // Gaussian along an axis),
+        // isotropic cubes, disks (isotropic or z-direction along an axis,
+        // homogeneous or core/shell; homogeneous with the Gaussian orientation
+        // along an axis),
         // isotropic or z-direction vesicles, and homogeneous isotropic
         // ellipsoids
         const bool ok = P.particle == 0 || (P.particle == 1 && (P.ordis == 6 || P.ordis == 0)) ||
                         (P.particle == 1 && P.ordis == 7 && (P.cs == 0 || P.cs == 1)) ||
                         (P.particle == 4 && P.ordis == 7 && P.cs == 0) ||
-                        (P.particle == 2 && (P.ordis == 6 || P.ordis == 0) && P.cs == 0 &&
+                        (P.particle == 2 && P.ordis == 6 && (P.cs == 0 || P.cs == 1) &&
                          P.orcase != CS_ORC_GENERAL) ||
-                        (P.particle == 2 && P.ordis == 7 && P.cs == 0) ||
+                        (P.particle == 2 && P.ordis == 0 && P.cs == 0 && P.orcase != CS_ORC_GENERAL) ||
+                        (P.particle == 2 && P.ordis == 7 && (P.cs == 0 || P.cs == 1)) ||
                         (P.particle == 3 && (P.ordis == 7 || P.ordis == 6)) ||
                         (P.particle == 5 && P.ordis == 7 && P.cs == 0);
         if (!ok) {

@@ -23,7 +23,7 @@ UNINIT_F = {"carr4f", "limq4f"}
 
 # The orientation-averaged cylinder's F(q) coefficients are formed only for
 # lattices, the only pixel functions that read them.
-F_ONLY_LATTICE = {"carr1f", "carr4f", "limq1f", "limq4f"}
+F_ONLY_LATTICE = {"carr1f", "carr2f", "carr4f", "carr5f", "carr6f", "limq1f", "limq4f"}
 
 
 def _skipped(case, name):
