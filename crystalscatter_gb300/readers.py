@@ -15,6 +15,11 @@ the same layout and metadata keys, so that a target can go straight to
 * the beam-stop centre finder (``SC_ReadData::findBeamCenter``,
   ``Source/sc_readdata.cpp:878-1010``).
 
+Numbers are parsed as Qt's ``QString::toDouble``/``toInt`` parse them (the
+whole text, else 0). Every reader is pinned to the reference's own readers,
+compiled from ``Source/sc_readdata.cpp`` with Qt stand-ins, on committed
+input files (``tests/test_readers_ref.py``).
+
 An image is returned as :class:`Image`: ``data`` has shape (rows, cols) =
 (maxY - minY, maxX - minX), row y holds x = minX .. maxX - 1 (the order of
 the files and of ``setFitData``), and ``meta`` holds the metadata strings
@@ -22,6 +27,7 @@ under the reference's keys.
 """
 import math
 import os
+import re
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -49,6 +55,22 @@ class Image:
         return self.data[y - self.minY, x - self.minX]
 
 
+_QT_NUMBER = re.compile(r"[+-]?(\d+\.?\d*|\.\d+)([eE][+-]?\d+)?|[+-]?(inf|nan)")
+
+
+def _qt_double(text):
+    """QString::toDouble: the whole text (white space around it allowed) as a
+    number, else 0."""
+    t = text.strip()
+    return float(t) if _QT_NUMBER.fullmatch(t) else 0.0
+
+
+def _qt_int(text):
+    """QString::toInt: the whole text as a decimal integer, else 0."""
+    t = text.strip()
+    return int(t) if re.fullmatch(r"[+-]?\d+", t) else 0
+
+
 def _base(path):
     root, _ = os.path.splitext(path)
     return root
@@ -74,11 +96,11 @@ def read_sascrystal_csv(path):
             if len(sl) < 2:
                 continue
             if sl[0] == "X:":
-                ncols = int(sl[2]) - int(sl[1])
+                ncols = _qt_int(sl[2]) - _qt_int(sl[1])
             elif sl[0] == "Y:":
-                nrows = int(sl[2]) - int(sl[1])
+                nrows = _qt_int(sl[2]) - _qt_int(sl[1])
             elif sl[0].startswith("Y=") and len(sl) > ncols:
-                vals.extend(float(t) for t in sl[1:])
+                vals.extend(_qt_double(t) for t in sl[1:])
     data = np.asarray(vals, dtype=np.float64)
     if data.size != nrows * ncols:
         raise ValueError(f"{fncsv}: {data.size} values for {nrows} x {ncols}")
@@ -200,7 +222,7 @@ def read_kws(path):
             elif look_lambda and "lambda=" in line:
                 look_lambda = False
                 rest = line[line.index("lambda=") + 7:]
-                wl = float(rest[:-1].strip())
+                wl = _qt_double(rest[:-1])  # the unit's last letter cut off; "0.45nm" reads as 0
                 if rest.endswith("A"):
                     wl = wl / 10
                 wavelen = f"{wl:g} nm"
@@ -221,7 +243,7 @@ def read_kws(path):
         sl = line.split()
         if len(sl) < 8:
             continue
-        vals.extend(max(float(t), 0.0) for t in sl)
+        vals.extend(max(_qt_double(t), 0.0) for t in sl)
     if len(vals) not in _KWS_SIZES:
         raise ValueError(f"{path}: {len(vals)} values, not a 128², 144² or 256² detector")
     n, beam = _KWS_SIZES[len(vals)]
@@ -261,7 +283,8 @@ def read_edf(path):
 
     ``EDF_DataFormatVersion`` headers are not read (None), as in the
     reference. Types: 32-bit float and signed integer, 16-bit unsigned, 64-bit
-    float, in either byte order. Pixel k of the file (row r = k / Dim_1,
+    float; both byte orders are read as little-endian, as the reference's
+    byte swap leaves the bytes as they are. Pixel k of the file (row r = k / Dim_1,
     column c = k % Dim_1) lands at x = rows - 1 - r, y = c, the reference's
     layout, which is defined for square detectors (others raise
     ValueError). Each record is read once; the reference's loops for the types
@@ -306,10 +329,7 @@ def read_edf(path):
                 yield tmp[0], v
 
     def num(v, conv):
-        try:
-            return conv(v)
-        except ValueError:
-            return conv(0)
+        return _qt_int(v) if conv is int else _qt_double(v)
 
     if line.startswith("EDF_DataBlockID"):
         file_type = "K1"
@@ -350,7 +370,10 @@ def read_edf(path):
     key = (vals["DataType"], rec)
     if key not in _EDF_TYPES:
         raise ValueError(f"{path}: data type {vals['DataType']} with {rec}-byte records is not supported")
-    order = "<" if vals["ByteOrder"] == "LowByteFirst" else ">"
+    # the reference's byte swap for HighByteFirst (SC_ReadData::swapBytes)
+    # copies the unswapped bytes back over its reversed copy: both orders are
+    # read as little-endian
+    order = "<"
     n = ncols * nrows
     body = raw[pos:pos + n * rec]
     if len(body) < n * rec:
@@ -364,7 +387,7 @@ def read_edf(path):
             "EditWAXSangle": "0.0 deg", "EDF_BinarySize": str(vals["EDF_BinarySize"]),
             "headSize": str(vals["EDF_HeaderSize"]), "ByteOrder": vals["ByteOrder"], "DataType": vals["DataType"],
             "Title": vals["Title"], "ExposureTime": _fmt_num(vals["ExposureTime"]),
-            "DetectorPos": _fmt_num(vals["DetectorPosition"])}
+            "DetectorPos": _fmt_num(vals["DetectorPosition"]), "@": ""}
     return Image(data, 0, ncols, 0, nrows, meta)
 
 
@@ -389,7 +412,7 @@ def read_spreadsheet(path):
         sl = line.split()
         if len(sl) < ncols:
             continue
-        vals.extend(float(t) for t in sl)
+        vals.extend(_qt_double(t) for t in sl)
     if len(vals) != nrows * ncols:
         raise ValueError(f"{path}: {len(vals)} values for {nrows} x {ncols}")
     img = Image(np.asarray(vals, dtype=np.float64).reshape(nrows, ncols), 0, ncols, 0, nrows,

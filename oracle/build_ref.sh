@@ -56,3 +56,12 @@ g++ $SFLAGS -c "$HERE/ref_simplex.cpp" -o "$OUT/ref_simplex.o" &
 wait
 g++ -shared -o "$OUT/libscsimplex.so" "$OUT/sc_simplexfit2d.o" "$OUT/ref_simplex.o"
 echo "built $OUT/libscsimplex.so"
+# the measured-data file readers (Source/sc_readdata.cpp) with the Qt
+# stand-ins of ref_stubs_io (HDF5 left out; the TIFF and 2D-SANS readers
+# compile but are not run) and the console widImage stand-in forced in
+RFLAGS="-O2 -std=gnu++17 -fPIC -w -DQ_OS_LINUX -I$HERE/ref_stubs_io -I$REF/Source -include $HERE/ref_stubs_io/readers_env.h"
+g++ $RFLAGS -c -x c++ "$REF/Source/sc_readdata.cpp" -o "$OUT/sc_readdata.o" &
+g++ $RFLAGS -c "$HERE/ref_readers.cpp" -o "$OUT/ref_readers.o" &
+wait
+g++ -shared -o "$OUT/libscreaders.so" "$OUT/sc_readdata.o" "$OUT/ref_readers.o"
+echo "built $OUT/libscreaders.so"

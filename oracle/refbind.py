@@ -202,3 +202,75 @@ def prepared_block(params, ign_new_switch=0, ign_cbs=0):
         return buf.raw[:n], ""
     finally:
         r.close()
+
+
+# ----------------------------------------------------------------- readers
+READERS = os.path.join(HERE, "_ref", "libscreaders.so")
+_readers = None
+
+
+def readers_available():
+    return os.path.exists(READERS)
+
+
+def _readers_lib():
+    global _readers
+    if _readers is None:
+        lib = ctypes.CDLL(READERS)
+        lib.ref_read_image.restype = ctypes.c_void_p
+        lib.ref_read_image.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+        lib.ref_image_dims.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        lib.ref_image_data.restype = ctypes.c_long
+        lib.ref_image_data.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_long]
+        lib.ref_image_meta_count.argtypes = [ctypes.c_void_p]
+        for f in (lib.ref_image_meta_key, lib.ref_image_meta_value):
+            f.restype = ctypes.c_char_p
+            f.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        lib.ref_image_title.restype = ctypes.c_char_p
+        lib.ref_image_title.argtypes = [ctypes.c_void_p]
+        lib.ref_image_from_data.restype = ctypes.c_void_p
+        lib.ref_image_from_data.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p]
+        lib.ref_find_beam_center.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                             ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+        lib.ref_image_free.argtypes = [ctypes.c_void_p]
+        _readers = lib
+    return _readers
+
+
+def read_image(kind, path):
+    """The reference's reader `kind` ("kws", "edf", "spreadsheet",
+    "sascrystal") on a file: {"dims": [minX, maxX, minY, maxY], "data": rows
+    y, columns x, "meta": [(key, value), ...] in reading order, "title"}, or
+    None where the reader returns no image."""
+    lib = _readers_lib()
+    h = lib.ref_read_image(kind.encode(), os.fsencode(path))
+    if not h:
+        return None
+    try:
+        d = (ctypes.c_int * 4)()
+        lib.ref_image_dims(h, d)
+        dims = list(d)
+        n = (dims[1] - dims[0]) * (dims[3] - dims[2])
+        data = np.zeros(max(n, 0))
+        got = lib.ref_image_data(h, data.ctypes.data, data.size)
+        assert got == n, (got, n)
+        meta = [(lib.ref_image_meta_key(h, i).decode("latin-1"), lib.ref_image_meta_value(h, i).decode("latin-1"))
+                for i in range(lib.ref_image_meta_count(h))]
+        return {"dims": dims, "data": data.reshape(dims[3] - dims[2], dims[1] - dims[0]), "meta": meta,
+                "title": lib.ref_image_title(h).decode("latin-1")}
+    finally:
+        lib.ref_image_free(h)
+
+
+def find_beam_center(data, minX, maxX, minY, maxY, x0, y0):
+    """The reference's findBeamCenter on an image (rows y, columns x) from the
+    start point (x0, y0)."""
+    lib = _readers_lib()
+    a = np.ascontiguousarray(data, dtype=np.float64)
+    h = lib.ref_image_from_data(minX, maxX, minY, maxY, a.ctypes.data)
+    try:
+        xe, ye = ctypes.c_int(0), ctypes.c_int(0)
+        lib.ref_find_beam_center(h, x0, y0, ctypes.byref(xe), ctypes.byref(ye))
+        return xe.value, ye.value
+    finally:
+        lib.ref_image_free(h)

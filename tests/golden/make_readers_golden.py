@@ -1,0 +1,165 @@
+"""Golden fixtures for the measured-data readers, from the reference's own
+readers (Source/sc_readdata.cpp, built by oracle/build_ref.sh into
+oracle/_ref/libscreaders.so with Qt stand-ins).
+
+Writes small synthetic input files in the reference's formats into
+tests/golden/readers/ (KWS text, EDF with each data type and byte order,
+spreadsheet text, the program's own .csv/.txt pair), runs the reference's
+reader on each and stores its image extents, data and meta information in
+readers_ref.npz / readers_ref.json, together with the reference's beam-centre
+finder on a set of images. Usage (needs the reference build):
+
+    python tests/golden/make_readers_golden.py
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from oracle import refbind  # noqa: E402
+
+IN = os.path.join(HERE, "readers")
+
+
+def kws_file(name, n, lam, det_rows, tail_short=True, seed=0):
+    rng = np.random.default_rng(seed)
+    counts = rng.integers(-2, 400, size=n * n)
+    lines = ["KWS1_MEASUREMENT KFA-IFF spectrum_data file version V-5.00", name,
+             "(* Comment *)", "kws1 | someone", f"test sample {lam}", "(* Collimation discription *)",
+             "Coll_Position Wind(1)_Pos Beamwindow_X Beamwindow_Y", "          [m]         [m]         [mm]"]
+    lines += ["(* Detector Discription *)", "Li6 Detector is in normal mode."]
+    lines += list(det_rows)
+    lines += ["(* Sample discription *)", "Sample_Nr Sample_Pos", "(* Detector Data *)", "$"]
+    for i in range(0, n * n, 8):
+        lines.append("  ".join(f"{v:7d}" for v in counts[i:i + 8]))
+    if tail_short:
+        lines.append("   1   2   3")
+    lines.append("")
+    return "\n".join(lines)
+
+
+def edf_file(kind, n, dtype, order, seed=0, extra=()):
+    rng = np.random.default_rng(seed)
+    data = rng.integers(0, 60000, size=(n, n)).astype(np.float64)
+    if dtype in ("f4", "f8"):
+        data = data / 7.0
+    bo = "<" if order == "LowByteFirst" else ">"
+    body = data.astype(bo + dtype).tobytes()
+    names = {"f4": "FloatValue", "i4": "SignedInteger", "u2": "UnsignedShort", "f8": "DoubleValue"}
+    if kind == "K1":
+        hdr = ["EDF_DataBlockID = 0.Image.Psd ;", f"EDF_BinarySize = {len(body)} ;", "EDF_HeaderSize = 1024 ;",
+               f"ByteOrder = {order} ;", f"DataType = {names[dtype]} ;", f"Dim_1 = {n} ;", f"Dim_2 = {n} ;",
+               "Title = test image ;", "Center_1 = 12.5 ;", "Center_2 = 7 ;", "PSize_1 = 0.000172 ;",
+               "PSize_2 = 0.000172 ;", "SampleDistance = 3.2 ;", "WaveLength = 1.54e-10 ;",
+               "ExposureTime = 60 ;", "DetectorPosition = 2.5 ;"]
+    else:
+        hdr = ["HeaderID = EH:000001:000000:000000 ;", f"ByteOrder = {order} ;", f"DataType = {names[dtype]} ;",
+               f"Dim_1 = {n} ;", f"Dim_2 = {n} ;", f"Size = {len(body)} ;"]
+    hdr += list(extra)
+    text = "{\n" + "\n".join(hdr) + "\n"
+    text += " " * ((-(len(text) + 2)) % 512) + "}\n"
+    return text.encode("latin-1") + body
+
+
+def spreadsheet_file(n, seed=0):
+    rng = np.random.default_rng(seed)
+    data = rng.uniform(0.5, 9.0, size=(n, n))
+    data[8:13, 5:10] = 0.0
+    lines = [f"    {n}    {n} Start pixel = (       1       1)"]
+    for r in range(n):
+        lines.append("  " + " ".join(f"{v:13.6e}" for v in data[r]))
+    return "\n".join(lines) + "\n"
+
+
+def sascrystal_files(minX, maxX, minY, maxY, seed=0):
+    rng = np.random.default_rng(seed)
+    data = rng.uniform(1e-6, 2.0, size=(maxY - minY, maxX - minX))
+    csv = [f"X:;{minX};{maxX}", f"Y:;{minY};{maxY}"]
+    for j, y in enumerate(range(minY, maxY)):
+        csv.append(f"Y={y}:;" + ";".join(f"{v:.6g}" for v in data[j]))
+    txt = ["From File\tsomewhere.csv", "NbRows\t1", "ComboBoxParticle\tsphere {0}", "EditRadius\t10",
+           "EditSigma\t0.1"]
+    return "\n".join(csv) + "\n", "\n".join(txt) + "\n"
+
+
+def inputs():
+    """name -> (reader kind, file name, bytes)"""
+    out = {}
+    det = ("Offset Z_Position X_Position Y_Position", "  [m]        [m]       [mm]       [mm]",
+           " -0.38       1.50      -4.10     9.00", " -0.38       1.50      -4.10     9.00")
+    out["kws_128_A"] = ("kws", "kws_128_A.kws", kws_file("kws_128_A", 128, "lambda=6.0A", det).encode())
+    out["kws_144_nm"] = ("kws", "kws_144_nm.kws",
+                         kws_file("kws_144_nm", 144, "lambda= 0.45nm", (), tail_short=False, seed=1).encode())
+    out["kws_128_n"] = ("kws", "kws_128_n.kws", kws_file("kws_128_n", 128, "lambda= 0.45n", det[:2], seed=2).encode())
+    out["kws_bad_size"] = ("kws", "kws_bad_size.kws", kws_file("kws_bad", 100, "lambda=5A", det).encode())
+    for dtype in ("f4", "i4", "u2", "f8"):
+        for order in ("LowByteFirst", "HighByteFirst"):
+            nm = f"edf_k1_{dtype}_{'le' if order == 'LowByteFirst' else 'be'}"
+            out[nm] = ("edf", nm + ".edf", edf_file("K1", 9, dtype, order, seed=3))
+    out["edf_e1_f4"] = ("edf", "edf_e1_f4.edf", edf_file("E1", 7, "f4", "LowByteFirst", seed=4))
+    out["edf_version2"] = ("edf", "edf_version2.edf", b"{\nEDF_DataFormatVersion = 2.0 ;\n}\n")
+    out["spreadsheet_20"] = ("spreadsheet", "spreadsheet_20.spr", spreadsheet_file(20, seed=5).encode())
+    csv, txt = sascrystal_files(-4, 5, -3, 3, seed=6)
+    out["sascrystal"] = ("sascrystal", "sascrystal.csv", csv.encode())
+    out["sascrystal_txt"] = (None, "sascrystal.txt", txt.encode())
+    return out
+
+
+def beam_images():
+    """name -> (data rows y, minX, maxX, minY, maxY, start x, start y)"""
+    out = {}
+    d = np.ones((64, 64))
+    d[17:24, 26:35] = 0.0
+    out["walk_inside"] = (d, 0, 64, 0, 64, 31, 21)
+    out["search_outside"] = (d, 0, 64, 0, 64, 5, 5)
+    d2 = np.ones((64, 64))
+    d2[25, 40] = 0.0
+    out["narrow_shadow"] = (d2, 0, 64, 0, 64, 5, 5)
+    d3 = np.ones((9, 11))
+    d3[3:6, 4:7] = 0.0
+    out["negative_extents"] = (d3, -5, 6, -4, 5, 0, 0)
+    rng = np.random.default_rng(7)
+    d4 = rng.uniform(0.5, 3.0, size=(48, 40))
+    d4[10:30, 12:20] = 0.0
+    d4[0, 0] = 0.0005
+    out["noisy_offcentre"] = (d4, 0, 40, 0, 48, 20, 24)
+    return out
+
+
+def main():
+    if not refbind.readers_available():
+        sys.exit("oracle/_ref/libscreaders.so not built (oracle/build_ref.sh)")
+    os.makedirs(IN, exist_ok=True)
+    files = inputs()
+    for _, (kind, fn, raw) in files.items():
+        with open(os.path.join(IN, fn), "wb") as f:
+            f.write(raw)
+    arrays, meta = {}, {"images": {}, "beam_center": {}}
+    for name, (kind, fn, _) in files.items():
+        if kind is None:
+            continue
+        r = refbind.read_image(kind, os.path.join(IN, fn))
+        if r is None:
+            meta["images"][name] = {"kind": kind, "file": fn, "image": None}
+            print(name, "no image")
+            continue
+        arrays[name] = r["data"]
+        kv = [(k, os.path.basename(v) if k == "From File" else v) for k, v in r["meta"]]
+        meta["images"][name] = {"kind": kind, "file": fn, "dims": r["dims"], "meta": kv, "title": r["title"]}
+        print(name, r["dims"], len(kv), "meta entries")
+    for name, (d, x0, x1, y0, y1, sx, sy) in beam_images().items():
+        arrays["beam_" + name] = d
+        c = refbind.find_beam_center(d, x0, x1, y0, y1, sx, sy)
+        meta["beam_center"][name] = {"dims": [x0, x1, y0, y1], "start": [sx, sy], "center": list(c)}
+        print("beam", name, c)
+    np.savez_compressed(os.path.join(HERE, "readers_ref.npz"), **arrays)
+    with open(os.path.join(HERE, "readers_ref.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

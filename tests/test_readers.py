@@ -191,6 +191,9 @@ def test_edf_types_and_layout(tmp_path, dtype, order):
     fn.write_bytes(_edf_bytes("K1", filedata, dtype, order))
     img = R.read_edf(str(fn))
     want = filedata.astype(dtype).astype(np.float64)
+    if order == "HighByteFirst":
+        # the reference reads both byte orders as little-endian (its swap is a no-op)
+        want = np.frombuffer(filedata.astype(">" + dtype).tobytes(), "<" + dtype).reshape(n, n).astype(np.float64)
     # file pixel (r, c) lands at x = n-1-r, y = c
     for r, c in [(0, 0), (0, 5), (3, 2), (8, 8)]:
         assert img.get(n - 1 - r, c) == want[r, c]
