@@ -913,15 +913,21 @@ bool Prep::coefficients() {
         // i0 = 2 norm integral bit for bit. It is computed once.
         const double intl_const = qromb_delta_1d(1, 0, P.dbeta);
         if (cdim == 2) {
-            // homogeneous disks along an axis: x :6045-6130, y :6875-6960,
-            // z :7644-7730. The x and y blocks differ only in carr11pm (whose
+            // disks along an axis, homogeneous: x :6045-6130, y :6875-6960,
+            // z :7644-7730; core/shell: x :6137-6273, y :6966-7100, z
+            // :7730-7860. The x and y blocks differ only in carr11pm (whose
             // moment-based first assignment the reference overwrites at once);
             // the z block leaves carr11pm at 1 and folds the delta moments into
-            // carr1p. The general orientation is not offered: the reference's
-            // disk P(q) has no branch for it and returns an uninitialised value.
-            if (P.cs != 0 || P.orcase == CS_ORC_GENERAL) {
+            // carr1p. Core/shell adds the cross (carr5) and shell (carr6)
+            // terms and forms carr4f with xrn (xln when homogeneous). The
+            // general orientation is not offered: the reference's disk P(q) has
+            // no branch for it and returns an uninitialised value.
+            if ((P.cs != 0 && P.cs != 1) || P.orcase == CS_ORC_GENERAL) {
                 supported = false;
             } else {
+                const bool cs1 = P.cs == 1;
+                bool search5 = true, search6 = true;
+                double xrmn_n = 1.0;
                 double z12v[kNmax + 1];
                 z12v[0] = 1.0;
                 double xrn_n = 1.0;
@@ -947,6 +953,10 @@ bool Prep::coefficients() {
                     gam3[n] = gam3[n - 1] * (2 * n + 1) / 2.0;
                     xln_n = -xln_n * xl2z;
                     xrn_n = -xrn_n * xr2z;
+                    if (cs1) {
+                        xrmn_n = -xrmn_n * xrm2z;
+                        pn[n] = pn[n - 1] * p * p;
+                    }
                     double sump;
                     if (orc == CS_ORC_ZAXIS) {
                         sump = 0.0;
@@ -976,7 +986,20 @@ bool Prep::coefficients() {
                     sump = 0.0;
                     for (int m = 0; m <= n; m++)
                         sump += z12v[m] * z12v[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
-                    carr4f[n] = M_PI * xln_n * sump / 4.0;
+                    if (!cs1) {
+                        carr4f[n] = M_PI * xln_n * sump / 4.0;
+                    } else {
+                        carr4f[n] = M_PI * xrn_n * sump / 4.0;
+                        sump = 0.0;
+                        for (int m = 0; m <= n; m++) sump += pn[m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                        carr5p[n] = M_PI * z12v[n] * xrmn_n * sump / 4.0;
+                        carr6p[n] = carr4p[n] / pn[n];
+                        sump = 0.0;
+                        for (int m = 0; m <= n; m++)
+                            sump += pn[m] * z12v[m] * z12v[n - m] / (gam3[m] * gam3[n - m] * fkv[m] * fkv[n - m]);
+                        carr5f[n] = M_PI * xrmn_n * sump / 4.0;
+                        carr6f[n] = carr4f[n] / pn[n];
+                    }
                     // the series of the orientation integral's Bessel approximation
                     carr2p[n] = std::pow(4.0, n + 1) * gam3[n] * z12vl[n] * xln_n /
                                 (std::sqrt(M_PI) * (n + 2) * (n + 1) * (n + 1) * fkv[n] * fkv[n] * fkv[n]);
@@ -997,11 +1020,29 @@ bool Prep::coefficients() {
                             search4 = false;
                         }
                     }
+                    if (cs1 && search5) {
+                        if (carr5p[n] < 1e-50) {
+                            n5 = n;
+                            search5 = false;
+                        }
+                    }
+                    if (cs1 && search6) {
+                        if (carr6p[n] < 1e-50) {
+                            n6 = n;
+                            search6 = false;
+                        }
+                    }
                     if (std::fabs(carr1f[n]) < kMin) {
                         if (n < n1f) n1f = n;
                     }
                     if (std::fabs(carr4f[n]) < kMin) {
                         if (n < n4f) n4f = n;
+                    }
+                    if (cs1 && std::fabs(carr5f[n]) < kMin) {
+                        if (n < n5f) n5f = n;
+                    }
+                    if (cs1 && std::fabs(carr6f[n]) < kMin) {
+                        if (n < n6f) n6f = n;
                     }
                 }
                 intl = intl_const;
@@ -2427,9 +2468,8 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
         // the generic pixel function covers the particles prepared above:
         // spheres, cylinders (z-direction, Gaussian orientation; isotropic,
         // homogeneous or core/shell), homogeneous
-        // isotropic cubes, disks (isotropic or z-direction along an axis,
-        // homogeneous or core/shell; homogeneous with the Gaussian orientation
-        // along an axis),
+        // isotropic cubes, disks (isotropic, or z-direction or Gaussian along
+        // an axis; homogeneous or core/shell),
         // isotropic or z-direction vesicles, and homogeneous isotropic
         // ellipsoids
         const bool ok = P.particle == 0 || (P.particle == 1 && (P.ordis == 6 || P.ordis == 0)) ||
@@ -2437,7 +2477,8 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
                         (P.particle == 4 && P.ordis == 7 && P.cs == 0) ||
                         (P.particle == 2 && P.ordis == 6 && (P.cs == 0 || P.cs == 1) &&
                          P.orcase != CS_ORC_GENERAL) ||
-                        (P.particle == 2 && P.ordis == 0 && P.cs == 0 && P.orcase != CS_ORC_GENERAL) ||
+                        (P.particle == 2 && P.ordis == 0 && (P.cs == 0 || P.cs == 1) &&
+                         P.orcase != CS_ORC_GENERAL) ||
                         (P.particle == 2 && P.ordis == 7 && (P.cs == 0 || P.cs == 1)) ||
                         (P.particle == 3 && (P.ordis == 7 || P.ordis == 6)) ||
                         (P.particle == 5 && P.ordis == 7 && P.cs == 0);

@@ -119,6 +119,10 @@ def image_cases():
                                            phi=0.0)
     cases["cyl_cs_zdir_z_g32"] = dict(C.scaled(C.CYL_GAUSS, 32), Ordis=6, theta=0.0, phi=0.0, ComboBoxInterior=1,
                                       EditRadiusi=7.0, EditRho=0.3)
+    cases["disk_cs_gauss_x_g24"] = dict(dg24, phi=0.0, theta=90.0, ComboBoxInterior=1, EditRadiusi=3.0, EditRho=0.3)
+    cases["disk_cs_gauss_z_fcc_g16"] = dict(C.scaled(C.SPHERE_FCC, 16), ComboBoxParticle=2, EditRadius=2.0,
+                                            Length=12.0, SigmaL=0.2, Ordis=0, theta=0.0, phi=0.0, EditDbeta=15.0,
+                                            ComboBoxInterior=1, EditRadiusi=3.0, EditRho=0.3)
     # core/shell cylinders with the Gaussian orientation
     ccs = dict(ComboBoxInterior=1, EditRadiusi=7.0, EditRho=0.3)
     cases["cyl_cs_gauss_g24"] = dict(C.scaled(C.CYL_GAUSS, 24), **ccs)
