@@ -11,6 +11,7 @@ the same layout and metadata keys, so that a target can go straight to
   ``Source/widimage.cpp:154-166`` and ``:243-262``);
 * KWS detector files (``Source/sc_readdata.cpp:655-876``);
 * EDF detector files (``Source/sc_readdata.cpp:1769-2121``);
+* SAXSLAB/Pilatus TIFF files (``Source/sc_readdata.cpp:24-520``);
 * spreadsheet text images (``Source/sc_readdata.cpp:2123-2190``);
 * the beam-stop centre finder (``SC_ReadData::findBeamCenter``,
   ``Source/sc_readdata.cpp:878-1010``).
@@ -421,6 +422,136 @@ def read_spreadsheet(path):
     img.meta["BeamPosX"] = str(bx)
     img.meta["BeamPosY"] = str(by)
     return img
+
+
+def _tiff_xml_params(window):
+    """The name/value pairs the reference scrapes from the 20000 bytes that
+    start at ``<?xml version=``: a double quote opens a name, the next one
+    closes it and starts its value, which runs (without ``<`` and ``>``)
+    up to the next ``<``. The scan starts at the window's second byte and
+    runs over whatever follows the XML (binary data included); a name whose
+    first character is NUL (or an empty name) drops every pair collected so
+    far and ends the scan. The XML declaration's pair is dropped."""
+    names, vals = [], []
+    pstart = nstart = False
+    for ii in range(1, len(window)):
+        c = chr(window[ii])
+        if pstart and c != '"':
+            names[-1] += c
+        if nstart and c != ">" and c != "<":
+            vals[-1] += c
+        if nstart and c == "<":
+            nstart = False
+        if c == '"':
+            if not pstart:
+                pstart = True
+                names.append("")
+                vals.append("")
+            else:
+                pstart = False
+                nstart = True
+                if names[-1][:1] in ("", "\0"):
+                    names, vals = [], []
+                    break
+    if names:
+        names.pop(0)
+        vals.pop(0)
+    return names, vals
+
+
+def read_tiff(path):
+    """A SAXSLAB/Pilatus TIFF image (``Source/sc_readdata.cpp:24-520``): the
+    parameters of its XML header (see :func:`_tiff_xml_params`; the file must
+    hold 20000 bytes from the header's start, else None), then the TIFF
+    directory's width, length, bits per sample, compression (1 only, else
+    None), photometric interpretation (0 or 1, else None), strip offset and
+    samples per pixel (1 only, else None), each added to the meta information
+    as the reference names it. As in the reference, the header's third byte
+    must be 42 (``II*`` files; a big-endian ``MM`` file has 0 there and is not
+    read), and every number of the directory is read little-endian.
+
+    Pixel values: 8-bit signed characters, 16-bit signed integers (both
+    stored transposed, at x = row, y = column, which the reference defines
+    for square images only), 32-bit signed integers (little-endian files:
+    row r at y = rows-1-r; ``MM*`` files: unswapped, transposed). Where the
+    reference's loops would write outside the image (1 and 2 bytes per pixel,
+    or a big-endian file, with data following the image in the last 2048-byte
+    block) or leave pixels unwritten, ValueError."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    head = raw[:20000]
+    anf = 0
+    for i in range(5, len(head)):
+        if head.startswith(b"<?xml version=", i):
+            anf = i
+            break
+    window = raw[anf:anf + 20000]
+    if len(window) != 20000:
+        return None
+    names, vals = _tiff_xml_params(window)
+    if len(raw) < 8 or raw[:2] not in (b"II", b"MM") or raw[2] != 42:
+        return None
+    little = raw[:2] == b"II"
+
+    def i32(off):
+        return int.from_bytes(raw[off:off + 4].ljust(4, b"\0"), "little", signed=True)
+
+    pos = i32(4)
+    ntags = int.from_bytes(raw[pos:pos + 2].ljust(2, b"\0"), "little", signed=True)
+    pos += 2
+    ncols = nrows = bps = strip = 0
+    for _ in range(max(ntags, 0)):
+        code = int.from_bytes(raw[pos:pos + 2], "little")
+        nval, val = i32(pos + 4), i32(pos + 8)
+        pos += 12
+        if code == 256 and nval == 1:
+            ncols = val
+            names.append("NbCols")
+            vals.append(str(ncols))
+        elif code == 257 and nval == 1:
+            nrows = val
+            names.append("NbRows")
+            vals.append(str(nrows))
+        elif code == 258 and nval == 1:
+            bps = val
+            names.append("BitsPerSample")
+            vals.append(str(bps))
+        elif code == 259 and nval == 1 and val != 1:
+            return None
+        elif code == 262 and nval == 1:
+            if val not in (0, 1):
+                return None
+            names.append("PhotomInterp")
+            vals.append(str(val))
+        elif code == 273:
+            strip = val if nval == 1 else i32(val)
+            names.append("StripOffsets")
+            vals.append(str(strip))
+        elif code == 277 and nval == 1:
+            if val != 1:
+                return None
+            names.append("SamplesPerPixel")
+            vals.append(str(val))
+    n = nrows * ncols
+    bpp = int(bps / 8)
+    if n <= 0 or bpp not in (1, 2, 4):
+        raise ValueError(f"{path}: {ncols} x {nrows} pixels of {bps} bits are not read")
+    kind = {1: "<i1", 2: "<i2", 4: "<i4"}[bpp]
+    body = raw[strip:]
+    bounded = bpp == 4 and little
+    # the reference reads 2048-byte blocks; unbounded loops finish the block
+    nrec = len(body) // bpp if bounded else min(len(body), -(-n * bpp // 2048) * 2048) // bpp
+    if nrec < n or (not bounded and (nrec > n or nrows != ncols)):
+        raise ValueError(f"{path}: the data do not fill the {ncols} x {nrows} image as the reference reads it")
+    v = np.frombuffer(body[:n * bpp], dtype=kind).astype(np.float64).reshape(nrows, ncols)
+    # origIma[x + cols*y]: little-endian 32-bit at x = c, y = rows-1-r;
+    # the others at x = r, y = c
+    data = v[::-1].copy() if bounded else v.T.copy()
+    meta = {"From File": path}
+    for k, val in zip(names, vals):
+        meta[k] = val
+    meta["@"] = ""
+    return Image(data, 0, ncols, 0, nrows, meta)
 
 
 def find_beam_center(img, x0, y0):

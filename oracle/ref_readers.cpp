@@ -35,7 +35,7 @@ static widImage *cs_add(int x0, int x1, int y0, int y1, double *d, QString title
 
 extern "C" {
 
-// kind: "kws", "edf", "spreadsheet", "sascrystal"; null when the reader
+// kind: "kws", "edf", "spreadsheet", "sascrystal", "tiff"; null when the reader
 // returns none
 void *ref_read_image(const char *kind, const char *fn) {
     const QString k(kind), f(fn);
@@ -43,6 +43,7 @@ void *ref_read_image(const char *kind, const char *fn) {
     if (k == "edf") return SC_ReadData::readImageEDF(cs_add, f);
     if (k == "spreadsheet") return SC_ReadData::readImageSpreadsheet(cs_add, f);
     if (k == "sascrystal") return SC_ReadData::readImageSasCrystal(cs_add, f);
+    if (k == "tiff") return SC_ReadData::readImageTiff(cs_add, f);
     return nullptr;
 }
 

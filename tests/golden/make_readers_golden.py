@@ -86,6 +86,41 @@ def sascrystal_files(minX, maxX, minY, maxY, seed=0):
     return "\n".join(csv) + "\n", "\n".join(txt) + "\n"
 
 
+SAXSLAB_XML = ('<?xml version="1.0" ?><SAXSLABparameters><param name="det_pixel_size">172e-6 172e-6</param>'
+               '<param name="wavelength">1.3414</param><param name="detector_dist">536.7868</param>'
+               '<param name="beamcenter_actual">371.94    198.97</param>'
+               '<param name="Meas.Description">test sample, 22.27C</param></SAXSLABparameters>')
+
+
+def tiff_file(n, bps, data_off=20480, magic=b"II*\0", compression=1, strip_table=False, xml_at=256,
+              total=None, data=None, seed=0):
+    """A TIFF in the SAXSLAB layout: directory at byte 8, the XML header at
+    xml_at, the n x n image (bps bits, little-endian) at data_off."""
+    rng = np.random.default_rng(seed)
+    if data is None:
+        hi = {8: 256, 16: 65536, 32: 2 ** 31 - 1}[bps]
+        data = rng.integers(0, hi, size=n * n)
+    kind = {8: "u1", 16: "<u2", 32: "<i4"}[bps]
+    body = np.asarray(data).astype(kind).tobytes()
+    tags = [(256, 4, 1, n), (257, 4, 1, n), (258, 3, 1, bps), (259, 3, 1, compression), (262, 3, 1, 1),
+            (270, 2, 12, 4000), (277, 3, 1, 1), (34710, 4, 1, 1024)]
+    out = bytearray(max(data_off + len(body), total or 0))
+    if strip_table:
+        tags.append((273, 4, 4, 6000))
+        out[6000:6016] = np.array([data_off, data_off + 1, 0, 0], dtype="<i4").tobytes()
+    else:
+        tags.append((273, 4, 1, data_off))
+    out[0:8] = magic + (8).to_bytes(4, "little")
+    ifd = len(tags).to_bytes(2, "little") + b"".join(
+        c.to_bytes(2, "little") + t.to_bytes(2, "little") + k.to_bytes(4, "little") + v.to_bytes(4, "little")
+        for c, t, k, v in tags)
+    out[8:8 + len(ifd)] = ifd
+    x = SAXSLAB_XML.encode("latin-1")
+    out[xml_at:xml_at + len(x)] = x
+    out[data_off:data_off + len(body)] = body
+    return bytes(out)
+
+
 def inputs():
     """name -> (reader kind, file name, bytes)"""
     out = {}
@@ -103,6 +138,20 @@ def inputs():
     out["edf_e1_f4"] = ("edf", "edf_e1_f4.edf", edf_file("E1", 7, "f4", "LowByteFirst", seed=4))
     out["edf_version2"] = ("edf", "edf_version2.edf", b"{\nEDF_DataFormatVersion = 2.0 ;\n}\n")
     out["spreadsheet_20"] = ("spreadsheet", "spreadsheet_20.spr", spreadsheet_file(20, seed=5).encode())
+    out["tiff_i4"] = ("tiff", "tiff_i4.tif", tiff_file(16, 32, seed=8))
+    out["tiff_i2"] = ("tiff", "tiff_i2.tif", tiff_file(16, 16, seed=9))
+    out["tiff_u1"] = ("tiff", "tiff_u1.tif", tiff_file(16, 8, seed=10))
+    out["tiff_strip_table"] = ("tiff", "tiff_strip_table.tif", tiff_file(16, 32, strip_table=True, seed=11))
+    out["tiff_mm"] = ("tiff", "tiff_mm.tif", tiff_file(16, 32, magic=b"MM\0*", seed=12))
+    out["tiff_mm_star"] = ("tiff", "tiff_mm_star.tif", tiff_file(16, 32, magic=b"MM*\0", seed=13))
+    out["tiff_compressed"] = ("tiff", "tiff_compressed.tif", tiff_file(16, 32, compression=5, seed=14))
+    out["tiff_short"] = ("tiff", "tiff_short.tif", tiff_file(16, 32, data_off=4096, seed=15))
+    # an image at the end of the XML window holding a quote, a NUL and a
+    # quote: the reference drops every XML parameter (the file ends with the
+    # image: the 8-bit loop would otherwise run past it)
+    q = np.full(16 * 16, 7)
+    q[40], q[41], q[60] = 0x22, 0, 0x22
+    out["tiff_quote"] = ("tiff", "tiff_quote.tif", tiff_file(16, 8, data_off=256 + 20000 - 256, data=q))
     csv, txt = sascrystal_files(-4, 5, -3, 3, seed=6)
     out["sascrystal"] = ("sascrystal", "sascrystal.csv", csv.encode())
     out["sascrystal_txt"] = (None, "sascrystal.txt", txt.encode())
