@@ -1771,6 +1771,9 @@ static __device__ __noinline__ double calc_generic(const Ctx &C, double qx, doub
     double width = 1;  // :511-524
     if (P.debyescherrer) width = 4.0 / P.domainsize;
     if (P.para) width = (4.0 / P.domainsize) + sqr(P.reldis) * P.dist * sqr(q);
+    // the anisotropic Gaussian peak on isotropic particles: |sig|/3
+    const double sig_len = sqrt(sqr(P.sig[0]) + sqr(P.sig[1]) + sqr(P.sig[2]));
+    if (P.lattice && P.shp == 8 && P.ordis == 7) width = sig_len / 3.0;
     width *= P.width_zuf;
     const double widthiso = 1.0 / P.uca;
     radintensity = 0.0;
@@ -1872,6 +1875,32 @@ static __device__ __noinline__ double calc_generic(const Ctx &C, double qx, doub
                     const double phiord = g3 / (peaknorm1 * exp(beta * log(1 + x2phi * yphit * yphit)));
                     psiord = P.ceff * psiord + (1 - P.ceff) * phiord;
                 }
+                break;
+            }
+            case 8: {  // anisotropic Gaussian, :599-691 (perfect orientation or isotropic)
+                auto aniso = [&](double hx, double hy, double hz) {
+                    if (P.ordis == 6 || fabs(P.dbeta) < CS_EPS9) {
+                        // the Gaussian ellipsoid of the unit-cell axes around q_hkl
+                        const double dqx = qx - hx, dqy = qy - hy, dqz = qz - hz;
+                        const double a1n = sqrt(sqr(P.ax1[0]) + sqr(P.ax1[1]) + sqr(P.ax1[2])) * P.sig[0];
+                        const double a2n = sqrt(sqr(P.ax2[0]) + sqr(P.ax2[1]) + sqr(P.ax2[2])) * P.sig[1];
+                        const double a3n = sqrt(sqr(P.ax3[0]) + sqr(P.ax3[1]) + sqr(P.ax3[2])) * P.sig[2];
+                        const double dqs1 = (dqx * P.ax1[0] + dqy * P.ax1[1] + dqz * P.ax1[2]) / a1n;
+                        const double dqs2 = (dqx * P.ax2[0] + dqy * P.ax2[1] + dqz * P.ax2[2]) / a2n;
+                        const double dqs3 = (dqx * P.ax3[0] + dqy * P.ax3[1] + dqz * P.ax3[2]) / a3n;
+                        const double xa = dqs1 * dqs1 + dqs2 * dqs2 + dqs3 * dqs3;
+                        return exp(-4 * xa / M_PI) / (sqrt(M_PI * M_PI * M_PI) * P.sig[0] * P.sig[1] * P.sig[2] / 8.0);
+                    }
+                    // isotropic orientation (the preparation offers no other case)
+                    const double locwidth = sig_len / 3.0;
+                    const double xa = (q - qhkl) * (q - qhkl) / (locwidth * locwidth);
+                    return g3 * exp(-4 * xa / M_PI) / (M_PI * locwidth / 2.0);
+                };
+                // with twinning the reference forms only the twin's term and
+                // mixes it with sq = 1
+                if (!P.twin) sq = aniso(qxhkl, qyhkl, qzhkl);
+                psiord = 1.0;
+                if (P.twin) sq = P.ceff * sq + (1 - P.ceff) * aniso(qxhklt, qyhklt, qzhklt);
                 break;
             }
             default:

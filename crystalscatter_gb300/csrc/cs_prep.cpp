@@ -2425,8 +2425,16 @@ int prepare(const cs_params &in, int calc_quadrants, int expand, int ign_new_swi
     P.sinphic = std::sin(-P.polphi * M_PI / 180.);
     P.cosphic = std::cos(-P.polphi * M_PI / 180.);
 
-    if (shp == 8 && P.lattice) {
-        err = "anisotropic Gaussian peak shape is not implemented";
+    // the anisotropic Gaussian peak on a lattice replaces norm by the
+    // distribution's norm integral (qrombdeltac i0 = 2, :967-973), which
+    // the particle's form factor then divides by as well
+    if (shp == 8 && P.lattice) P.norm = qromb_delta_1d(2, 0, P.dbeta);
+
+    // the anisotropic Gaussian peak: perfect orientation (z-direction or
+    // dbeta = 0) and isotropic particles; the fiber pattern and the other
+    // orientations (the unit-cell rotation integrals) are not built
+    if (shp == 8 && P.lattice && !(P.ordis == 6 || std::fabs(P.dbeta) < kEps9 || P.ordis == 7)) {
+        err = "anisotropic Gaussian peak shape: only the perfect and isotropic orientations are implemented";
         return CS_ERR_UNSUPPORTED;
     }
 

@@ -82,6 +82,15 @@ def image_cases():
     cases["sphere_fcc_voigt_g24"] = dict(sph, ComboBoxPeak=4, EditPeakPar=40.0)
     cases["sphere_fcc_pearson_g24"] = dict(sph, ComboBoxPeak=5, EditPeakPar=1.5)
     cases["sphere_fcc_twin_g24"] = dict(sph, LType=4, CheckBoxTwinned=1, EditCeff=0.7)
+    # the anisotropic Gaussian peak: isotropic, perfect orientation (z
+    # direction, and dbeta = 0), twinned; unit-cell axes and widths as set
+    ani = dict(sph, ComboBoxPeak=7, EditAxis1x=1.0, EditAxis1y=0.2, EditAxis1z=0.0, EditAxis2x=0.0, EditAxis2y=1.0,
+               EditAxis2z=0.1, EditAxis3x=0.0, EditAxis3y=0.0, EditAxis3z=1.0, Editdom1=60.0, Editdom2=45.0,
+               Editdom3=30.0)
+    cases["sphere_fcc_aniso_iso_g24"] = dict(ani, Ordis=7)
+    cases["sphere_fcc_aniso_zdir_g24"] = dict(ani, Ordis=6)
+    cases["sphere_fcc_aniso_dbeta0_g24"] = dict(ani, EditDbeta=0.0)
+    cases["sphere_bcc_aniso_twin_g24"] = dict(ani, LType=4, Ordis=6, CheckBoxTwinned=1, EditCeff=0.7)
     cases["sphere_fcc_ignswitch_g24"] = dict(sph)
     cases["cyl_zdir_fcc_g24"] = dict(C.scaled(C.bct_set(2), 24), LType=5)
     cases["cyl_gauss_x_ignswitch_g16"] = C.scaled(C.CYL_GAUSS_X, 16)
