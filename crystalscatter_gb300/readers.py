@@ -554,6 +554,31 @@ def read_tiff(path):
     return Image(data, 0, ncols, 0, nrows, meta)
 
 
+def open_meas_file(path):
+    """local_OpenMeasFile (``Source/sc_mainCons.cpp:1613-1652``): the reader
+    for a measured-data file by its extension; returns (image, is_kws). A
+    ``.dat``/``.csv``/``.txt`` with all three files of its base present is the
+    program's own saved image; otherwise ``.tif``/``.tiff`` TIFF, ``.dat``/
+    ``.data`` KWS, ``.edf`` EDF, ``.spr`` spreadsheet. HDF5 and the 2D-SANS
+    formats (``.xml``, ``.csv``, ``.txt``) are not built (ValueError)."""
+    low = path.lower()
+    if low.endswith((".dat", ".csv", ".txt")):
+        base = _base(path)
+        if all(os.path.exists(base + e) for e in (".csv", ".dat", ".txt")):
+            img = read_sascrystal_csv(path)
+            if img is not None:
+                return img, False
+    if low.endswith((".tif", ".tiff")):
+        return read_tiff(path), False
+    if low.endswith((".dat", ".data")):
+        return read_kws(path), True
+    if low.endswith(".edf"):
+        return read_edf(path), False
+    if low.endswith(".spr"):
+        return read_spreadsheet(path), False
+    raise ValueError(f"{path}: no reader for this file type here")
+
+
 def find_beam_center(img, x0, y0):
     """Centre of the beam stop, SC_ReadData::findBeamCenter: pixels at or
     below the reference level (the first pixel's value when that is at most
