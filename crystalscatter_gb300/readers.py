@@ -203,13 +203,13 @@ def read_kws(path):
     detector description table), then whitespace-separated counts (lines of
     at least 8 numbers; negative counts read as 0). 128², 144² and 256²
     detectors are recognised, with the beam at the centre and 5.3 mm pixels.
-    Files whose first 40 lines name ``Data columns`` are 2D-SANS files, which
-    this reader does not handle (ValueError)."""
+    Files whose first 40 lines name ``Data columns`` are 2D-SANS files and go
+    to :func:`read_2dsans`."""
     with open(path, "r", errors="replace") as f:
         lines = f.read().split("\n")
     for line in lines[:40]:
         if "Data columns" in line.strip():
-            raise ValueError(f"{path}: a 2D-SANS file, not KWS data")
+            return read_2dsans(path)  # a 2D-SANS file, as the reference decides
     is_hdr = True
     look_lambda = look_det = False
     det_hdr = True
@@ -554,13 +554,100 @@ def read_tiff(path):
     return Image(data, 0, ncols, 0, nrows, meta)
 
 
+def read_2dsans(path):
+    """A 2D-SANS (ILL) image (``Source/sc_readdata.cpp:1466-1767``) in its
+    text forms:
+
+    * ``.csv``: the first block of lines (it ends at a line shorter than two
+      characters); lines starting with ``A`` are skipped, the rest hold a
+      three-character row index and comma-separated values (at least 8;
+      ``nan...`` reads as 0); the rows are the last index + 1 (an index that
+      does not parse, e.g. one padded with blanks, which the line's trimming
+      moves, leaves them at 0: an empty image), the columns the first row's
+      count;
+    * ``.dat``: a header up to the ``ASCII`` line (``Data columns are A - B -
+      I - ...`` names the intensity column, the first starting with ``I``,
+      else None; ``key: value`` lines become meta information), then
+      whitespace-separated rows whose intensity column is read (0 where it
+      does not parse, rows too short skipped); the image is sqrt(n) rows
+      (at least 2) of n / rows columns.
+
+    Rows are stored bottom-up (file row r at y = rows - 1 - r). The XML form
+    is not built (ValueError); other extensions give None, as in the
+    reference. Data that do not fill rows x columns raise ValueError (the
+    reference reads past its buffer there)."""
+    low = path.lower()
+    if low.endswith(".xml"):
+        raise ValueError(f"{path}: the XML form of 2D-SANS files is not read here")
+    meta = {}
+    vals = []
+    nrows = ncols = 0
+    if low.endswith(".csv"):
+        with open(path, "rb") as f:
+            raw = f.read().decode("latin-1")
+        for line in raw.split("\n"):
+            line = line.strip()
+            if len(line) < 2:
+                break
+            if line.startswith("A"):
+                continue
+            sl = [t for t in line[3:].split(",") if t != ""]
+            if len(sl) < 8:
+                continue
+            head = line[:3].strip()
+            if re.fullmatch(r"[+-]?\d+", head):
+                nrows = int(head) + 1
+            if ncols == 0:
+                ncols = len(sl)
+            for t in sl:
+                vals.append(0.0 if t.startswith("nan") else _qt_double(t))
+    elif low.endswith(".dat"):
+        with open(path, "rb") as f:
+            raw = f.read().decode("latin-1")
+        hdr, index = True, -1
+        for line in raw.split("\n"):
+            line = line.strip()
+            if len(line) < 2:
+                continue
+            if hdr:
+                if line.startswith("Data columns"):
+                    cols = line.replace("Data columns ", "").replace("are ", "").split(" - ")
+                    for i, c in enumerate(cols):
+                        if c.startswith("I"):
+                            index = i
+                            break
+                elif line.startswith("ASCII"):
+                    hdr = False
+                    if index < 0:
+                        return None
+                elif ":" in line:
+                    pos = line.index(":")
+                    meta[line[:pos]] = line[pos + 1:].strip()
+            else:
+                sl = [t for t in re.split(r"[\t ]", line) if t != ""]
+                if index >= len(sl):
+                    continue
+                vals.append(_qt_double(sl[index]))
+        nrows = max(int(math.sqrt(len(vals))), 2)
+        ncols = len(vals) // nrows
+    else:
+        return None
+    if nrows * ncols > len(vals) or nrows < 0 or ncols < 0:
+        raise ValueError(f"{path}: {len(vals)} values for {nrows} x {ncols}")
+    data = np.asarray(vals[:nrows * ncols], dtype=np.float64).reshape(nrows, ncols)[::-1].copy()
+    m = {"From File": path, "NbRows": str(nrows), "NbCols": str(ncols)}
+    m.update(meta)
+    return Image(data, 0, ncols, 0, nrows, m)
+
+
 def open_meas_file(path):
     """local_OpenMeasFile (``Source/sc_mainCons.cpp:1613-1652``): the reader
     for a measured-data file by its extension; returns (image, is_kws). A
     ``.dat``/``.csv``/``.txt`` with all three files of its base present is the
     program's own saved image; otherwise ``.tif``/``.tiff`` TIFF, ``.dat``/
-    ``.data`` KWS, ``.edf`` EDF, ``.spr`` spreadsheet. HDF5 and the 2D-SANS
-    formats (``.xml``, ``.csv``, ``.txt``) are not built (ValueError)."""
+    ``.data`` KWS, ``.edf`` EDF, ``.spr`` spreadsheet, ``.xml``/``.csv``/
+    ``.txt`` 2D-SANS (its XML form not built). HDF5 is not built
+    (ValueError)."""
     low = path.lower()
     if low.endswith((".dat", ".csv", ".txt")):
         base = _base(path)
@@ -576,6 +663,8 @@ def open_meas_file(path):
         return read_edf(path), False
     if low.endswith(".spr"):
         return read_spreadsheet(path), False
+    if low.endswith((".xml", ".csv", ".txt")):
+        return read_2dsans(path), False
     raise ValueError(f"{path}: no reader for this file type here")
 
 

@@ -35,7 +35,8 @@ static widImage *cs_add(int x0, int x1, int y0, int y1, double *d, QString title
 
 extern "C" {
 
-// kind: "kws", "edf", "spreadsheet", "sascrystal", "tiff"; null when the reader
+// kind: "kws", "edf", "spreadsheet", "sascrystal", "tiff", "2dsans" (its text
+// forms: the XML stand-in reads nothing); null when the reader
 // returns none
 void *ref_read_image(const char *kind, const char *fn) {
     const QString k(kind), f(fn);
@@ -44,6 +45,7 @@ void *ref_read_image(const char *kind, const char *fn) {
     if (k == "spreadsheet") return SC_ReadData::readImageSpreadsheet(cs_add, f);
     if (k == "sascrystal") return SC_ReadData::readImageSasCrystal(cs_add, f);
     if (k == "tiff") return SC_ReadData::readImageTiff(cs_add, f);
+    if (k == "2dsans") return SC_ReadData::readImage2dSans(cs_add, f);
     return nullptr;
 }
 

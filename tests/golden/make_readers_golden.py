@@ -152,6 +152,22 @@ def inputs():
     q = np.full(16 * 16, 7)
     q[40], q[41], q[60] = 0x22, 0, 0x22
     out["tiff_quote"] = ("tiff", "tiff_quote.tif", tiff_file(16, 8, data_off=256 + 20000 - 256, data=q))
+    rng = np.random.default_rng(16)
+    for name, fmt in (("2dsans_csv", "{:03d}"), ("2dsans_csv_blanks", "{:3d}")):
+        rows = ["A  ," + ",".join(f"{c}" for c in range(10))]
+        for r in range(6):
+            v = rng.uniform(0.0, 50.0, size=10)
+            rows.append(fmt.format(r) + "," + ",".join("nan" if (r, c) == (2, 3) else f"{x:.5f}"
+                                                      for c, x in enumerate(v)))
+        rows += ["", "000,9,9,9,9,9,9,9,9,9,9"]  # a second block: not read
+        out[name] = ("2dsans", name + ".csv", ("\n".join(rows) + "\n").encode())
+    hdr = ["Instrument: D22", "Date: 2024-03-01 12:00:00", "Data columns are Qx - Qy - I(Qx,Qy) - Err", "ASCII data"]
+    body = [f"{0.01 * i:.4f} {0.02 * i:.4f}\t{rng.uniform(1, 9):.6f} 0.1" for i in range(30)]
+    body.insert(5, "0.5 0.5")  # too short: skipped
+    body.insert(9, "0.5 0.5 x7 0.1")  # the intensity does not parse: 0
+    out["2dsans_dat"] = ("2dsans", "sans_ill.dat", ("\n".join(hdr + body) + "\n").encode())
+    out["2dsans_dat_no_i"] = ("2dsans", "sans_noi.dat", b"Data columns are Qx - Qy - Err\nASCII data\n1 2 3\n")
+    out["kws_to_2dsans"] = ("kws", "sans_via_kws.dat", ("\n".join(hdr + body) + "\n").encode())
     csv, txt = sascrystal_files(-4, 5, -3, 3, seed=6)
     out["sascrystal"] = ("sascrystal", "sascrystal.csv", csv.encode())
     out["sascrystal_txt"] = (None, "sascrystal.txt", txt.encode())

@@ -19,7 +19,7 @@ with open(os.path.join(GOLD, "readers_ref.json")) as f:
     REF = json.load(f)
 ARR = dict(np.load(os.path.join(GOLD, "readers_ref.npz")))
 READ = {"kws": R.read_kws, "edf": R.read_edf, "spreadsheet": R.read_spreadsheet,
-        "sascrystal": R.read_sascrystal_csv, "tiff": R.read_tiff}
+        "sascrystal": R.read_sascrystal_csv, "tiff": R.read_tiff, "2dsans": R.read_2dsans}
 
 
 def ours(kind, path):
