@@ -12,6 +12,7 @@ the same layout and metadata keys, so that a target can go straight to
 * KWS detector files (``Source/sc_readdata.cpp:655-876``);
 * EDF detector files (``Source/sc_readdata.cpp:1769-2121``);
 * SAXSLAB/Pilatus TIFF files (``Source/sc_readdata.cpp:24-520``);
+* 2D-SANS (ILL) images, text and XML (``Source/sc_readdata.cpp:1466-1767``);
 * spreadsheet text images (``Source/sc_readdata.cpp:2123-2190``);
 * the beam-stop centre finder (``SC_ReadData::findBeamCenter``,
   ``Source/sc_readdata.cpp:878-1010``).
@@ -554,6 +555,57 @@ def read_tiff(path):
     return Image(data, 0, ncols, 0, nrows, meta)
 
 
+def _2dsans_xml(path):
+    """The XML (canSAS-like) walk of readImage2dSans: rows = SASdata
+    elements, columns = the Idata elements before the second SASdata, values
+    = the I elements' text; ID, name, radiation and date texts become meta
+    information under the path of the enclosing elements (all but SASroot,
+    SASentry and Idata; an end tag removes its name and everything after it
+    from the path); Q, Idev and Qdev are skipped. None for a malformed
+    document or a value element with child elements (Qt's reader fails
+    there)."""
+    import xml.etree.ElementTree as ET
+    try:
+        root = ET.parse(path).getroot()
+    except ET.ParseError:
+        return None
+    loc = lambda t: t.rsplit("}", 1)[-1].split(":")[-1]  # noqa: E731
+    state = {"rows": 0, "cols": 0, "first": True, "path": [], "vals": [], "meta": {}, "bad": False}
+
+    def walk(e):
+        name = loc(e.tag)
+        if name == "SASdata":
+            state["rows"] += 1
+            if state["rows"] > 1:
+                state["first"] = False
+        elif name == "Idata" and state["first"]:
+            state["cols"] += 1
+        elif name in ("I", "ID", "name", "radiation", "date"):
+            if len(e):
+                state["bad"] = True
+                return False
+            text = e.text or ""
+            if name == "I":
+                state["vals"].append(_qt_double(text))
+            elif text:
+                state["meta"]["/".join(state["path"]) + "/" + name] = text
+            return True  # its end tag is consumed with the text
+        elif name not in ("Q", "Idev", "Qdev", "Idata", "SASroot", "SASentry"):
+            state["path"].append(name)
+        for c in e:
+            if not walk(c):
+                return False
+        if name in state["path"]:
+            while name in state["path"]:
+                state["path"].pop()
+        return True
+
+    walk(root)
+    if state["bad"]:
+        return None
+    return state["vals"], state["rows"], state["cols"], state["meta"]
+
+
 def read_2dsans(path):
     """A 2D-SANS (ILL) image (``Source/sc_readdata.cpp:1466-1767``) in its
     text forms:
@@ -572,17 +624,21 @@ def read_2dsans(path):
       does not parse, rows too short skipped); the image is sqrt(n) rows
       (at least 2) of n / rows columns.
 
-    Rows are stored bottom-up (file row r at y = rows - 1 - r). The XML form
-    is not built (ValueError); other extensions give None, as in the
-    reference. Data that do not fill rows x columns raise ValueError (the
-    reference reads past its buffer there)."""
+    * ``.xml``: see :func:`_2dsans_xml`.
+
+    Rows are stored bottom-up (file row r at y = rows - 1 - r). Other
+    extensions give None, as in the reference. Data that do not fill rows x
+    columns raise ValueError (the reference reads past its buffer there)."""
     low = path.lower()
-    if low.endswith(".xml"):
-        raise ValueError(f"{path}: the XML form of 2D-SANS files is not read here")
     meta = {}
     vals = []
     nrows = ncols = 0
-    if low.endswith(".csv"):
+    if low.endswith(".xml"):
+        r = _2dsans_xml(path)
+        if r is None:
+            return None
+        vals, nrows, ncols, meta = r
+    elif low.endswith(".csv"):
         with open(path, "rb") as f:
             raw = f.read().decode("latin-1")
         for line in raw.split("\n"):
@@ -646,8 +702,7 @@ def open_meas_file(path):
     ``.dat``/``.csv``/``.txt`` with all three files of its base present is the
     program's own saved image; otherwise ``.tif``/``.tiff`` TIFF, ``.dat``/
     ``.data`` KWS, ``.edf`` EDF, ``.spr`` spreadsheet, ``.xml``/``.csv``/
-    ``.txt`` 2D-SANS (its XML form not built). HDF5 is not built
-    (ValueError)."""
+    ``.txt`` 2D-SANS. HDF5 is not built (ValueError)."""
     low = path.lower()
     if low.endswith((".dat", ".csv", ".txt")):
         base = _base(path)

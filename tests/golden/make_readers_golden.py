@@ -168,6 +168,19 @@ def inputs():
     out["2dsans_dat"] = ("2dsans", "sans_ill.dat", ("\n".join(hdr + body) + "\n").encode())
     out["2dsans_dat_no_i"] = ("2dsans", "sans_noi.dat", b"Data columns are Qx - Qy - Err\nASCII data\n1 2 3\n")
     out["kws_to_2dsans"] = ("kws", "sans_via_kws.dat", ("\n".join(hdr + body) + "\n").encode())
+    x = ['<?xml version="1.0"?>', '<!-- canSAS-like 2D data -->',
+         '<SASroot xmlns="urn:cansas1d:1.1"><SASentry><Title>run 7</Title>',
+         '<SASsample><ID>sample A &amp; B</ID><name></name></SASsample>',
+         '<SASinstrument><SASsource><radiation>neutron</radiation></SASsource></SASinstrument>']
+    for r in range(4):
+        x.append("<SASdata>")
+        for c in range(5):
+            x.append(f"<Idata><Q>0.{r}{c}</Q><I> {rng.uniform(1, 9):.6f} </I><Idev>0.1</Idev></Idata>")
+        x.append("</SASdata>")
+    x.append("<SASnote><date>2024-03-01</date></SASnote></SASentry></SASroot>")
+    out["2dsans_xml"] = ("2dsans", "sans_cansas.xml", ("\n".join(x) + "\n").encode())
+    out["2dsans_xml_nested"] = ("2dsans", "sans_nested.xml",
+                                b"<SASroot><SASdata><Idata><I><v>1</v></I></Idata></SASdata></SASroot>\n")
     csv, txt = sascrystal_files(-4, 5, -3, 3, seed=6)
     out["sascrystal"] = ("sascrystal", "sascrystal.csv", csv.encode())
     out["sascrystal_txt"] = (None, "sascrystal.txt", txt.encode())
