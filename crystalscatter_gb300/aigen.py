@@ -137,7 +137,6 @@ class LibraryCalc:
         self.cs = cs
         self.mode = cs.CS_MODE_MIXED if mode is None else mode
         self.params = params if params is not None else cs.default_params()
-        self._keys = {}
 
     def update_param(self, key, value):
         c = self.cs.SasCalc_GENERIC_calculation()

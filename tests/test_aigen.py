@@ -3,7 +3,6 @@ generateAIfiles) on the CPU, with a stand-in calculation: settings and TPV
 lines, the reference's file names, the text images and the post-processing
 (noise, beam stop, detector lines, r-phi) in its order."""
 import math
-import os
 
 import numpy as np
 import pytest
