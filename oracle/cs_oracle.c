@@ -34,6 +34,7 @@
  *   calc_partCylinder_lattNone_ordisGauss         Source/sc_gpu_pCyl_lNon_oGau.h:15-100
  *   calc_partCylinder_lattNone_ordisZDir          Source/sc_gpu_pCyl_lNon_oZDi.h:17-88
  *   calc_partCylinder_peakGauss_lattBCT_ordisZDir Source/sc_gpu_pCyl_pGau_lBCT_oZDi.h:16-245
+ *   calc_GENERIC (restated combinations)          Source/sc_gpu_generic.h:27-881
  *   doCalculation (loops, quadrant mirroring)     Source/sc_calc_generic_cpu.cpp:1151-1275
  *   doFitCalculation (sum)                        Source/sc_calc_generic_cpu.cpp:1334-1443
  */
@@ -925,6 +926,126 @@ static void peak_sums(const cs_prepared *P, double qx, double qy, double qz, dou
     *intens = intensity;
 }
 
+/* calc_GENERIC's lattice factor, Source/sc_gpu_generic.h:511-846: the isotropic
+   peak sum with the isotropic width 1/uca, then the oriented peaks with the
+   selected peak shape (1 Lorentzian, 2 Gaussian, 3/4 modified Lorentzians,
+   5 pseudo-Voigt, 6 Pearson VII, 8 anisotropic Gaussian for perfect or
+   isotropic orientation; any other shape returns 0 for the pixel). Both sums
+   keep their last finite value when a term makes them infinite or NaN. The
+   twin's angle is normalised by q_hkl, not by the twin's own |q_hkl|.
+   Returns 0 when the shape has no branch. */
+static int peak_sums_generic(const cs_prepared *P, double qx, double qy, double qz, double q, double *radint,
+                             double *intens) {
+    const double c0 = 1.0; /* Source/sc_calc_generic_cpu.cpp:585 */
+    const double siglen = sqrt(sqr(P->sig[0]) + sqr(P->sig[1]) + sqr(P->sig[2]));
+    double width = 1;
+    if (P->debyescherrer) width = 4.0 / P->domainsize;
+    if (P->para) width = (4.0 / P->domainsize) + sqr(P->reldis) * P->dist * sqr(q);
+    if (P->lattice && P->shp == 8 && P->ordis == 7) width = siglen / 3.0;
+    width *= P->width_zuf;
+    const double widthiso = 1.0 / P->uca;
+    double radintensity = 0.0, intensity = 0.0;
+    for (int ii = 1; ii <= P->peakmax1; ii++) {
+        const double qhkl = P->latpar3[ii][5];
+        const double x2 = sqr(q - qhkl) / sqr(widthiso);
+        const double sq = exp(-4 * x2 / M_PI) / (M_PI * widthiso / 2.0);
+        const double keep = radintensity;
+        radintensity += sq * P->latpar1[ii][4] * P->latpar1[ii][5];
+        if (isinf(radintensity) || isnan(radintensity)) {
+            radintensity = keep;
+            break;
+        }
+    }
+    /* ax_k.length() * sig_k, Source/sc_calc_generic_cpu.cpp:396-398 */
+    const double a1n = sqrt(sqr(P->ax1[0]) + sqr(P->ax1[1]) + sqr(P->ax1[2])) * P->sig[0];
+    const double a2n = sqrt(sqr(P->ax2[0]) + sqr(P->ax2[1]) + sqr(P->ax2[2])) * P->sig[1];
+    const double a3n = sqrt(sqr(P->ax3[0]) + sqr(P->ax3[1]) + sqr(P->ax3[2])) * P->sig[2];
+    for (int ii = 1; ii <= P->peakmax2; ii++) {
+        const double qhkl = P->latpar3[ii][5];
+        if (qhkl <= 0 || isnan(qhkl)) continue;
+        const int mhkl = P->latpar2[ii][4], fhkl = P->latpar2[ii][5];
+        const double hx = P->latpar3[ii][2], hy = P->latpar3[ii][3], hz = P->latpar3[ii][4];
+        const double tx = P->latpar3[ii][7], ty = P->latpar3[ii][8], tz = P->latpar3[ii][9];
+        const double g3 = P->latpar3[ii][10];
+        const double pn1 = P->latpar3[ii][11];
+        double sq = 1.0, psiord = 1.0;
+        if (P->shp == 8) {
+            /* perfect orientation (ordis 6 or dbeta 0): a Gaussian ellipsoid
+               along the cell axes around the peak; isotropic: a radial
+               Gaussian of width |sig|/3 */
+            double term[2];
+            for (int t = 0; t < 2; t++) {
+                const double px = t ? tx : hx, py = t ? ty : hy, pz = t ? tz : hz;
+                if (P->ordis == 6 || fabs(P->dbeta) < EPS9) {
+                    const double dx = qx - px, dy = qy - py, dz = qz - pz;
+                    const double s1 = (dx * P->ax1[0] + dy * P->ax1[1] + dz * P->ax1[2]) / a1n;
+                    const double s2 = (dx * P->ax2[0] + dy * P->ax2[1] + dz * P->ax2[2]) / a2n;
+                    const double s3 = (dx * P->ax3[0] + dy * P->ax3[1] + dz * P->ax3[2]) / a3n;
+                    const double x2 = s1 * s1 + s2 * s2 + s3 * s3;
+                    term[t] = exp(-4 * x2 / M_PI) /
+                              (sqrt(M_PI * M_PI * M_PI) * P->sig[0] * P->sig[1] * P->sig[2] / 8.0);
+                } else {
+                    const double lw = siglen / 3.0;
+                    const double x2 = (q - qhkl) * (q - qhkl) / (lw * lw);
+                    term[t] = g3 * exp(-4 * x2 / M_PI) / (M_PI * lw / 2.0);
+                }
+            }
+            /* without a twin the peak's own term; with one, sq keeps 1 and is
+               mixed with the twin's term (:600-661) */
+            if (!P->twin) sq = term[0];
+            else sq = P->ceff * sq + (1 - P->ceff) * term[1];
+        } else {
+            if (P->shp < 1 || P->shp > 6) return 0;
+            const double x2 = (q - qhkl) * (q - qhkl) / (width * width);
+            const double cphi[2] = {(qx * hx + qy * hy + qz * hz) / (q * qhkl), (qx * tx + qy * ty + qz * tz) / (q * qhkl)};
+            double ord[2];
+            for (int t = 0; t < (P->twin ? 2 : 1); t++) {
+                const double y = myacos(cphi[t]);
+                const double b = 4 * q * q / sqr(P->phiwidth); /* b/c factors */
+                const double a = 4 * q * q / (M_PI * sqr(P->phiwidth)); /* a factor */
+                switch (P->shp) {
+                case 1: ord[t] = g3 / (pn1 * (1 + b * y * y)); break;
+                case 2: ord[t] = g3 * exp(-a * y * y) / pn1; break;
+                case 3: ord[t] = g3 / (pn1 * (1 + b * y * y) * (1 + b * y * y)); break;
+                case 4: ord[t] = g3 / (pn1 * exp(3 * log(1 + b * y * y) / 2.0)); break;
+                case 5: {
+                    const double e = P->pk_eta;
+                    ord[t] = g3 * (e * (1 / (1 + b * y * y)) + (1 - e) * exp(-a * y * y)) /
+                             (e * pn1 + (1 - e) * P->latpar3[ii][12]);
+                    break;
+                }
+                default: ord[t] = g3 / (pn1 * exp(P->pk_beta * log(1 + b * y * y))); break;
+                }
+            }
+            switch (P->shp) {
+            case 1: sq = sqrt(P->pk_c1) / (M_PI * width * (1.0 + P->pk_c1 * x2)); break;
+            case 2: sq = exp(-4 * x2 / M_PI) / (M_PI * width / 2.0); break;
+            case 3: sq = 2 * sqrt(P->pk_c2) / (M_PI * width * (1 + P->pk_c1 * x2) * (1 + P->pk_c1 * x2)); break;
+            case 4: sq = sqrt(P->pk_c3) / (2 * width * exp(3 * log(1 + P->pk_c1 * x2) / 2.0)); break;
+            case 5:
+                sq = P->pk_eta * sqrt(P->pk_c1) / (M_PI * width * (1 + P->pk_c1 * x2)) +
+                     (1 - P->pk_eta) * sqrt(c0) * exp(-c0 * x2) / (sqrt(M_PI) * width);
+                break;
+            default:
+                sq = ref_gamma(P->pk_beta) * P->pk_c4 * 2 /
+                     (ref_gamma(P->pk_beta - 0.5) * M_PI * width * exp(P->pk_beta * log(1 + 4 * P->pk_c4 * x2)));
+                break;
+            }
+            psiord = ord[0];
+            if (P->twin) psiord = P->ceff * psiord + (1 - P->ceff) * ord[1];
+        }
+        const double keep = intensity;
+        intensity += sq * mhkl * fhkl * psiord;
+        if (isinf(intensity) || isnan(intensity)) {
+            intensity = keep;
+            break;
+        }
+    }
+    *radint = radintensity;
+    *intens = intensity;
+    return 1;
+}
+
 /* ------------------------------------------------------- pixel functions */
 
 double oracle_pixel_q(const cs_prepared *P, double qx, double qy, double qz) {
@@ -1010,9 +1131,22 @@ double oracle_pixel_q(const cs_prepared *P, double qx, double qy, double qz) {
     }
     case CS_KEY_GENERIC:
         /* calc_GENERIC, Source/sc_gpu_generic.h:27-881, for the combinations
-           restated here: isotropic cylinders (cs 0/1), isotropic homogeneous
-           disks and homogeneous disks with the Gaussian orientation along an
-           axis, without a lattice (szq = szqiso = 1) */
+           restated here: homogeneous spheres on any lattice with the peak
+           shapes 1-8; without a lattice (szq = szqiso = 1) isotropic
+           cylinders (cs 0/1), isotropic homogeneous disks and homogeneous
+           disks with the Gaussian orientation along an axis */
+        if (P->particle == 0 && P->lattice) {
+            /* spheres, :44-58, on a lattice, :537-846 */
+            const double pq = formpq_partSphere(P, q);
+            const double fq = formfq_partSphere(P, q);
+            double radintensity, intensity;
+            if (!peak_sums_generic(P, qx, qy, qz, q, &radintensity, &intensity)) return 0.0;
+            const double sphno_cubevol = P->latpar[1] * P->latpar[2];
+            const double szqiso = (1 + (1) * (8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol) - 1) *
+                                           exp(-P->ucb * q * q));
+            const double szq = (1 + (fq / pq) * (2 * M_PI * intensity / (sphno_cubevol)-1) * exp(-P->dwfactor * q * q));
+            return P->base + P->izero * (szq * pq + P->iso * szqiso * pq) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
+        }
         if (P->particle == 1 && P->ordis == 7) {
             const double pq = formpq_partCylinder(P, qx, qy, q);
             return P->base + P->izero * (pq + P->iso * 1.0) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
@@ -1045,7 +1179,8 @@ int oracle_supported(const cs_prepared *P) {
     case CS_KEY_CYL_GAUSS_BCT_ZDIR:
     case CS_KEY_CUBE_NONE_ISO: return 1;
     case CS_KEY_GENERIC:
-        return !P->lattice && ((P->ordis == 7 && ((P->particle == 1 && (P->cs == 0 || P->cs == 1)) ||
+        if (P->particle == 0 && P->lattice && P->cs == 0) return 1;
+        return !P->lattice &&((P->ordis == 7 && ((P->particle == 1 && (P->cs == 0 || P->cs == 1)) ||
                                                   (P->particle == 2 && P->cs == 0))) ||
                                (P->ordis == 0 && P->particle == 2 && P->cs == 0 && P->orcase >= 1 &&
                                 P->orcase <= 3));

@@ -206,7 +206,7 @@ def main():
         img = r.image()
         # per-pixel conditioning of the reference computation: spread of the
         # (reference-pinned) oracle under one-ulp math-library perturbations;
-        # for the generic pixel function, which the oracle does not restate,
+        # for the generic combinations the oracle does not restate,
         # the spread of the reference's own probe build (oracle/ref_probe.c)
         P0 = cpu_oracle.prepare(p, ign)
         if ins == 0 and cpu_oracle.supported(P0):
