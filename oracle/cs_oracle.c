@@ -1046,6 +1046,17 @@ static int peak_sums_generic(const cs_prepared *P, double qx, double qy, double 
     return 1;
 }
 
+/* szq and szqiso of calc_GENERIC on a lattice, :848-851, from the peak sums */
+static int lattice_factors_generic(const cs_prepared *P, double qx, double qy, double qz, double q, double pq, double fq,
+                                   double *szq, double *szqiso) {
+    double radintensity, intensity;
+    if (!peak_sums_generic(P, qx, qy, qz, q, &radintensity, &intensity)) return 0;
+    const double sphno_cubevol = P->latpar[1] * P->latpar[2];
+    *szqiso = (1 + (1) * (8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol) - 1) * exp(-P->ucb * q * q));
+    *szq = (1 + (fq / pq) * (2 * M_PI * intensity / (sphno_cubevol)-1) * exp(-P->dwfactor * q * q));
+    return 1;
+}
+
 /* ------------------------------------------------------- pixel functions */
 
 double oracle_pixel_q(const cs_prepared *P, double qx, double qy, double qz) {
@@ -1131,21 +1142,44 @@ double oracle_pixel_q(const cs_prepared *P, double qx, double qy, double qz) {
     }
     case CS_KEY_GENERIC:
         /* calc_GENERIC, Source/sc_gpu_generic.h:27-881, for the combinations
-           restated here: homogeneous spheres on any lattice with the peak
-           shapes 1-8; without a lattice (szq = szqiso = 1) isotropic
-           cylinders (cs 0/1), isotropic homogeneous disks and homogeneous
-           disks with the Gaussian orientation along an axis */
+           restated here: homogeneous spheres and homogeneous z-direction
+           cylinders on any lattice with the peak shapes 1-8; without a
+           lattice (szq = szqiso = 1) isotropic cylinders (cs 0/1), isotropic
+           homogeneous disks and homogeneous disks with the Gaussian
+           orientation along an axis */
         if (P->particle == 0 && P->lattice) {
-            /* spheres, :44-58, on a lattice, :537-846 */
+            /* spheres, :44-58, on a lattice */
             const double pq = formpq_partSphere(P, q);
             const double fq = formfq_partSphere(P, q);
-            double radintensity, intensity;
-            if (!peak_sums_generic(P, qx, qy, qz, q, &radintensity, &intensity)) return 0.0;
-            const double sphno_cubevol = P->latpar[1] * P->latpar[2];
-            const double szqiso = (1 + (1) * (8 * M_PI * M_PI * M_PI * radintensity / (4 * M_PI * sphno_cubevol) - 1) *
-                                           exp(-P->ucb * q * q));
-            const double szq = (1 + (fq / pq) * (2 * M_PI * intensity / (sphno_cubevol)-1) * exp(-P->dwfactor * q * q));
+            double szq, szqiso;
+            if (!lattice_factors_generic(P, qx, qy, qz, q, pq, fq, &szq, &szqiso)) return 0.0;
             return P->base + P->izero * (szq * pq + P->iso * szqiso * pq) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
+        }
+        if (P->particle == 1 && P->ordis == 6 && P->lattice) {
+            /* z-direction cylinders, :318-353, on a lattice (pqiso stays 1) */
+            double pq = 0, fq = 0;
+            switch (P->orcase) {
+            case CS_ORC_GENERAL:
+                pq = formpq_partCylinder(P, qx * P->cosphi * P->sintheta, qy * P->sinphi * P->sintheta, q);
+                fq = formfq_partCylinder(P, sqrt(P->cosphi * qx * qx + P->sinphi * qy * qy + EPS9),
+                                         qx * P->cosphi * P->sintheta, qy * P->sinphi * P->sintheta, q);
+                break;
+            case CS_ORC_XAXIS:
+                pq = formpq_partCylinder(P, qx, 0, q);
+                fq = formfq_partCylinder(P, fabs(qx), qx, 0, q);
+                break;
+            case CS_ORC_YAXIS:
+                pq = formpq_partCylinder(P, 0, qy, q);
+                fq = formfq_partCylinder(P, fabs(qy), 0, qy, q);
+                break;
+            default:
+                pq = formpq_partCylinder(P, qx, qy, q);
+                fq = formfq_partCylinder(P, q, qx, qy, q);
+                break;
+            }
+            double szq, szqiso;
+            if (!lattice_factors_generic(P, qx, qy, qz, q, pq, fq, &szq, &szqiso)) return 0.0;
+            return P->base + P->izero * (szq * pq + P->iso * szqiso * 1.0) + P->ifluc / (1 + q * q * P->rfluc * P->rfluc);
         }
         if (P->particle == 1 && P->ordis == 7) {
             const double pq = formpq_partCylinder(P, qx, qy, q);
@@ -1179,7 +1213,7 @@ int oracle_supported(const cs_prepared *P) {
     case CS_KEY_CYL_GAUSS_BCT_ZDIR:
     case CS_KEY_CUBE_NONE_ISO: return 1;
     case CS_KEY_GENERIC:
-        if (P->particle == 0 && P->lattice && P->cs == 0) return 1;
+        if (P->lattice && P->cs == 0 && (P->particle == 0 || (P->particle == 1 && P->ordis == 6))) return 1;
         return !P->lattice &&((P->ordis == 7 && ((P->particle == 1 && (P->cs == 0 || P->cs == 1)) ||
                                                   (P->particle == 2 && P->cs == 0))) ||
                                (P->ordis == 0 && P->particle == 2 && P->cs == 0 && P->orcase >= 1 &&
